@@ -1,0 +1,429 @@
+"""Benchmark: AMIPS + envelope queries/s on the isolated FP64 query batches.
+
+Workload (one step): 4,000,000 tets from regular tets of edge 0.01 in the
+unit cube, every vertex perturbed by N(0, 0.1 edge): orientation + AMIPS
+energy (calTetQuality_AMIPS sentinel), gradient and Hessian; plus
+10,000,000 points offset along the normal by U(-2 eps, 2 eps) around a
+100,000-triangle displaced sphere, eps = 1e-3: squared distance <= eps^2.
+A query is one tet E+J+H evaluation or one point-envelope decision, so a
+step is 14,000,000 queries.  Inputs are seeded synthetic data of those
+shapes (no dataset is available); all inputs exceed the 129 MB L2.
+
+``value`` times the device-resident kernels (inputs already in HBM);
+``e2e`` times the same step through the C-ABI with host buffers (pinned),
+host<->device copies included.  ``--impl reference`` times the reference's
+own CPU code (oracle/_ref) on a bounded sample with all host threads.
+
+Multi-GPU: the queries are independent and every box has one GPU, so
+``--gpus N`` under torchrun runs N replicas (weak scaling) with a barrier and
+the max over ranks; there is no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_TETS = 4_000_000
+N_POINTS = 10_000_000
+EPS = 1e-3
+METRIC = "AMIPS+envelope queries/s (plain FP64, 0 decision mismatches)"
+UNIT = "queries/s"
+BYTES_PER_TET = 96 + 8 + 24 + 72 + 1     # coords in; E, J, H, flip out
+BYTES_PER_POINT = 24 + 1                 # point in; decision out
+# The CPU legs time the whole step's work (about 1 us per query and thread
+# on the host cores, so a few seconds with all threads).
+CPU_SAMPLE_TETS = N_TETS
+CPU_SAMPLE_POINTS = N_POINTS
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [x.strip() for x in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_inputs(seed=0):
+    from tetwild_gb300 import synthetic as syn
+
+    T = syn.energy_batch(N_TETS, seed=seed)
+    V, F = syn.displaced_sphere(seed=seed)
+    P = syn.envelope_points(V, F, N_POINTS, EPS, seed=seed + 1)
+    return T, V, F, P
+
+
+def cpu_baseline(T, V, F, P, nthreads):
+    """The reference's own CPU code when oracle/_ref is built, else the oracle port,
+    on a bounded sample (CPU_SAMPLE_TETS tets + CPU_SAMPLE_POINTS points)."""
+    from oracle.oracle import Oracle, RefLib
+
+    Ts = np.ascontiguousarray(T[:, :CPU_SAMPLE_TETS])
+    Ps = np.ascontiguousarray(P[:CPU_SAMPLE_POINTS])
+    kind = "port"
+    try:
+        ref = RefLib()
+        kind = "reference"
+    except Exception:
+        ref = None
+    o = Oracle()
+    if kind == "reference":
+        S = ref.surface(V, F)
+        t0 = time.perf_counter()
+        ref.amips_batch_soa(Ts, nthreads=nthreads)
+        o.amips_batch_soa(Ts, quality=True, nthreads=nthreads, jacobian=False, hessian=False)
+        S.points_out(Ps, EPS * EPS, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        sample = (f"{CPU_SAMPLE_TETS} tets (reference comformalAMIPS E/J/H + oracle exact orientation) "
+                  f"+ {CPU_SAMPLE_POINTS} points (reference isPointOutEnvelop over MeshFacetsAABBWithEps)")
+    else:
+        S = o.surface(V, F)
+        t0 = time.perf_counter()
+        o.amips_batch_soa(Ts, quality=True, nthreads=nthreads)
+        S.points_out(Ps, EPS * EPS, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        sample = f"{CPU_SAMPLE_TETS} tets E/J/H + {CPU_SAMPLE_POINTS} points (oracle port)"
+    q = CPU_SAMPLE_TETS + CPU_SAMPLE_POINTS
+    return {"value": q / dt, "unit": UNIT, "cores": nthreads, "kind": kind, "sample": sample,
+            "seconds": dt}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle.oracle import default_threads
+
+    T, V, F, P = make_inputs()
+    nthreads = default_threads()
+    for _ in range(args.warmup):
+        cpu_baseline(T, V, F, P, nthreads)
+    times = []
+    kind = sample = None
+    for _ in range(args.steps):
+        r = cpu_baseline(T, V, F, P, nthreads)
+        times.append(r["seconds"])
+        kind, sample = r["kind"], r["sample"]
+    q = CPU_SAMPLE_TETS + CPU_SAMPLE_POINTS
+    total = sum(times)
+    value = q * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "isolated query batches, FP64 plain: energy 4M tets E/J/H + envelope "
+                               "10M points vs 100k-tri displaced sphere (bounded CPU sample per step)",
+                   "sample_tets": CPU_SAMPLE_TETS, "sample_points": CPU_SAMPLE_POINTS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def run_ours(args):
+    import torch
+
+    import tetwild_gb300 as tw
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    T, V, F, P = make_inputs(seed=rank)
+    ctx = tw.Context(dev)
+    ctx.set_params(EPS * EPS, EPS)
+    ctx.surface_upload(V, F)
+    fp64_tflops, fp32_tflops = ctx.probe_peaks()
+
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=f"cuda:{dev}")
+    d = torch.device(f"cuda:{dev}")
+    dT = torch.from_numpy(T).to(d)
+    dP = torch.from_numpy(P).to(d)
+    dE = torch.empty(N_TETS, dtype=torch.float64, device=d)
+    dJ = torch.empty(3 * N_TETS, dtype=torch.float64, device=d)
+    dH = torch.empty(9 * N_TETS, dtype=torch.float64, device=d)
+    dFl = torch.empty(N_TETS, dtype=torch.uint8, device=d)
+    dO = torch.empty(N_POINTS, dtype=torch.uint8, device=d)
+    torch.cuda.synchronize()
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        ctx.amips_device(dT.data_ptr(), N_TETS, tw.TW_ENERGY_QUALITY, dE.data_ptr(), dJ.data_ptr(),
+                         dH.data_ptr(), dFl.data_ptr())
+        if ev:
+            ev[1].record(stream)
+        ctx.envelope_points_device(dP.data_ptr(), N_POINTS, dO.data_ptr())
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+
+    # correctness gate on this very workload: a sample of each output vs the oracle
+    mism = check_sample(T, P, V, F, dE, dFl, dO)
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step(evs[k])
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    t_amips = [evs[k][0].elapsed_time(evs[k][1]) for k in range(args.steps)]
+    t_env = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
+    step_ms = [a + b for a, b in zip(t_amips, t_env)]
+    dev_ms = sum(step_ms)
+    dev_ms = max_over_ranks(dev_ms, ws)
+    q_step = N_TETS + N_POINTS
+    value = ws * q_step * args.steps / (dev_ms * 1e-3)
+
+    # e2e: the same step through the C-ABI with pinned host buffers
+    e2e = run_e2e(ctx, T, P, args, ws)
+
+    hbm_peak, peak_kind = measured_peaks()
+    ma, me = statistics.mean(t_amips), statistics.mean(t_env)
+    if me >= ma:
+        dom = {"kernel": "k_env_points", "ms": me, "bytes": BYTES_PER_POINT * N_POINTS,
+               "units": N_POINTS, "per_unit": BYTES_PER_POINT}
+    else:
+        dom = {"kernel": "k_amips_soa", "ms": ma, "bytes": BYTES_PER_TET * N_TETS,
+               "units": N_TETS, "per_unit": BYTES_PER_TET}
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+    traffic = load_traffic().get(dom["kernel"])
+    traffic_bytes = None
+    if traffic and traffic.get("bytes_per_unit"):
+        traffic_bytes = traffic["bytes_per_unit"] * dom["units"]
+    flops_per_tet = 260.0   # FP64 operations per tet (orientation filter + E/J/H), static count
+    fp64_achieved = flops_per_tet * N_TETS / (ma * 1e-3) / 1e12
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "isolated query batches, FP64 plain: energy 4M tets "
+                               "(orientation + AMIPS E/J/H) + envelope 10M points vs a 100k-tri "
+                               "displaced sphere, eps=1e-3",
+                   "tets": N_TETS, "points": N_POINTS, "surface_tris": int(len(F)),
+                   "l2": "inputs larger than L2 (384 MB tets, 240 MB points); no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
+        "kernels_ms": {"k_amips_soa": ma, "k_env_points": me},
+        "decision_mismatches": mism,
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": traffic_bytes, "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_unit": dom["per_unit"]},
+        "fp64_pipe": {"kernel": "k_amips_soa", "achieved_tflops": fp64_achieved,
+                      "peak_tflops_measured": fp64_tflops, "frac": fp64_achieved / fp64_tflops,
+                      "flops_per_tet": flops_per_tet, "fp32_peak_tflops_measured": fp32_tflops},
+        "e2e": e2e,
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle.oracle import default_threads
+
+        line["cpu_baseline"] = cpu_baseline(T, V, F, P, default_threads())
+        line["cpu_baseline"].pop("seconds", None)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def check_sample(T, P, V, F, dE, dFl, dO, n=20000):
+    """Decision mismatches vs the oracle on a strided sample of this step's outputs."""
+    from oracle.oracle import Oracle, default_threads
+
+    o = Oracle()
+    idx = np.linspace(0, N_TETS - 1, n).astype(np.int64)
+    Ts = np.ascontiguousarray(T[:, idx])
+    E, _, _, Fo = o.amips_batch_soa(Ts, quality=True, nthreads=default_threads(), jacobian=False,
+                                    hessian=False)
+    gE = dE.cpu().numpy()[idx]
+    gF = dFl.cpu().numpy()[idx]
+    pidx = np.linspace(0, N_POINTS - 1, n).astype(np.int64)
+    Po = o.surface(V, F).points_out(np.ascontiguousarray(P[pidx]), EPS * EPS,
+                                    nthreads=default_threads())
+    gO = dO.cpu().numpy()[pidx]
+    return {"sampled": 2 * n, "flip": int((gF != Fo).sum()), "energy_bits": int((gE != E).sum()),
+            "envelope": int((gO != Po).sum())}
+
+
+def run_e2e(ctx, T, P, args, ws):
+    import tetwild_gb300 as tw
+
+    hT = tw.PinnedArray(T.shape, np.float64)
+    hT.array[...] = T
+    hP = tw.PinnedArray(P.shape, np.float64)
+    hP.array[...] = P
+    oE = tw.PinnedArray((N_TETS,), np.float64)
+    oJ = tw.PinnedArray((3, N_TETS), np.float64)
+    oH = tw.PinnedArray((9, N_TETS), np.float64)
+    oF = tw.PinnedArray((N_TETS,), np.uint8)
+    oO = tw.PinnedArray((N_POINTS,), np.uint8)
+    lib, h = ctx.lib, ctx.h
+
+    def step():
+        st = lib.tw_amips_soa(h, hT.array.ctypes.data, N_TETS, tw.TW_ENERGY_QUALITY,
+                              oE.array.ctypes.data, oJ.array.ctypes.data, oH.array.ctypes.data,
+                              oF.array.ctypes.data)
+        assert st == 0, st
+        st = lib.tw_envelope_points(h, hP.array.ctypes.data, N_POINTS, tw.TW_SURFACE_INPUT,
+                                    oO.array.ctypes.data)
+        assert st == 0, st
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    dt = max_over_ranks(dt, ws)
+    for a in (hT, hP, oE, oJ, oH, oF, oO):
+        a.free()
+    q = (N_TETS + N_POINTS) * args.steps * ws
+    return {"value": q / dt, "unit": UNIT, "h2d_bytes_per_step": 96 * N_TETS + 24 * N_POINTS,
+            "d2h_bytes_per_step": (8 + 24 + 72 + 1) * N_TETS + N_POINTS,
+            "ms_per_step": 1e3 * dt / args.steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,156 @@
+/*
+ * tw_gb300.h -- C-ABI of the GB300 (sm_103a) implementation of TetWild's
+ * mesh-optimisation query path: conformal-AMIPS energy/gradient/Hessian,
+ * exact tet-inversion checks, the sampled envelope test and the Newton
+ * vertex-smoothing step.
+ *
+ * The reference exposes these as C++ member functions of LocalOperations and
+ * VertexSmoother, switched at compile time between the scalar code and the
+ * ISPC kernel (TETWILD_WITH_ISPC, LocalOperations.h:21-23).  Each entry point
+ * below names the reference routine it replaces; a TetWild build binds them
+ * behind the same switch.
+ *
+ * Conventions
+ *  - Every call returns an int status: TW_OK (0), a negative error code, or
+ *    TW_NEEDS_EXACT_HOST (1) when part of a result must come from the host's
+ *    exact-rational state (tets with unrounded vertices, LocalOperations.cpp
+ *    :546-548).  tw_last_error() gives a message for the last failure.
+ *  - Pointers are host pointers unless the function name ends in _device;
+ *    _device calls take device pointers and are asynchronous on the
+ *    context's stream (tw_stream()).  Host calls are synchronous.
+ *  - A context belongs to one device and one stream; distinct contexts may be
+ *    used from distinct threads.
+ *  - Coordinates are binary64.  Decisions (signs, in/out, accept/reject) are
+ *    exact or bit-identical to the CPU oracle; energies, gradients and
+ *    Hessians agree with the reference expressions to 1e-12 relative.
+ */
+#ifndef TW_GB300_H
+#define TW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__) || defined(__clang__)
+#define TW_API __attribute__((visibility("default")))
+#else
+#define TW_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TW_OK 0
+#define TW_NEEDS_EXACT_HOST 1
+#define TW_ERR_ARG (-1)
+#define TW_ERR_CUDA (-2)
+#define TW_ERR_OOM (-3)          /* device allocation failed or budget exceeded */
+#define TW_ERR_NO_SURFACE (-4)
+#define TW_ERR_NO_MESH (-5)
+#define TW_ERR_TIMEOUT (-6)
+
+/* AMIPS output modes */
+#define TW_ENERGY_RAW 0          /* comformalAMIPSEnergy_new value            */
+#define TW_ENERGY_QUALITY 1      /* calTetQuality_AMIPS value (1e50 sentinel) */
+
+/* surfaces */
+#define TW_SURFACE_INPUT 0       /* geo_sf_tree (MeshRefinement.cpp:209)      */
+#define TW_SURFACE_BOUNDARY 1    /* geo_b_tree  (MeshRefinement.cpp:213)      */
+
+typedef struct tw_ctx tw_ctx;
+
+/* ---- context --------------------------------------------------------------
+ * Replaces: the LocalOperations constructor's state (LocalOperations.h:56-64)
+ * and State's eps_2 / sampling_dist (State.h:41-43, State.cpp:34-40).     */
+TW_API int tw_ctx_create(int device, size_t hbm_budget_bytes, tw_ctx** out);
+TW_API int tw_ctx_destroy(tw_ctx* ctx);
+TW_API const char* tw_last_error(const tw_ctx* ctx);
+/* newton_max_step / newton_max_it: MAX_STEP=15, MAX_IT=20 in the reference
+ * (VertexSmoother.cpp:469-470).                                             */
+TW_API int tw_set_params(tw_ctx* ctx, double eps_2, double sampling_dist, int newton_max_step,
+                  int newton_max_it);
+TW_API int tw_stream(tw_ctx* ctx, void** cuda_stream);
+TW_API int tw_synchronize(tw_ctx* ctx);
+/* Device bytes currently held by the context (mesh, surfaces, scratch).   */
+TW_API int tw_memory_used(const tw_ctx* ctx, size_t* bytes);
+
+/* ---- AMIPS energy / gradient / Hessian -------------------------------------
+ * Replaces: LocalOperations::comformalAMIPSEnergy_new (LocalOperations.cpp:28,
+ * decl LocalOperations.h:109), comformalAMIPSJacobian_new (:83, decl :110),
+ * comformalAMIPSHessian_new (:149, decl :111), the ISPC batch energy_ispc
+ * (energy.ispc:7) and the per-tet body of calTetQualities (:695-773).
+ * T: SoA [12][n] doubles (the energy_ispc layout: v0x[n] v0y[n] ... v3z[n]).
+ * E [n], J SoA [3][n], H SoA [9][n] (row-major 3x3 per tet), flip [n]
+ * (1 = orientation not POSITIVE, isTetFlip on rounded coordinates).  Any
+ * output may be NULL.  mode: TW_ENERGY_RAW or TW_ENERGY_QUALITY.           */
+TW_API int tw_amips_soa(tw_ctx* ctx, const double* T, int64_t n, int mode, double* E, double* J,
+                 double* H, uint8_t* flip);
+TW_API int tw_amips_soa_device(tw_ctx* ctx, const double* T, int64_t n, int mode, double* E,
+                        double* J, double* H, uint8_t* flip);
+
+/* ---- resident mesh -----------------------------------------------------------
+ * The tet-mesh vertex array (TetVertex::posf / is_rounded,
+ * TetmeshElements.h:24-64) kept in HBM for index-based queries.
+ * xyz: [nv][3] doubles; rounded: [nv] (NULL = all rounded).                 */
+TW_API int tw_mesh_upload(tw_ctx* ctx, const double* xyz, int32_t nv, const uint8_t* rounded);
+TW_API int tw_mesh_update_vertices(tw_ctx* ctx, const int32_t* ids, const double* xyz,
+                            const uint8_t* rounded, int32_t n);
+
+/* Replaces: LocalOperations::calTetQualities (LocalOperations.cpp:695, decl
+ * LocalOperations.h:69) and isTetFlip / isFlip (:535-573, decl :77-79).
+ * tets: [n][4] vertex ids into the resident mesh.  energy[n] gets the
+ * calTetQuality_AMIPS value, flip[n] the isTetFlip value; either may be NULL.
+ * Tets with an unrounded vertex get needs_host[i] = 1 (if non-NULL) and the
+ * call returns TW_NEEDS_EXACT_HOST: their orientation must come from the
+ * host's exact coordinates (LocalOperations.cpp:546-548).                  */
+TW_API int tw_tet_quality(tw_ctx* ctx, const int32_t* tets, int64_t n, double* energy, uint8_t* flip,
+                   uint8_t* needs_host);
+TW_API int tw_tet_quality_device(tw_ctx* ctx, const int32_t* tets, int64_t n, double* energy,
+                          uint8_t* flip, uint8_t* needs_host);
+
+/* ---- envelope -----------------------------------------------------------------
+ * Replaces: the MeshFacetsAABBWithEps constructor (mesh_AABB.cpp:356-379):
+ * builds an LBVH over the surface on the device.  V: [nv][3], F: [nf][3].   */
+TW_API int tw_surface_upload(tw_ctx* ctx, const double* V, int32_t nv, const int32_t* F, int32_t nf,
+                      int which);
+/* Replaces: LocalOperations::isPointOutEnvelop (LocalOperations.cpp:1034,
+ * decl LocalOperations.h:98) and isPointOutBoundaryEnvelop (:1111, decl :100)
+ * for which = TW_SURFACE_BOUNDARY.  P: [n][3]; out[i] = 1 iff the squared
+ * distance from P[i] to the surface exceeds eps_2.                          */
+TW_API int tw_envelope_points(tw_ctx* ctx, const double* P, int64_t n, int which, uint8_t* out);
+TW_API int tw_envelope_points_device(tw_ctx* ctx, const double* P, int64_t n, int which, uint8_t* out);
+/* Replaces: LocalOperations::isFaceOutEnvelop / isFaceOutEnvelop_sampling
+ * (LocalOperations.cpp:967, :1046; decl LocalOperations.h:97,99) with
+ * sampleTriangle (Common.cpp:143).  tris: [n][9] (three vertices).
+ * out[i] = 0 for a degenerate triangle, else 1 iff some sample is out.     */
+TW_API int tw_envelope_faces(tw_ctx* ctx, const double* tris, int64_t n, uint8_t* out);
+TW_API int tw_envelope_faces_device(tw_ctx* ctx, const double* tris, int64_t n, uint8_t* out);
+/* sampleTriangle (Common.cpp:143-228) evaluated on the device for one
+ * triangle: writes min(count, cap) samples [..][3] to out (host) and the
+ * full count to *count.  For checking the device sampling arithmetic.     */
+TW_API int tw_sample_triangle(tw_ctx* ctx, const double* tri9, double sampling_dist, double* out,
+                       int64_t cap, int64_t* count);
+
+/* ---- Newton smoothing ---------------------------------------------------------
+ * Replaces: VertexSmoother::NewtonsMethod (VertexSmoother.cpp:465, decl
+ * VertexSmoother.h:28) with NewtonsUpdate (:627) and getNewEnergy (:544),
+ * for a batch of independent one-ring stars over the resident mesh.
+ * star_off: [nstars+1] offsets into tets ([.][4] ids, each star's tets in
+ * the caller's order, which fixes the summation order); centers: [nstars]
+ * vertex ids.  out: [nstars][3] new position, moved: [nstars] is_moved.    */
+TW_API int tw_newton_stars(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                    const int32_t* centers, int32_t nstars, double* out, uint8_t* moved);
+
+/* ---- pinned host memory for fast copies --------------------------------------- */
+TW_API int tw_host_alloc(size_t bytes, void** out);
+TW_API int tw_host_free(void* p);
+
+/* ---- measured pipe peaks (roofline denominators) ------------------------------
+ * Times a dependent-FMA loop over the whole GPU and returns FP64 and FP32
+ * FMA throughput in TFLOP/s (2 flops per FMA).                              */
+TW_API int tw_probe_peaks(tw_ctx* ctx, double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TW_GB300_H */

@@ -1,0 +1,255 @@
+"""ctypes wrappers for the CPU oracle (libtw_oracle.so) and for the
+reference's own code compiled into oracle/_ref/libtwref.so.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline / reference legs of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "libtw_oracle.so"
+REF_SO = HERE / "_ref" / "libtwref.so"
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return ORACLE_SO
+
+
+def build_ref() -> Path | None:
+    """Slice (when the reference checkout is present) and compile oracle/_ref."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("tw_build_ref", HERE / "ref" / "build_ref.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.do_slice()
+    return mod.do_compile()
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def default_threads() -> int:
+    return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
+
+
+class Oracle:
+    """The CPU restatement (oracle/tw_oracle.c)."""
+
+    def __init__(self):
+        if not ORACLE_SO.exists():
+            build_oracle()
+        L = ctypes.CDLL(str(ORACLE_SO))
+        sig = {
+            "two_icbrt": ([_D], _D),
+            "two_amips_energy": ([_P], _D),
+            "two_amips_jacobian": ([_P, _P], None),
+            "two_amips_hessian": ([_P, _P], None),
+            "two_orient3d": ([_P, _P, _P, _P], _I),
+            "two_orient3d_exact": ([_P, _P, _P, _P], _I),
+            "two_collinear": ([_P, _P, _P], _I),
+            "two_tet_quality": ([_P], _D),
+            "two_tet_flip": ([_P], _I),
+            "two_point_triangle_sqdist": ([_P, _P, _P, _P, _P], _D),
+            "two_sample_triangle": ([_P, _D, _P, _I64], _I64),
+            "two_sample_count": ([_P, _D], _I64),
+            "two_surface_build": ([_P, _I32, _P, _I32], _P),
+            "two_surface_free": ([_P], None),
+            "two_point_out": ([_P, _P, _D], _I),
+            "two_point_out_brute": ([_P, _P, _D], _I),
+            "two_face_out": ([_P, _P, _D, _D], _I),
+            "two_qr_solve3": ([_P, _P, _P], _I),
+            "two_newton_star": ([_P, _P, _I32, _I32, _I, _I, _P], _I),
+            "two_amips_batch_soa": ([_P, _I64, _I, _P, _P, _P, _P, _I], None),
+            "two_points_out_batch": ([_P, _P, _I64, _D, _P, _I], None),
+            "two_faces_out_batch": ([_P, _P, _I64, _D, _D, _P, _I], None),
+            "two_newton_stars_batch": ([_P, _P, _P, _P, _I64, _I, _I, _P, _P, _I], None),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        self.L = L
+
+    # scalar helpers
+    def icbrt(self, x: float) -> float:
+        return self.L.two_icbrt(x)
+
+    def orient3d(self, p, q, r, s) -> int:
+        a = [_c(v, np.float64) for v in (p, q, r, s)]
+        return self.L.two_orient3d(*[_p(v) for v in a])
+
+    def orient3d_exact(self, p, q, r, s) -> int:
+        a = [_c(v, np.float64) for v in (p, q, r, s)]
+        return self.L.two_orient3d_exact(*[_p(v) for v in a])
+
+    def collinear(self, a, b, c) -> int:
+        v = [_c(x, np.float64) for x in (a, b, c)]
+        return self.L.two_collinear(*[_p(x) for x in v])
+
+    def point_triangle_sqdist(self, p, a, b, c) -> float:
+        v = [_c(x, np.float64) for x in (p, a, b, c)]
+        return self.L.two_point_triangle_sqdist(*[_p(x) for x in v], None)
+
+    def qr_solve3(self, H, b):
+        Hm = _c(H, np.float64).reshape(9)
+        bb = _c(b, np.float64)
+        x = np.empty(3)
+        self.L.two_qr_solve3(_p(Hm), _p(bb), _p(x))
+        return x
+
+    def sample_triangle(self, tri9, sd):
+        t = _c(tri9, np.float64).reshape(9)
+        n = self.L.two_sample_count(_p(t), sd)
+        out = np.empty((max(n, 1), 3))
+        self.L.two_sample_triangle(_p(t), sd, _p(out), n)
+        return out[:n]
+
+    # batches
+    def amips_batch_soa(self, T, quality=True, nthreads=1, energy=True, jacobian=True,
+                        hessian=True, flip=True):
+        T = _c(T, np.float64)
+        n = T.shape[1]
+        E = np.empty(n) if energy else None
+        J = np.empty((3, n)) if jacobian else None
+        H = np.empty((9, n)) if hessian else None
+        F = np.empty(n, np.uint8) if flip else None
+        self.L.two_amips_batch_soa(_p(T), n, 1 if quality else 0, _p(E), _p(J), _p(H), _p(F),
+                                   nthreads)
+        return E, J, H, F
+
+    def surface(self, V, F):
+        return OracleSurface(self, V, F)
+
+    def newton_stars(self, xyz, star_off, tets, centers, max_step=15, max_it=20, nthreads=1):
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        C = _c(centers, np.int32)
+        ns = C.size
+        out = np.empty((ns, 3))
+        moved = np.empty(ns, np.uint8)
+        self.L.two_newton_stars_batch(_p(X), _p(O), _p(T), _p(C), ns, max_step, max_it, _p(out),
+                                      _p(moved), nthreads)
+        return out, moved
+
+
+class OracleSurface:
+    def __init__(self, o: Oracle, V, F):
+        self.o = o
+        self.V = _c(V, np.float64).reshape(-1, 3)
+        self.F = _c(F, np.int32).reshape(-1, 3)
+        self.h = o.L.two_surface_build(_p(self.V), self.V.shape[0], _p(self.F), self.F.shape[0])
+
+    def __del__(self):
+        try:
+            self.o.L.two_surface_free(self.h)
+        except Exception:
+            pass
+
+    def points_out(self, P, eps2, nthreads=1):
+        X = _c(P, np.float64).reshape(-1, 3)
+        out = np.empty(X.shape[0], np.uint8)
+        self.o.L.two_points_out_batch(self.h, _p(X), X.shape[0], eps2, _p(out), nthreads)
+        return out
+
+    def point_out_brute(self, p, eps2) -> int:
+        x = _c(p, np.float64)
+        return self.o.L.two_point_out_brute(self.h, _p(x), eps2)
+
+    def faces_out(self, tris, eps2, sd, nthreads=1):
+        X = _c(tris, np.float64).reshape(-1, 9)
+        out = np.empty(X.shape[0], np.uint8)
+        self.o.L.two_faces_out_batch(self.h, _p(X), X.shape[0], eps2, sd, _p(out), nthreads)
+        return out
+
+
+class RefLib:
+    """The reference's own code (oracle/_ref/libtwref.so)."""
+
+    def __init__(self):
+        if not REF_SO.exists():
+            if build_ref() is None:
+                raise FileNotFoundError("oracle/_ref is not built (reference sources unavailable)")
+        L = ctypes.CDLL(str(REF_SO))
+        sig = {
+            "twref_amips_batch_soa": ([_P, _I64, _P, _P, _P, _I], None),
+            "twref_sample_triangle": ([_P, _D, _P, _I64], _I64),
+            "twref_surface_build": ([_P, _I32, _P, _I32], _P),
+            "twref_surface_free": ([_P], None),
+            "twref_points_out": ([_P, _P, _I64, _D, _P, _I], None),
+            "twref_faces_out": ([_P, _P, _I64, _D, _D, _P, _I], None),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        self.L = L
+
+    @staticmethod
+    def available() -> bool:
+        return REF_SO.exists() or (HERE / "_ref" / "src" / "amips_slice.inc").exists() or \
+            Path(os.environ.get("TW_REFERENCE_ROOT", "/root/reference"), "src").is_dir()
+
+    def amips_batch_soa(self, T, nthreads=1, energy=True, jacobian=True, hessian=True):
+        T = _c(T, np.float64)
+        n = T.shape[1]
+        E = np.empty(n) if energy else None
+        J = np.empty((3, n)) if jacobian else None
+        H = np.empty((9, n)) if hessian else None
+        self.L.twref_amips_batch_soa(_p(T), n, _p(E), _p(J), _p(H), nthreads)
+        return E, J, H
+
+    def sample_triangle(self, tri9, sd):
+        t = _c(tri9, np.float64).reshape(9)
+        n = self.L.twref_sample_triangle(_p(t), sd, None, 0)
+        out = np.empty((max(n, 1), 3))
+        self.L.twref_sample_triangle(_p(t), sd, _p(out), n)
+        return out[:n]
+
+    def surface(self, V, F):
+        return RefSurface(self, V, F)
+
+
+class RefSurface:
+    def __init__(self, r: RefLib, V, F):
+        self.r = r
+        self.V = _c(V, np.float64).reshape(-1, 3)
+        self.F = _c(F, np.int32).reshape(-1, 3)
+        self.h = r.L.twref_surface_build(_p(self.V), self.V.shape[0], _p(self.F), self.F.shape[0])
+
+    def __del__(self):
+        try:
+            self.r.L.twref_surface_free(self.h)
+        except Exception:
+            pass
+
+    def points_out(self, P, eps2, nthreads=1):
+        X = _c(P, np.float64).reshape(-1, 3)
+        out = np.empty(X.shape[0], np.uint8)
+        self.r.L.twref_points_out(self.h, _p(X), X.shape[0], eps2, _p(out), nthreads)
+        return out
+
+    def faces_out(self, tris, eps2, sd, nthreads=1):
+        X = _c(tris, np.float64).reshape(-1, 9)
+        out = np.empty(X.shape[0], np.uint8)
+        self.r.L.twref_faces_out(self.h, _p(X), X.shape[0], eps2, sd, _p(out), nthreads)
+        return out

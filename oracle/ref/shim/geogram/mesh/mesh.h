@@ -1,0 +1,3 @@
+// Forwards to the shared geogram shim (test infrastructure only).
+#pragma once
+#include "../../geo_shim.h"

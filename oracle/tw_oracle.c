@@ -1,0 +1,1163 @@
+/*
+ * tw_oracle.c -- CPU oracle (test infrastructure) for the TetWild query path.
+ *
+ * Build: see oracle/Makefile (-O2 -ffp-contract=off; no -ffast-math).
+ * Only the tests, the smoke check and the CPU-baseline leg of bench.py use
+ * this file.  See tw_oracle.h for the pinning of each routine.
+ *
+ * Arithmetic contract shared with the .cuh headers in tetwild_gb300/csrc: every floating
+ * point expression below is evaluated left to right exactly as written, with
+ * no fused multiply-add except where fma() is called explicitly (exact
+ * two-product in the expansion arithmetic).
+ */
+#include "tw_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* =========================================================================
+ * Inverse cube root x^(-1/3), x >= 0.
+ *
+ * The reference evaluates pow(pow(det, 2), -0.333333333333333)
+ * (LocalOperations.cpp:78-80).  libm pow is not correctly rounded on every
+ * platform, so the GPU and the oracle share this routine instead: exponent
+ * reduction x = m * 2^(3q), m in [1, 8), then Newton-Raphson on
+ * f(y) = y^-3 - m, y <- y + y*(1 - m*y^3)/3, three steps in binary32 from a
+ * linear seed and two in binary64.  Every step is a plain IEEE operation, so
+ * the result is bit-identical on any IEEE machine without FP contraction.
+ * Accuracy: within 2 ulp of the exact value (measured against mpmath in the
+ * tests); relative difference to the reference's pow(.., -0.333333333333333)
+ * is below 3e-13 over the whole double range (the reference's exponent is
+ * itself 3.3e-16 away from -1/3).
+ * ========================================================================= */
+static inline uint64_t tw_bits(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
+static inline double tw_from_bits(uint64_t u) { double x; memcpy(&x, &u, 8); return x; }
+
+double two_icbrt(double x)
+{
+    if (!(x == x)) return x;                 /* NaN */
+    if (x <= 0.0) {
+        if (x == 0.0) return INFINITY;       /* pow(0, -1/3) = +inf */
+        return NAN;                          /* not reached: x = det^2 */
+    }
+    if (x == INFINITY) return 0.0;
+    uint64_t u = tw_bits(x);
+    int e = (int)((u >> 52) & 0x7ff);
+    int ebias = 0;
+    if (e == 0) {                            /* subnormal: scale by 2^54 */
+        x = x * 18014398509481984.0;
+        u = tw_bits(x);
+        e = (int)((u >> 52) & 0x7ff);
+        ebias = -54;
+    }
+    int ex = e - 1023 + ebias;               /* x = m1 * 2^ex, m1 in [1,2) */
+    int q = (ex >= 0) ? ex / 3 : -((-ex + 2) / 3);   /* floor(ex / 3) */
+    int rem = ex - 3 * q;                    /* 0, 1, 2 */
+    double m = tw_from_bits((u & 0x000fffffffffffffULL) | ((uint64_t)(1023 + rem) << 52));
+    /* m in [1, 8).  Seed for m^(-1/3) on [1,8): chord-like linear fit.     */
+    float mf = (float)m;                     /* round to nearest binary32 */
+    float yf = 0.9318f - 0.06015f * mf;
+    const float third_f = 0.333333343f;
+    for (int i = 0; i < 3; ++i) {
+        float y3 = (yf * yf) * yf;
+        float t = 1.0f - mf * y3;
+        yf = yf + (yf * t) * third_f;
+    }
+    double y = (double)yf;
+    const double third = 0.33333333333333331483;
+    for (int i = 0; i < 2; ++i) {
+        double y3 = (y * y) * y;
+        double t = 1.0 - m * y3;
+        y = y + (y * t) * third;
+    }
+    /* scale by 2^(-q) exactly */
+    double s = tw_from_bits((uint64_t)(1023 - q) << 52);
+    return y * s;
+}
+
+/* =========================================================================
+ * Conformal AMIPS energy of a tet, its gradient and Hessian w.r.t. vertex 0.
+ *
+ * Reference: LocalOperations.cpp:28-81 (energy), :83-147 (Jacobian),
+ * :149-291 (Hessian); the same expression is energy.ispc:39-60.  The
+ * reference evaluates machine-generated expressions; this restatement
+ * evaluates the same function in closed form:
+ *   a = p0 - p3,  b = (p0 - 2 p1 + p3)/sqrt3,  c = (p0 + p1 + p3 - 3 p2)/sqrt6
+ *   (rows of the map from the regular tet), N = |a|^2 + |b|^2 + |c|^2,
+ *   D = a . (b x c),  E = N * (D^2)^(-1/3).
+ * dD/dp0 = g = b x c + (c x a)/sqrt3 + (a x b)/sqrt6 (D is affine in p0),
+ * dN/dp0 = gN = 2 (a + b/sqrt3 + c/sqrt6), d2N/dp0^2 = 3 I, so with
+ * r = (D^2)^(-1/3):
+ *   J = r (gN - (2/3)(N/D) g)
+ *   H = 3 r I - (2/3)(r/D)(gN g^T + g gN^T) + (10/9)(N r/D^2) g g^T.
+ * Agreement with the generated expressions: 1e-12 relative (tested).
+ * ========================================================================= */
+#define TW_ISQ3 0.57735026918962576451   /* 1/sqrt(3) */
+#define TW_ISQ6 0.40824829046386301637   /* 1/sqrt(6) */
+#define TW_2_3  0.66666666666666662966   /* 2/3 */
+#define TW_10_9 1.1111111111111111605    /* 10/9 */
+
+static inline void tw_frame(const double* T, double a[3], double b[3], double c[3])
+{
+    for (int k = 0; k < 3; ++k) {
+        double x0 = T[k], x1 = T[3 + k], x2 = T[6 + k], x3 = T[9 + k];
+        a[k] = x0 - x3;
+        b[k] = ((x0 - x1) + (x3 - x1)) * TW_ISQ3;
+        c[k] = (((x0 - x2) + (x1 - x2)) + (x3 - x2)) * TW_ISQ6;
+    }
+}
+static inline double tw_dot(const double u[3], const double v[3])
+{
+    return (u[0] * v[0] + u[1] * v[1]) + u[2] * v[2];
+}
+static inline void tw_cross(const double u[3], const double v[3], double w[3])
+{
+    w[0] = u[1] * v[2] - u[2] * v[1];
+    w[1] = u[2] * v[0] - u[0] * v[2];
+    w[2] = u[0] * v[1] - u[1] * v[0];
+}
+
+double two_amips_energy(const double T[12])
+{
+    double a[3], b[3], c[3], bc[3];
+    tw_frame(T, a, b, c);
+    double N = (tw_dot(a, a) + tw_dot(b, b)) + tw_dot(c, c);
+    tw_cross(b, c, bc);
+    double D = tw_dot(a, bc);
+    return N * two_icbrt(D * D);
+}
+
+/* Shared body of J and H. */
+static void tw_amips_grad_terms(const double* T, double* N_, double* D_, double* r_,
+                                double g[3], double gN[3])
+{
+    double a[3], b[3], c[3], bc[3], ca[3], ab[3];
+    tw_frame(T, a, b, c);
+    double N = (tw_dot(a, a) + tw_dot(b, b)) + tw_dot(c, c);
+    tw_cross(b, c, bc);
+    tw_cross(c, a, ca);
+    tw_cross(a, b, ab);
+    double D = tw_dot(a, bc);
+    for (int k = 0; k < 3; ++k) {
+        g[k] = (bc[k] + TW_ISQ3 * ca[k]) + TW_ISQ6 * ab[k];
+        gN[k] = 2.0 * ((a[k] + TW_ISQ3 * b[k]) + TW_ISQ6 * c[k]);
+    }
+    *N_ = N;
+    *D_ = D;
+    *r_ = two_icbrt(D * D);
+}
+
+void two_amips_jacobian(const double T[12], double J[3])
+{
+    double N, D, r, g[3], gN[3];
+    tw_amips_grad_terms(T, &N, &D, &r, g, gN);
+    double invD = 1.0 / D;
+    double t = (TW_2_3 * N) * invD;
+    for (int k = 0; k < 3; ++k) J[k] = r * (gN[k] - t * g[k]);
+}
+
+void two_amips_hessian(const double T[12], double H[9])
+{
+    double N, D, r, g[3], gN[3];
+    tw_amips_grad_terms(T, &N, &D, &r, g, gN);
+    double invD = 1.0 / D;
+    double s1 = (TW_2_3 * r) * invD;
+    double s2 = (((TW_10_9 * N) * r) * invD) * invD;
+    double r3 = 3.0 * r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double base = (i == j) ? r3 : 0.0;
+            H[i * 3 + j] = (base - s1 * (gN[i] * g[j] + g[i] * gN[j])) + s2 * (g[i] * g[j]);
+        }
+}
+
+/* =========================================================================
+ * Exact orientation and collinearity.
+ *
+ * CGAL::orientation(p,q,r,s) on Epick points (LocalOperations.cpp:544,
+ * :755, :864; VertexSmoother.cpp:166) is POSITIVE iff det[q-p, r-p, s-p] > 0.
+ * Method (Shewchuk, "Adaptive Precision Floating-Point Arithmetic and Fast
+ * Robust Geometric Predicates", 1997): a floating-point evaluation with the
+ * paper's forward error bound (7 + 56 eps) eps * permanent, and, when the
+ * filter cannot decide, an exact evaluation with nonoverlapping expansions
+ * (Two-Sum, Two-Diff, Two-Product via fma, Grow-Expansion and
+ * Scale-Expansion, both with zero elimination).
+ * ========================================================================= */
+#define TW_EPS 1.1102230246251565404e-16      /* 2^-53 */
+#define TW_O3D_BOUND ((7.0 + 56.0 * TW_EPS) * TW_EPS)
+
+static inline void tw_two_sum(double a, double b, double* x, double* y)
+{
+    double s = a + b, bv = s - a, av = s - bv, br = b - bv, ar = a - av;
+    *x = s;
+    *y = ar + br;
+}
+static inline void tw_two_diff(double a, double b, double* x, double* y)
+{
+    double d = a - b, bv = a - d, av = d + bv, br = bv - b, ar = a - av;
+    *x = d;
+    *y = ar + br;
+}
+static inline void tw_fast_two_sum(double a, double b, double* x, double* y)
+{
+    double s = a + b, bv = s - a;
+    *x = s;
+    *y = b - bv;
+}
+static inline void tw_two_prod(double a, double b, double* x, double* y)
+{
+    double p = a * b;
+    *x = p;
+    *y = fma(a, b, -p);
+}
+/* h = e + b  (Grow-Expansion with zero elimination); returns length. */
+static int tw_grow(const double* e, int n, double b, double* h)
+{
+    double Q = b, hh;
+    int k = 0;
+    for (int i = 0; i < n; ++i) {
+        tw_two_sum(Q, e[i], &Q, &hh);
+        if (hh != 0.0) h[k++] = hh;
+    }
+    if (Q != 0.0 || k == 0) h[k++] = Q;
+    return k;
+}
+/* h = e + f by repeated growth; h must hold n + m entries; tmp likewise. */
+static int tw_sum(const double* e, int n, const double* f, int m, double* h, double* tmp)
+{
+    int k = n;
+    for (int i = 0; i < n; ++i) h[i] = e[i];
+    for (int j = 0; j < m; ++j) {
+        k = tw_grow(h, k, f[j], tmp);
+        for (int i = 0; i < k; ++i) h[i] = tmp[i];
+    }
+    return k;
+}
+/* h = e * b (Scale-Expansion with zero elimination); h holds 2n entries. */
+static int tw_scale(const double* e, int n, double b, double* h)
+{
+    double Q, hh, p1, p0, sum;
+    int k = 0;
+    tw_two_prod(e[0], b, &Q, &hh);
+    if (hh != 0.0) h[k++] = hh;
+    for (int i = 1; i < n; ++i) {
+        tw_two_prod(e[i], b, &p1, &p0);
+        tw_two_sum(Q, p0, &sum, &hh);
+        if (hh != 0.0) h[k++] = hh;
+        tw_fast_two_sum(p1, sum, &Q, &hh);
+        if (hh != 0.0) h[k++] = hh;
+    }
+    if (Q != 0.0 || k == 0) h[k++] = Q;
+    return k;
+}
+/* product of two expansions (each <= 2 terms) -> <= 8 terms */
+static int tw_mul22(const double* x, int nx, const double* y, int ny, double* h)
+{
+    double t0[4], t1[4], tmp[8];
+    int k0 = tw_scale(y, ny, x[0], t0);
+    if (nx == 1) {
+        for (int i = 0; i < k0; ++i) h[i] = t0[i];
+        return k0;
+    }
+    int k1 = tw_scale(y, ny, x[1], t1);
+    return tw_sum(t0, k0, t1, k1, h, tmp);
+}
+static inline int tw_diff_exp(double a, double b, double* e)
+{
+    double x, y;
+    tw_two_diff(a, b, &x, &y);
+    if (y == 0.0) { e[0] = x; return 1; }
+    e[0] = y;
+    e[1] = x;
+    return 2;
+}
+static inline int tw_sign_exp(const double* e, int n)
+{
+    double top = e[n - 1];
+    return (top > 0.0) - (top < 0.0);
+}
+/* exact (u1 * v2 - u2 * v1) with u,v 2-term expansions -> <= 16 terms */
+static int tw_minor(const double* u1, int n1, const double* v2, int m2, const double* u2, int n2,
+                    const double* v1, int m1, double* h)
+{
+    double p[8], q[8], tmp[16];
+    int kp = tw_mul22(u1, n1, v2, m2, p);
+    int kq = tw_mul22(u2, n2, v1, m1, q);
+    for (int i = 0; i < kq; ++i) q[i] = -q[i];
+    return tw_sum(p, kp, q, kq, h, tmp);
+}
+
+int two_orient3d_exact(const double p[3], const double q[3], const double r[3], const double s[3])
+{
+    double u[3][2], v[3][2], w[3][2];
+    int nu[3], nv[3], nw[3];
+    for (int k = 0; k < 3; ++k) {
+        nu[k] = tw_diff_exp(q[k], p[k], u[k]);
+        nv[k] = tw_diff_exp(r[k], p[k], v[k]);
+        nw[k] = tw_diff_exp(s[k], p[k], w[k]);
+    }
+    /* det = ux (vy wz - vz wy) + uy (vz wx - vx wz) + uz (vx wy - vy wx) */
+    double m[16], t0[32], t1[32], term[64], acc[192], acc2[192], tmp[192];
+    int nacc = 0;
+    static const int ia[3] = {1, 2, 0}, ib[3] = {2, 0, 1};
+    for (int k = 0; k < 3; ++k) {
+        int i = ia[k], j = ib[k];
+        int nm = tw_minor(v[i], nv[i], w[j], nw[j], v[j], nv[j], w[i], nw[i], m);
+        int k0 = tw_scale(m, nm, u[k][0], t0);
+        int nt;
+        if (nu[k] == 2) {
+            int k1 = tw_scale(m, nm, u[k][1], t1);
+            nt = tw_sum(t0, k0, t1, k1, term, tmp);
+        } else {
+            for (int z = 0; z < k0; ++z) term[z] = t0[z];
+            nt = k0;
+        }
+        if (nacc == 0) {
+            for (int z = 0; z < nt; ++z) acc[z] = term[z];
+            nacc = nt;
+        } else {
+            nacc = tw_sum(acc, nacc, term, nt, acc2, tmp);
+            for (int z = 0; z < nacc; ++z) acc[z] = acc2[z];
+        }
+    }
+    return tw_sign_exp(acc, nacc);
+}
+
+int two_orient3d(const double p[3], const double q[3], const double r[3], const double s[3])
+{
+    for (int k = 0; k < 3; ++k)
+        if (!isfinite(p[k]) || !isfinite(q[k]) || !isfinite(r[k]) || !isfinite(s[k])) return 0;
+    double ux = q[0] - p[0], uy = q[1] - p[1], uz = q[2] - p[2];
+    double vx = r[0] - p[0], vy = r[1] - p[1], vz = r[2] - p[2];
+    double wx = s[0] - p[0], wy = s[1] - p[1], wz = s[2] - p[2];
+    double vywz = vy * wz, vzwy = vz * wy;
+    double vzwx = vz * wx, vxwz = vx * wz;
+    double vxwy = vx * wy, vywx = vy * wx;
+    double det = (ux * (vywz - vzwy) + uy * (vzwx - vxwz)) + uz * (vxwy - vywx);
+    double perm = (fabs(ux) * (fabs(vywz) + fabs(vzwy)) + fabs(uy) * (fabs(vzwx) + fabs(vxwz))) +
+                  fabs(uz) * (fabs(vxwy) + fabs(vywx));
+    double bound = TW_O3D_BOUND * perm;
+    if (det > bound) return 1;
+    if (-det > bound) return -1;
+    return two_orient3d_exact(p, q, r, s);
+}
+
+/* CGAL collinear(p,q,r) (Triangle_3f::is_degenerate, LocalOperations.cpp:1048):
+ * all three 2x2 minors of [p-r, q-r] vanish, decided exactly. */
+static int tw_minor2_zero(double px, double py, double qx, double qy, double rx, double ry)
+{
+    double a[2], b[2], c[2], d[2], m[16];
+    int na = tw_diff_exp(px, rx, a), nb = tw_diff_exp(qy, ry, b);
+    int nc = tw_diff_exp(py, ry, c), nd = tw_diff_exp(qx, rx, d);
+    int k = tw_minor(a, na, b, nb, c, nc, d, nd, m);
+    return tw_sign_exp(m, k) == 0;
+}
+int two_collinear(const double a[3], const double b[3], const double c[3])
+{
+    if (!tw_minor2_zero(a[0], a[1], b[0], b[1], c[0], c[1])) return 0;
+    if (!tw_minor2_zero(a[0], a[2], b[0], b[2], c[0], c[2])) return 0;
+    return tw_minor2_zero(a[1], a[2], b[1], b[2], c[1], c[2]);
+}
+
+/* ========================================================================= */
+int two_tet_flip(const double T[12])
+{
+    return two_orient3d(T, T + 3, T + 6, T + 9) != 1;
+}
+
+double two_tet_quality(const double T[12])
+{
+    /* calTetQuality_AMIPS, LocalOperations.cpp:862-884 */
+    if (two_orient3d(T, T + 3, T + 6, T + 9) != 1) return TWO_MAX_ENERGY;
+    double e = two_amips_energy(T);
+    if (isinf(e) || isnan(e) || e <= 0.0) return TWO_MAX_ENERGY;
+    return e;
+}
+
+/* =========================================================================
+ * Point-triangle squared distance: closest point by Voronoi regions
+ * (Ericson, "Real-Time Collision Detection", 2005, sec. 5.1.5), then
+ * d^2 = |p - q|^2.  Stands in for geogram's
+ * Geom::point_triangle_squared_distance (DistanceQuery.h:36,
+ * mesh_AABB.cpp:168), which is not part of the reference sources.  A
+ * triangle whose face region is degenerate (va + vb + vc <= 0) falls back to
+ * the nearest of its three edges.
+ * ========================================================================= */
+static double tw_seg_sqdist(const double p[3], const double a[3], const double b[3], double q[3])
+{
+    double ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    double ap[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
+    double t = tw_dot(ap, ab), l = tw_dot(ab, ab);
+    if (t <= 0.0 || l <= 0.0) {
+        q[0] = a[0]; q[1] = a[1]; q[2] = a[2];
+    } else if (t >= l) {
+        q[0] = b[0]; q[1] = b[1]; q[2] = b[2];
+    } else {
+        double s = t / l;
+        for (int k = 0; k < 3; ++k) q[k] = a[k] + s * ab[k];
+    }
+    double d[3] = {p[0] - q[0], p[1] - q[1], p[2] - q[2]};
+    return tw_dot(d, d);
+}
+
+double two_point_triangle_sqdist(const double p[3], const double a[3], const double b[3],
+                                 const double c[3], double q_out[3])
+{
+    double q[3];
+    double ab[3], ac[3], ap[3], bp[3], cp[3];
+    for (int k = 0; k < 3; ++k) {
+        ab[k] = b[k] - a[k];
+        ac[k] = c[k] - a[k];
+        ap[k] = p[k] - a[k];
+    }
+    double d1 = tw_dot(ab, ap), d2 = tw_dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) {
+        q[0] = a[0]; q[1] = a[1]; q[2] = a[2];
+        goto done;
+    }
+    for (int k = 0; k < 3; ++k) bp[k] = p[k] - b[k];
+    double d3 = tw_dot(ab, bp), d4 = tw_dot(ac, bp);
+    if (d3 >= 0.0 && d4 <= d3) {
+        q[0] = b[0]; q[1] = b[1]; q[2] = b[2];
+        goto done;
+    }
+    double vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+        double v = d1 / (d1 - d3);
+        for (int k = 0; k < 3; ++k) q[k] = a[k] + v * ab[k];
+        goto done;
+    }
+    for (int k = 0; k < 3; ++k) cp[k] = p[k] - c[k];
+    double d5 = tw_dot(ab, cp), d6 = tw_dot(ac, cp);
+    if (d6 >= 0.0 && d5 <= d6) {
+        q[0] = c[0]; q[1] = c[1]; q[2] = c[2];
+        goto done;
+    }
+    double vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        double w = d2 / (d2 - d6);
+        for (int k = 0; k < 3; ++k) q[k] = a[k] + w * ac[k];
+        goto done;
+    }
+    double va = d3 * d6 - d5 * d4;
+    double d43 = d4 - d3, d56 = d5 - d6;
+    if (va <= 0.0 && d43 >= 0.0 && d56 >= 0.0) {
+        double w = d43 / (d43 + d56);
+        for (int k = 0; k < 3; ++k) q[k] = b[k] + w * (c[k] - b[k]);
+        goto done;
+    }
+    {
+        double den = (va + vb) + vc;
+        if (!(den > 0.0)) {
+            /* degenerate face region: nearest of the three edges */
+            double qa[3], qb[3];
+            double best = tw_seg_sqdist(p, a, b, q);
+            double d = tw_seg_sqdist(p, b, c, qa);
+            if (d < best) { best = d; q[0] = qa[0]; q[1] = qa[1]; q[2] = qa[2]; }
+            d = tw_seg_sqdist(p, c, a, qb);
+            if (d < best) { best = d; q[0] = qb[0]; q[1] = qb[1]; q[2] = qb[2]; }
+            if (q_out) { q_out[0] = q[0]; q_out[1] = q[1]; q_out[2] = q[2]; }
+            return best;
+        }
+        double inv = 1.0 / den;
+        double v = vb * inv, w = vc * inv;
+        for (int k = 0; k < 3; ++k) q[k] = (a[k] + ab[k] * v) + ac[k] * w;
+    }
+done:
+    if (q_out) { q_out[0] = q[0]; q_out[1] = q[1]; q_out[2] = q[2]; }
+    {
+        double d[3] = {p[0] - q[0], p[1] - q[1], p[2] - q[2]};
+        return tw_dot(d, d);
+    }
+}
+
+/* point_box_signed_squared_distance, mesh_AABB.cpp:201-220, outside part
+ * (a point inside the box gets 0; the reference returns a negative number
+ * there, which prunes identically since both are <= any threshold >= 0). */
+double two_point_box_sqdist(const double p[3], const double lo[3], const double hi[3])
+{
+    double r = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        if (p[k] < lo[k]) {
+            double d = p[k] - lo[k];
+            r += d * d;
+        } else if (p[k] > hi[k]) {
+            double d = p[k] - hi[k];
+            r += d * d;
+        }
+    }
+    return r;
+}
+
+/* =========================================================================
+ * sampleTriangle, Common.cpp:143-228, with geogram vec3 semantics:
+ *   length2(v) = (x*x + y*y) + z*z, length = sqrt(length2),
+ *   distance(a,b) = sqrt(((a-b).x^2 + (a-b).y^2) + (a-b).z^2),
+ *   normalize(v) = (1/length(v)) * v  (when length > 1e-30),
+ *   s * v and v * s scale each component, v / s divides each component.
+ * Samples are emitted in the reference order.
+ * ========================================================================= */
+typedef struct { double x, y, z; } tw_v3;
+static inline tw_v3 v3(double x, double y, double z) { tw_v3 r = {x, y, z}; return r; }
+static inline tw_v3 v3_sub(tw_v3 a, tw_v3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline tw_v3 v3_add(tw_v3 a, tw_v3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline tw_v3 v3_mul(tw_v3 a, double s) { return v3(a.x * s, a.y * s, a.z * s); }
+static inline tw_v3 s_mul(double s, tw_v3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+static inline tw_v3 v3_div(tw_v3 a, double s) { return v3(a.x / s, a.y / s, a.z / s); }
+static inline double v3_len2(tw_v3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+static inline double v3_len(tw_v3 a) { return sqrt(v3_len2(a)); }
+static inline double v3_dist(tw_v3 a, tw_v3 b) { return v3_len(v3_sub(a, b)); }
+static inline double v3_dot(tw_v3 a, tw_v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline tw_v3 v3_cross(tw_v3 a, tw_v3 b)
+{
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline tw_v3 v3_normalize(tw_v3 a)
+{
+    double s = v3_len(a);
+    if (s > 1e-30) s = 1.0 / s;
+    return s_mul(s, a);
+}
+/* double -> int conversion as C does for values in range; clamps outside it
+ * (the reference's behaviour there is undefined). */
+static inline int tw_trunc_int(double x)
+{
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0) return 2147483647;
+    if (x <= -2147483648.0) return -2147483647 - 1;
+    return (int)x;
+}
+
+#define TW_EMIT(P)                                                         \
+    do {                                                                   \
+        if (cnt < cap && out) {                                            \
+            out[3 * cnt] = (P).x; out[3 * cnt + 1] = (P).y; out[3 * cnt + 2] = (P).z; \
+        }                                                                  \
+        ++cnt;                                                             \
+    } while (0)
+
+int64_t two_sample_triangle(const double vv[9], double sd, double* out, int64_t cap)
+{
+    int64_t cnt = 0;
+    const double sqrt3_2 = sqrt(3.0) / 2.0;
+    tw_v3 vs[3] = {v3(vv[0], vv[1], vv[2]), v3(vv[3], vv[4], vv[5]), v3(vv[6], vv[7], vv[8])};
+    double ls[3];
+    for (int i = 0; i < 3; ++i) ls[i] = v3_len2(v3_sub(vs[i], vs[(i + 1) % 3]));
+    /* std::minmax_element: first smallest, LAST largest */
+    int max_i = 0;
+    for (int i = 1; i < 3; ++i)
+        if (!(ls[i] < ls[max_i])) max_i = i;
+    double N = sqrt(ls[max_i]) / sd;
+    if (N <= 1) {
+        for (int i = 0; i < 3; ++i) TW_EMIT(vs[i]);
+        return cnt;
+    }
+    if (N == (double)tw_trunc_int(N)) N -= 1;
+
+    tw_v3 v0 = vs[max_i], v1 = vs[(max_i + 1) % 3], v2 = vs[(max_i + 2) % 3];
+    tw_v3 n_v0v1 = v3_normalize(v3_sub(v1, v0));
+    for (int n = 0; n <= N; ++n) TW_EMIT(v3_add(v0, v3_mul(v3_mul(n_v0v1, sd), (double)n)));
+    TW_EMIT(v1);
+
+    double h = v3_dist(v3_add(v3_div(s_mul(v3_dot(v3_sub(v2, v0), v3_sub(v1, v0)), v3_sub(v1, v0)), ls[max_i]), v0), v2);
+    int M = tw_trunc_int(h / (sqrt3_2 * sd));
+    if (M < 1) {
+        TW_EMIT(v2);
+        return cnt;
+    }
+    tw_v3 n_v0v2 = v3_normalize(v3_sub(v2, v0));
+    tw_v3 n_v1v2 = v3_normalize(v3_sub(v2, v1));
+    double cr0 = v3_len(v3_cross(v3_sub(v2, v0), v3_sub(v1, v0)));
+    double cr1 = v3_len(v3_cross(v3_sub(v2, v1), v3_sub(v0, v1)));
+    double sin_v0 = cr0 / (v3_dist(v0, v2) * v3_dist(v0, v1));
+    double tan_v0 = cr0 / v3_dot(v3_sub(v2, v0), v3_sub(v1, v0));
+    double tan_v1 = cr1 / v3_dot(v3_sub(v2, v1), v3_sub(v0, v1));
+    double sin_v1 = cr1 / (v3_dist(v1, v2) * v3_dist(v0, v1));
+    (void)tan_v1;
+    for (int m = 1; m <= M; ++m) {
+        int n = tw_trunc_int(sqrt3_2 / tan_v0 * m + 0.5);
+        int n1 = tw_trunc_int(sqrt3_2 / tan_v0 * m);
+        if (m % 2 == 0 && n == n1) n += 1;
+        tw_v3 v0_m = v3_add(v0, s_mul((double)m * sqrt3_2 * sd / sin_v0, n_v0v2));
+        tw_v3 v1_m = v3_add(v1, s_mul((double)m * sqrt3_2 * sd / sin_v1, n_v1v2));
+        if (v3_dist(v0_m, v1_m) <= sd) break;
+        double delta_d = (((double)n + (m % 2) / 2.0) - (double)m * sqrt3_2 / tan_v0) * sd;
+        tw_v3 v = v3_add(v0_m, s_mul(delta_d, n_v0v1));
+        int N1 = tw_trunc_int(v3_dist(v, v1_m) / sd);
+        for (int i = 0; i <= N1; ++i) TW_EMIT(v3_add(v, v3_mul(s_mul((double)i, n_v0v1), sd)));
+    }
+    TW_EMIT(v2);
+
+    N = sqrt(ls[(max_i + 1) % 3]) / sd;
+    if (N > 1) {
+        if (N == (double)tw_trunc_int(N)) N -= 1;
+        tw_v3 nv = v3_normalize(v3_sub(v2, v1));
+        for (int n = 1; n <= N; ++n) TW_EMIT(v3_add(v1, v3_mul(v3_mul(nv, sd), (double)n)));
+    }
+    N = sqrt(ls[(max_i + 2) % 3]) / sd;
+    if (N > 1) {
+        if (N == (double)tw_trunc_int(N)) N -= 1;
+        tw_v3 nv = v3_normalize(v3_sub(v0, v2));
+        for (int n = 1; n <= N; ++n) TW_EMIT(v3_add(v2, v3_mul(v3_mul(nv, sd), (double)n)));
+    }
+    return cnt;
+}
+
+int64_t two_sample_count(const double v[9], double sd)
+{
+    return two_sample_triangle(v, sd, NULL, 0);
+}
+
+/* =========================================================================
+ * Surface tree for the envelope: the layout of geogram's
+ * MeshFacetsAABBWithEps (mesh_AABB.cpp:356-379): facets reordered by a
+ * recursive median split of their centroids, an implicit binary tree over
+ * index ranges (node n covers [b,e), children 2n and 2n+1, split at
+ * b + (e-b)/2), boxes = exact min/max of the facet vertices.
+ *
+ * Query semantics (isPointOutEnvelop, LocalOperations.cpp:1034-1044):
+ * out <=> min over facets of sqdist(p, f) > eps2.  The traversal stops at the
+ * first facet with sqdist <= eps2 (facet_in_envelope_recursive,
+ * mesh_AABB.cpp:482-548) and prunes a box only when its distance exceeds
+ * (eps + tau)^2, tau = 64 * 2^-53 * max(|coord|): a box is never pruned
+ * while it may hold a facet whose computed distance is <= eps2, so the
+ * decision equals the brute-force decision bit for bit.
+ * ========================================================================= */
+struct two_surface {
+    int32_t nf;
+    double* tri;      /* 9 doubles per facet, tree order */
+    double* box;      /* 6 doubles per node (lo, hi), implicit indexing */
+    int32_t nbox;
+    double scale;     /* max |coordinate| of the surface */
+};
+
+typedef struct { double c; int32_t id; } tw_key;
+static int tw_key_cmp(const void* x, const void* y)
+{
+    const tw_key* a = (const tw_key*)x;
+    const tw_key* b = (const tw_key*)y;
+    if (a->c < b->c) return -1;
+    if (a->c > b->c) return 1;
+    return (a->id > b->id) - (a->id < b->id);
+}
+static void tw_median_order(const double* cen, int32_t* ids, int32_t n, int axis, tw_key* scratch)
+{
+    if (n <= 1) return;
+    for (int32_t i = 0; i < n; ++i) {
+        scratch[i].c = cen[3 * ids[i] + axis];
+        scratch[i].id = ids[i];
+    }
+    qsort(scratch, (size_t)n, sizeof(tw_key), tw_key_cmp);
+    for (int32_t i = 0; i < n; ++i) ids[i] = scratch[i].id;
+    int32_t m = n / 2;
+    tw_median_order(cen, ids, m, (axis + 1) % 3, scratch);
+    tw_median_order(cen, ids + m, n - m, (axis + 1) % 3, scratch);
+}
+static int32_t tw_max_node(int32_t node, int32_t b, int32_t e)
+{
+    if (b + 1 == e) return node;
+    int32_t m = b + (e - b) / 2;
+    int32_t l = tw_max_node(2 * node, b, m), r = tw_max_node(2 * node + 1, m, e);
+    return l > r ? l : r;
+}
+static void tw_init_boxes(two_surface* s, int32_t node, int32_t b, int32_t e)
+{
+    double* B = s->box + 6 * node;
+    if (b + 1 == e) {
+        const double* t = s->tri + 9 * b;
+        for (int k = 0; k < 3; ++k) {
+            double lo = t[k], hi = t[k];
+            for (int v = 1; v < 3; ++v) {
+                if (t[3 * v + k] < lo) lo = t[3 * v + k];
+                if (t[3 * v + k] > hi) hi = t[3 * v + k];
+            }
+            B[k] = lo;
+            B[3 + k] = hi;
+        }
+        return;
+    }
+    int32_t m = b + (e - b) / 2;
+    tw_init_boxes(s, 2 * node, b, m);
+    tw_init_boxes(s, 2 * node + 1, m, e);
+    const double* L = s->box + 12 * node;
+    const double* R = L + 6;
+    for (int k = 0; k < 3; ++k) {
+        B[k] = L[k] < R[k] ? L[k] : R[k];
+        B[3 + k] = L[3 + k] > R[3 + k] ? L[3 + k] : R[3 + k];
+    }
+}
+
+two_surface* two_surface_build(const double* V, int32_t nV, const int32_t* F, int32_t nF)
+{
+    (void)nV;
+    if (nF <= 0) return NULL;
+    two_surface* s = (two_surface*)calloc(1, sizeof(two_surface));
+    s->nf = nF;
+    double* cen = (double*)malloc(sizeof(double) * 3 * (size_t)nF);
+    int32_t* ids = (int32_t*)malloc(sizeof(int32_t) * (size_t)nF);
+    tw_key* scratch = (tw_key*)malloc(sizeof(tw_key) * (size_t)nF);
+    double scale = 0.0;
+    for (int32_t f = 0; f < nF; ++f) {
+        ids[f] = f;
+        for (int k = 0; k < 3; ++k) {
+            double c = 0.0;
+            for (int v = 0; v < 3; ++v) {
+                double x = V[3 * F[3 * f + v] + k];
+                c += x;
+                if (fabs(x) > scale) scale = fabs(x);
+            }
+            cen[3 * f + k] = c / 3.0;
+        }
+    }
+    tw_median_order(cen, ids, nF, 0, scratch);
+    s->tri = (double*)malloc(sizeof(double) * 9 * (size_t)nF);
+    for (int32_t i = 0; i < nF; ++i)
+        for (int v = 0; v < 3; ++v)
+            for (int k = 0; k < 3; ++k) s->tri[9 * i + 3 * v + k] = V[3 * F[3 * ids[i] + v] + k];
+    s->nbox = tw_max_node(1, 0, nF) + 1;
+    s->box = (double*)calloc((size_t)s->nbox * 6, sizeof(double));
+    tw_init_boxes(s, 1, 0, nF);
+    s->scale = scale;
+    free(cen);
+    free(ids);
+    free(scratch);
+    return s;
+}
+
+void two_surface_free(two_surface* s)
+{
+    if (!s) return;
+    free(s->tri);
+    free(s->box);
+    free(s);
+}
+
+static double tw_prune_threshold(const two_surface* s, const double p[3], double eps2)
+{
+    double m = s->scale;
+    for (int k = 0; k < 3; ++k)
+        if (fabs(p[k]) > m) m = fabs(p[k]);
+    double eps = sqrt(eps2);
+    double tau = 64.0 * TW_EPS * m + 4.0 * TW_EPS * eps;
+    return (eps + tau) * (eps + tau);
+}
+
+static int tw_in_recursive(const two_surface* s, const double p[3], double eps2, double thr,
+                           int32_t node, int32_t b, int32_t e)
+{
+    if (b + 1 == e) {
+        const double* t = s->tri + 9 * b;
+        return two_point_triangle_sqdist(p, t, t + 3, t + 6, NULL) <= eps2;
+    }
+    int32_t m = b + (e - b) / 2;
+    const double* L = s->box + 12 * node;
+    const double* R = L + 6;
+    double dl = two_point_box_sqdist(p, L, L + 3);
+    double dr = two_point_box_sqdist(p, R, R + 3);
+    if (dl < dr) {
+        if (dl <= thr && tw_in_recursive(s, p, eps2, thr, 2 * node, b, m)) return 1;
+        if (dr <= thr && tw_in_recursive(s, p, eps2, thr, 2 * node + 1, m, e)) return 1;
+    } else {
+        if (dr <= thr && tw_in_recursive(s, p, eps2, thr, 2 * node + 1, m, e)) return 1;
+        if (dl <= thr && tw_in_recursive(s, p, eps2, thr, 2 * node, b, m)) return 1;
+    }
+    return 0;
+}
+
+int two_point_out(const two_surface* s, const double p[3], double eps2)
+{
+    if (!s) return 1;
+    double thr = tw_prune_threshold(s, p, eps2);
+    const double* B = s->box + 6;
+    if (two_point_box_sqdist(p, B, B + 3) > thr) return 1;
+    return !tw_in_recursive(s, p, eps2, thr, 1, 0, s->nf);
+}
+
+int two_point_out_brute(const two_surface* s, const double p[3], double eps2)
+{
+    if (!s) return 1;
+    for (int32_t f = 0; f < s->nf; ++f) {
+        const double* t = s->tri + 9 * f;
+        if (two_point_triangle_sqdist(p, t, t + 3, t + 6, NULL) <= eps2) return 0;
+    }
+    return 1;
+}
+
+/* isFaceOutEnvelop_sampling, LocalOperations.cpp:1046-1109: a degenerate
+ * triangle is never out; otherwise out iff some sample is out.  The order in
+ * which the reference visits the samples (from the middle, with a facet
+ * hint) changes only how much work is done, not the decision. */
+int two_face_out(const two_surface* s, const double tri[9], double eps2, double sd)
+{
+    if (two_collinear(tri, tri + 3, tri + 6)) return 0;
+    int64_t n = two_sample_count(tri, sd);
+    double* ps = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    two_sample_triangle(tri, sd, ps, n);
+    int out = 0;
+    for (int64_t i = n / 2, c = 0; c < n; i = (i + 1) % n, ++c)
+        if (two_point_out(s, ps + 3 * i, eps2)) { out = 1; break; }
+    free(ps);
+    return out;
+}
+
+/* =========================================================================
+ * 3x3 solve by Householder QR with column pivoting (Golub & Van Loan,
+ * "Matrix Computations", Alg. 5.4.1), standing in for Eigen's
+ * ColPivHouseholderQR::solve (VertexSmoother.cpp:492).  Columns are chosen by
+ * largest remaining squared norm (first index on ties); a pivot with
+ * |R_kk| <= 3 * 2^-52 * |R_00| ends the rank and the remaining unknowns are
+ * set to zero (Eigen's default threshold is diagonal size * machine epsilon).
+ * ========================================================================= */
+int two_qr_solve3(const double Hm[9], const double bvec[3], double x[3])
+{
+    double R[3][3], c[3];
+    int perm[3] = {0, 1, 2};
+    for (int i = 0; i < 3; ++i) {
+        c[i] = bvec[i];
+        for (int j = 0; j < 3; ++j) R[i][j] = Hm[3 * i + j];
+    }
+    for (int k = 0; k < 3; ++k) {
+        int p = k;
+        double best = -1.0;
+        for (int j = k; j < 3; ++j) {
+            double nrm = 0.0;
+            for (int i = k; i < 3; ++i) nrm = nrm + R[i][j] * R[i][j];
+            if (nrm > best) { best = nrm; p = j; }
+        }
+        if (p != k) {
+            for (int i = 0; i < 3; ++i) { double t = R[i][k]; R[i][k] = R[i][p]; R[i][p] = t; }
+            int t = perm[k]; perm[k] = perm[p]; perm[p] = t;
+        }
+        if (k == 2) break;
+        double xn = 0.0;
+        for (int i = k; i < 3; ++i) xn = xn + R[i][k] * R[i][k];
+        xn = sqrt(xn);
+        if (xn == 0.0) continue;
+        double alpha = (R[k][k] > 0.0) ? -xn : xn;
+        double v[3] = {0.0, 0.0, 0.0};
+        for (int i = k; i < 3; ++i) v[i] = R[i][k];
+        v[k] = v[k] - alpha;
+        double vv = 0.0;
+        for (int i = k; i < 3; ++i) vv = vv + v[i] * v[i];
+        if (vv == 0.0) continue;
+        double beta = 2.0 / vv;
+        for (int j = k + 1; j < 3; ++j) {
+            double s = 0.0;
+            for (int i = k; i < 3; ++i) s = s + v[i] * R[i][j];
+            s = s * beta;
+            for (int i = k; i < 3; ++i) R[i][j] = R[i][j] - s * v[i];
+        }
+        {
+            double s = 0.0;
+            for (int i = k; i < 3; ++i) s = s + v[i] * c[i];
+            s = s * beta;
+            for (int i = k; i < 3; ++i) c[i] = c[i] - s * v[i];
+        }
+        R[k][k] = alpha;
+        for (int i = k + 1; i < 3; ++i) R[i][k] = 0.0;
+    }
+    double thr = 3.0 * 2.220446049250313e-16 * fabs(R[0][0]);
+    int rank = 0;
+    for (int k = 0; k < 3; ++k)
+        if (fabs(R[k][k]) > thr) rank = k + 1; else break;
+    double y[3] = {0.0, 0.0, 0.0};
+    for (int k = rank - 1; k >= 0; --k) {
+        double s = c[k];
+        for (int j = k + 1; j < rank; ++j) s = s - R[k][j] * y[j];
+        y[k] = s / R[k][k];
+    }
+    for (int k = 0; k < 3; ++k) x[perm[k]] = y[k];
+    return rank == 3 ? 0 : 1;
+}
+
+/* =========================================================================
+ * NewtonsMethod / NewtonsUpdate / getNewEnergy, VertexSmoother.cpp:465-702
+ * (scalar build: TETWILD_WITH_ISPC off).  Per-tet terms are summed in caller
+ * order.  NewtonsUpdate evaluates E/J/H on the tet rotated so the centre
+ * vertex comes first (:640-651); getNewEnergy evaluates E on the tet in its
+ * stored order (:606-614).
+ * ========================================================================= */
+static void tw_gather(const double* xyz, const int32_t* t, int32_t v, const double* pos,
+                      int start, double T[12])
+{
+    for (int j = 0; j < 4; ++j) {
+        int32_t id = t[(start + j) % 4];
+        const double* src = (id == v) ? pos : xyz + 3 * (size_t)id;
+        T[3 * j] = src[0];
+        T[3 * j + 1] = src[1];
+        T[3 * j + 2] = src[2];
+    }
+}
+
+static int tw_star_flip(const double* xyz, const int32_t* tets, int32_t nt, int32_t v,
+                        const double* pos)
+{
+    double T[12];
+    for (int32_t i = 0; i < nt; ++i) {
+        tw_gather(xyz, tets + 4 * i, v, pos, 0, T);
+        if (two_tet_flip(T)) return 1;
+    }
+    return 0;
+}
+
+static double tw_new_energy(const double* xyz, const int32_t* tets, int32_t nt, int32_t v,
+                            const double* pos)
+{
+    double s = 0.0, T[12];
+    for (int32_t i = 0; i < nt; ++i) {
+        tw_gather(xyz, tets + 4 * i, v, pos, 0, T);
+        s += two_amips_energy(T);
+    }
+    if (isinf(s) || isnan(s) || s <= 0.0 || s > TWO_MAX_ENERGY) s = TWO_MAX_ENERGY;
+    return s;
+}
+
+static int tw_newton_update(const double* xyz, const int32_t* tets, int32_t nt, int32_t v,
+                            const double* pos, double* energy, double J[3], double H[9])
+{
+    double e = 0.0, T[12], J1[3], H1[9];
+    for (int k = 0; k < 3; ++k) J[k] = 0.0;
+    for (int k = 0; k < 9; ++k) H[k] = 0.0;
+    for (int32_t i = 0; i < nt; ++i) {
+        const int32_t* t = tets + 4 * i;
+        int start = 0;
+        for (int j = 0; j < 4; ++j)
+            if (t[j] == v) { start = j; break; }
+        tw_gather(xyz, t, v, pos, start, T);
+        e += two_amips_energy(T);
+        two_amips_jacobian(T, J1);
+        two_amips_hessian(T, H1);
+        for (int j = 0; j < 3; ++j) {
+            J[j] += J1[j];
+            H[3 * j + 0] += H1[3 * j + 0];
+            H[3 * j + 1] += H1[3 * j + 1];
+            H[3 * j + 2] += H1[3 * j + 2];
+        }
+    }
+    if (isinf(e)) e = TWO_MAX_ENERGY;
+    *energy = e;
+    if (isnan(e)) return 0;
+    if (e <= 0.0) return 0;
+    for (int k = 0; k < 3; ++k)
+        if (!isfinite(J[k])) return 0;
+    for (int k = 0; k < 9; ++k)
+        if (!isfinite(H[k])) return 0;
+    return 1;
+}
+
+int two_newton_star(const double* xyz, const int32_t* tets, int32_t nt, int32_t v, int max_step,
+                    int max_it, double out[3])
+{
+    double pos[3] = {xyz[3 * (size_t)v], xyz[3 * (size_t)v + 1], xyz[3 * (size_t)v + 2]};
+    int is_moved = 0;
+    double old_energy = 0.0, new_energy = 0.0, J[3], H[9];
+    for (int step = 0; step < max_step; ++step) {
+        if (!tw_newton_update(xyz, tets, nt, v, pos, &old_energy, J, H)) break;
+        double old_pf[3] = {pos[0], pos[1], pos[2]};
+        double X0[3] = {pos[0], pos[1], pos[2]};
+        double a = 1.0;
+        int step_taken = 0;
+        for (int it = 0; it < max_it; ++it) {
+            double rhs[3], X[3];
+            for (int i = 0; i < 3; ++i)
+                rhs[i] = ((H[3 * i] * X0[0] + H[3 * i + 1] * X0[1]) + H[3 * i + 2] * X0[2]) - a * J[i];
+            two_qr_solve3(H, rhs, X);
+            if (!isfinite(X[0]) || !isfinite(X[1]) || !isfinite(X[2])) {
+                a /= 2.0;
+                continue;
+            }
+            pos[0] = X[0]; pos[1] = X[1]; pos[2] = X[2];
+            if (tw_star_flip(xyz, tets, nt, v, pos)) {
+                pos[0] = old_pf[0]; pos[1] = old_pf[1]; pos[2] = old_pf[2];
+                a /= 2.0;
+                continue;
+            }
+            new_energy = tw_new_energy(xyz, tets, nt, v, pos);
+            if (new_energy >= old_energy || isinf(new_energy) || isnan(new_energy)) {
+                pos[0] = old_pf[0]; pos[1] = old_pf[1]; pos[2] = old_pf[2];
+                a /= 2.0;
+                continue;
+            }
+            step_taken = 1;
+            break;
+        }
+        if (fabs(new_energy - old_energy) < 1e-5) step_taken = 0;
+        if (!step_taken) {
+            is_moved = (step != 0);
+            break;
+        }
+        is_moved = 1;
+    }
+    out[0] = pos[0];
+    out[1] = pos[1];
+    out[2] = pos[2];
+    return is_moved;
+}
+
+/* =========================================================================
+ * Threaded batch drivers.
+ * ========================================================================= */
+typedef struct {
+    int kind;
+    int64_t lo, hi;
+    const void* a0;
+    const void* a1;
+    const void* a2;
+    const void* a3;
+    double d0, d1;
+    int i0, i1, i2;
+    void* o0;
+    void* o1;
+    void* o2;
+    void* o3;
+    int64_t n;
+} tw_job;
+
+static void tw_run_amips(tw_job* j)
+{
+    const double* T = (const double*)j->a0;
+    int64_t n = j->n;
+    double* E = (double*)j->o0;
+    double* J = (double*)j->o1;
+    double* H = (double*)j->o2;
+    uint8_t* flip = (uint8_t*)j->o3;
+    for (int64_t i = j->lo; i < j->hi; ++i) {
+        double t[12], jj[3], hh[9];
+        for (int c = 0; c < 12; ++c) t[c] = T[c * n + i];
+        if (flip) flip[i] = (uint8_t)two_tet_flip(t);
+        if (E) E[i] = j->i0 ? two_tet_quality(t) : two_amips_energy(t);
+        if (J) {
+            two_amips_jacobian(t, jj);
+            for (int c = 0; c < 3; ++c) J[c * n + i] = jj[c];
+        }
+        if (H) {
+            two_amips_hessian(t, hh);
+            for (int c = 0; c < 9; ++c) H[c * n + i] = hh[c];
+        }
+    }
+}
+static void tw_run_points(tw_job* j)
+{
+    const two_surface* s = (const two_surface*)j->a0;
+    const double* P = (const double*)j->a1;
+    uint8_t* out = (uint8_t*)j->o0;
+    for (int64_t i = j->lo; i < j->hi; ++i) out[i] = (uint8_t)two_point_out(s, P + 3 * i, j->d0);
+}
+static void tw_run_faces(tw_job* j)
+{
+    const two_surface* s = (const two_surface*)j->a0;
+    const double* tris = (const double*)j->a1;
+    uint8_t* out = (uint8_t*)j->o0;
+    for (int64_t i = j->lo; i < j->hi; ++i)
+        out[i] = (uint8_t)two_face_out(s, tris + 9 * i, j->d0, j->d1);
+}
+static void tw_run_stars(tw_job* j)
+{
+    const double* xyz = (const double*)j->a0;
+    const int32_t* off = (const int32_t*)j->a1;
+    const int32_t* tets = (const int32_t*)j->a2;
+    const int32_t* cen = (const int32_t*)j->a3;
+    double* out = (double*)j->o0;
+    uint8_t* moved = (uint8_t*)j->o1;
+    for (int64_t i = j->lo; i < j->hi; ++i) {
+        int32_t b = off[i], e = off[i + 1];
+        double o[3];
+        int mv = two_newton_star(xyz, tets + 4 * (size_t)b, e - b, cen[i], j->i0, j->i1, o);
+        out[3 * i] = o[0];
+        out[3 * i + 1] = o[1];
+        out[3 * i + 2] = o[2];
+        moved[i] = (uint8_t)mv;
+    }
+}
+static void* tw_thread_main(void* arg)
+{
+    tw_job* j = (tw_job*)arg;
+    switch (j->kind) {
+    case 0: tw_run_amips(j); break;
+    case 1: tw_run_points(j); break;
+    case 2: tw_run_faces(j); break;
+    case 3: tw_run_stars(j); break;
+    default: break;
+    }
+    return NULL;
+}
+static void tw_parallel(tw_job proto, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    if ((int64_t)nthreads > n) nthreads = (int)(n > 0 ? n : 1);
+    pthread_t th[256];
+    tw_job jobs[256];
+    /* contiguous chunks, one per thread */
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t] = proto;
+        jobs[t].lo = n * t / nthreads;
+        jobs[t].hi = n * (t + 1) / nthreads;
+    }
+    if (nthreads == 1) {
+        tw_thread_main(&jobs[0]);
+        return;
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, tw_thread_main, &jobs[t]);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+}
+
+void two_amips_batch_soa(const double* T, int64_t n, int quality, double* E, double* J, double* H,
+                         uint8_t* flip, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 0;
+    j.a0 = T;
+    j.n = n;
+    j.i0 = quality;
+    j.o0 = E;
+    j.o1 = J;
+    j.o2 = H;
+    j.o3 = flip;
+    tw_parallel(j, n, nthreads);
+}
+void two_points_out_batch(const two_surface* s, const double* P, int64_t n, double eps2,
+                          uint8_t* out, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 1;
+    j.a0 = s;
+    j.a1 = P;
+    j.d0 = eps2;
+    j.o0 = out;
+    tw_parallel(j, n, nthreads);
+}
+void two_faces_out_batch(const two_surface* s, const double* tris, int64_t n, double eps2,
+                         double sd, uint8_t* out, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 2;
+    j.a0 = s;
+    j.a1 = tris;
+    j.d0 = eps2;
+    j.d1 = sd;
+    j.o0 = out;
+    tw_parallel(j, n, nthreads);
+}
+void two_newton_stars_batch(const double* xyz, const int32_t* star_off, const int32_t* tets,
+                            const int32_t* centers, int64_t nstars, int max_step, int max_it,
+                            double* out, uint8_t* moved, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 3;
+    j.a0 = xyz;
+    j.a1 = star_off;
+    j.a2 = tets;
+    j.a3 = centers;
+    j.i0 = max_step;
+    j.i1 = max_it;
+    j.o0 = out;
+    j.o1 = moved;
+    tw_parallel(j, nstars, nthreads);
+}

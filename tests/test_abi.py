@@ -1,0 +1,82 @@
+"""The C-ABI library loads and exports every symbol include/tw_gb300.h declares
+(no compute calls: this runs without a GPU)."""
+import ctypes
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = ROOT / "include" / "tw_gb300.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^TW_API\s+(?:const\s+char\*|int)\s+(tw_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    import tetwild_gb300 as tw
+    from tetwild_gb300 import build as twbuild
+
+    if not tw.library_path().exists():
+        twbuild.build()
+    return tw.library_path()
+
+
+def test_header_declares_api():
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    assert "tw_amips_soa" in syms and "tw_envelope_points" in syms and "tw_newton_stars" in syms
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = ctypes.CDLL(str(libpath))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_library_exports_nothing_else(libpath):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(libpath)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = sorted({l.split()[-1] for l in out.splitlines() if " T " in l and l.split()[-1].startswith("tw_")})
+    assert exported == declared_symbols()
+
+
+def test_python_binding_covers_header():
+    import tetwild_gb300 as tw
+
+    assert sorted(tw.EXPORTED_SYMBOLS) == declared_symbols()
+
+
+def test_python_binding_loads(libpath):
+    import tetwild_gb300 as tw
+
+    lib = tw.load_library()
+    assert lib.tw_last_error(None) == b"null context"
+    assert lib.tw_ctx_destroy(None) == tw.TW_ERR_ARG
+
+
+def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
+    import tetwild_gb300 as tw
+
+    monkeypatch.setattr(tw, "_LIB", None)
+    monkeypatch.setattr(tw, "library_path", lambda: tmp_path / "missing.so")
+    with pytest.raises(tw.TetWildGpuError):
+        tw.Context(0)
+
+
+def test_synthetic_shapes():
+    from tetwild_gb300 import synthetic as syn
+
+    V, F = syn.displaced_sphere(seed=0)
+    assert F.shape == (100000, 3) and V.shape == (50002, 3)
+    V, F = syn.icosphere(3)
+    assert V.shape == (642, 3) and F.shape == (1280, 3)
+    T = syn.energy_batch(1000, seed=0)
+    assert T.shape == (12, 1000)
+    xyz, off, tets, cen = syn.star_batch(20, seed=0)
+    n = off[1:] - off[:-1]
+    assert n.min() >= 4 and n.max() <= 96 and len(cen) == 20

@@ -1,0 +1,311 @@
+"""Pins the CPU oracle (oracle/tw_oracle.c) to the reference.
+
+The reference has no tests or golden data of its own.  The oracle is pinned
+against (a) fixtures produced by the reference's own code (tests/golden,
+regenerated by tests/golden/make_golden.py from oracle/_ref), (b) the
+reference's code run live when oracle/_ref can be built, and (c) exact
+rational arithmetic and high-precision evaluation.
+"""
+import math
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from tetwild_gb300 import synthetic as syn
+
+
+# ---------------------------------------------------------------- icbrt ----
+def test_icbrt_close_to_exact(oracle):
+    import mpmath
+
+    mpmath.mp.prec = 200
+    rng = np.random.default_rng(0)
+    xs = list(10.0 ** rng.uniform(-300, 300, 3000)) + [5e-324, 1e-310, 2.2250738585072014e-308,
+                                                        1.0, 8.0, 7.999999999999999, 1e308]
+    worst = 0.0
+    for x in xs:
+        y = oracle.icbrt(float(x))
+        exact = mpmath.mpf(x) ** (mpmath.mpf(-1) / 3)
+        ulp = math.ulp(y)
+        worst = max(worst, float(abs(mpmath.mpf(y) - exact) / ulp))
+    assert worst <= 2.0, worst
+
+
+def test_icbrt_special_values(oracle):
+    assert oracle.icbrt(0.0) == math.inf
+    assert oracle.icbrt(math.inf) == 0.0
+    assert math.isnan(oracle.icbrt(math.nan))
+
+
+# ---------------------------------------------------------------- AMIPS ----
+def _aos_to_soa(T):
+    return np.ascontiguousarray(np.asarray(T).T)
+
+
+def test_amips_known_answers(oracle):
+    t = (syn.REGULAR_TET * 0.37 + np.array([3.0, -2.0, 5.0])).reshape(12)
+    E, J, H, F = oracle.amips_batch_soa(_aos_to_soa([t]), quality=False)
+    assert abs(E[0] - 3.0) < 1e-14
+    assert np.abs(J[:, 0]).max() < 1e-12 / 0.37
+    # at the minimum the Hessian is symmetric positive definite
+    Hm = H[:, 0].reshape(3, 3)
+    assert np.array_equal(Hm, Hm.T)
+    assert np.linalg.eigvalsh(Hm).min() > 0
+    # either orientation gives 3 (README: range 3..inf)
+    t2 = t.reshape(4, 3)[[0, 2, 1, 3]].reshape(12)
+    E2, _, _, F2 = oracle.amips_batch_soa(_aos_to_soa([t2]), quality=False)
+    assert abs(E2[0] - 3.0) < 1e-14 and F2[0] == 1 and F[0] == 0
+
+
+def test_amips_invariances(oracle):
+    T = syn.energy_batch(2000, seed=3).T
+    E0 = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)[0]
+    Ts = T * 7.5
+    E1 = oracle.amips_batch_soa(_aos_to_soa(Ts), quality=False)[0]
+    perm = T.reshape(-1, 4, 3)[:, [1, 0, 3, 2]].reshape(-1, 12)
+    E2 = oracle.amips_batch_soa(_aos_to_soa(perm), quality=False)[0]
+    assert np.max(np.abs(E1 - E0) / E0) < 1e-12
+    assert np.max(np.abs(E2 - E0) / E0) < 1e-12
+    assert np.all(E0 >= 3.0 - 1e-12)
+
+
+def test_amips_derivatives_match_finite_differences(oracle):
+    T = syn.energy_batch(50, seed=4).T
+    E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)
+    h = 1e-7
+    for i in range(0, 50, 7):
+        for k in range(3):
+            tp, tm = T[i].copy(), T[i].copy()
+            tp[k] += h
+            tm[k] -= h
+            Ep, Jp, _, _ = oracle.amips_batch_soa(_aos_to_soa([tp]), quality=False)
+            Em, Jm, _, _ = oracle.amips_batch_soa(_aos_to_soa([tm]), quality=False)
+            fd = (Ep[0] - Em[0]) / (2 * h)
+            assert abs(fd - J[k, i]) < 1e-5 * max(1.0, abs(E[i]) / 0.01)
+            fdH = (Jp[:, 0] - Jm[:, 0]) / (2 * h)
+            Hrow = H[:, i].reshape(3, 3)[:, k]
+            assert np.max(np.abs(fdH - Hrow)) < 1e-4 * np.max(np.abs(Hrow))
+
+
+def _amips_tolerances(T):
+    """Reference-vs-restatement tolerance per tet.  The reference's generated
+    expressions round their coefficients to 15 digits (e.g. 1.15470053837925 is
+    not 2 * 0.577350269189626), which makes them depend on the absolute position
+    of the tet: an error of about 2e-15 * |x| / edge on each row of the map,
+    amplified by the conditioning edge^3 / |det| of the map.  The bound is
+    1e-12 relative for tets at the origin, growing with |x|/edge * conditioning."""
+    P = T.reshape(-1, 4, 3)
+    edge = np.linalg.norm(P[:, 0] - P[:, 3], axis=1)
+    far = np.abs(P).max(axis=(1, 2)) / np.maximum(edge, 1e-300)
+    a = P[:, 0] - P[:, 3]
+    b = (P[:, 0] - 2 * P[:, 1] + P[:, 3]) / np.sqrt(3)
+    c = (P[:, 0] + P[:, 1] + P[:, 3] - 3 * P[:, 2]) / np.sqrt(6)
+    D = np.einsum("ij,ij->i", a, np.cross(b, c))
+    cond = np.maximum(1.0, edge ** 3 / np.maximum(np.abs(D), 1e-300))
+    return 1e-12 + 5e-14 * far * cond
+
+
+def _term_scales(T):
+    """Magnitudes of the terms summed in J = r (gN - 2/3 N/D g) and
+    H = 3r I - 2/3 r/D (gN g' + g gN') + 10/9 N r/D^2 g g'."""
+    P = T.reshape(-1, 4, 3)
+    a = P[:, 0] - P[:, 3]
+    b = (P[:, 0] - 2 * P[:, 1] + P[:, 3]) / np.sqrt(3)
+    c = (P[:, 0] + P[:, 1] + P[:, 3] - 3 * P[:, 2]) / np.sqrt(6)
+    N = (a * a).sum(1) + (b * b).sum(1) + (c * c).sum(1)
+    D = np.einsum("ij,ij->i", a, np.cross(b, c))
+    g = np.cross(b, c) + np.cross(c, a) / np.sqrt(3) + np.cross(a, b) / np.sqrt(6)
+    gN = 2 * (a + b / np.sqrt(3) + c / np.sqrt(6))
+    r = np.abs(D) ** (-2.0 / 3.0)
+    ng, ngN = np.linalg.norm(g, axis=1), np.linalg.norm(gN, axis=1)
+    sJ = r * (ngN + 2.0 / 3.0 * N / np.abs(D) * ng)
+    sH = 3 * r + 4.0 / 3.0 * r / np.abs(D) * ngN * ng + 10.0 / 9.0 * N * r / D ** 2 * ng ** 2
+    return sJ, sH
+
+
+def test_amips_matches_reference_golden(oracle):
+    g = golden("amips_ref.npz")
+    T = g["T"]
+    E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)
+    ok = np.isfinite(g["E"]) & (g["E"] < 1e8)
+    tol = _amips_tolerances(T)
+    relE = np.abs(E - g["E"]) / np.abs(g["E"])
+    assert np.all(relE[ok] <= tol[ok]), relE[ok].max()
+    # J, H: relative to the magnitude of the terms they sum (forward-error scale)
+    sJ, sH = _term_scales(T)
+    errJ = np.abs(J.T - g["J"]).max(1) / sJ
+    errH = np.abs(H.T - g["H"]).max(1) / sH
+    assert np.all(errJ[ok] <= 10 * tol[ok]), errJ[ok].max()
+    assert np.all(errH[ok] <= 10 * tol[ok]), errH[ok].max()
+    # origin-centred subset (the last 200 tets): 1e-12 relative outright
+    c = slice(len(T) - 200, len(T))
+    assert relE[c].max() <= 1e-12
+    assert errJ[c].max() <= 1e-12 and errH[c].max() <= 1e-12
+
+
+def test_amips_matches_reference_live(oracle, reflib):
+    T = syn.energy_batch(20000, seed=21)
+    Er, Jr, Hr = reflib.amips_batch_soa(T, nthreads=4)
+    E, J, H, _ = oracle.amips_batch_soa(T, quality=False, nthreads=4)
+    tol = _amips_tolerances(T.T)
+    ok = np.isfinite(Er) & (Er < 1e8)
+    rel = np.abs(E - Er) / np.abs(Er)
+    assert np.all(rel[ok] <= tol[ok])
+
+
+# ---------------------------------------------------------- orientation ----
+def test_orientation_matches_exact_golden(oracle):
+    g = golden("orient_exact.npz")
+    got = np.array([oracle.orient3d(*q) for q in g["quads"]], np.int8)
+    assert np.array_equal(got, g["signs"])
+    got_exact = np.array([oracle.orient3d_exact(*q) for q in g["quads"]], np.int8)
+    assert np.array_equal(got_exact, g["signs"])
+
+
+def _frac_orient(p, q, r, s):
+    P = [[Fraction(float(x)) for x in v] for v in (p, q, r, s)]
+    u = [P[1][k] - P[0][k] for k in range(3)]
+    v = [P[2][k] - P[0][k] for k in range(3)]
+    w = [P[3][k] - P[0][k] for k in range(3)]
+    d = (u[0] * (v[1] * w[2] - v[2] * w[1]) + u[1] * (v[2] * w[0] - v[0] * w[2]) +
+         u[2] * (v[0] * w[1] - v[1] * w[0]))
+    return (d > 0) - (d < 0)
+
+
+def test_orientation_random_vs_fraction(oracle):
+    rng = np.random.default_rng(7)
+    for _ in range(400):
+        base = rng.normal(size=(3, 3)) * 10 ** rng.uniform(-6, 6)
+        w = rng.random(2)
+        p4 = base[0] + w[0] * (base[1] - base[0]) + w[1] * (base[2] - base[0])
+        q = np.vstack([base, p4])
+        i, j = rng.integers(0, 4), rng.integers(0, 3)
+        for _ in range(rng.integers(0, 3)):
+            q[i, j] = np.nextafter(q[i, j], np.inf)
+        assert oracle.orient3d(*q) == _frac_orient(*q)
+
+
+def test_collinear_exact(oracle):
+    rng = np.random.default_rng(8)
+    for _ in range(300):
+        a = rng.integers(-5, 6, 3).astype(float) * 0.125
+        d = rng.integers(-3, 4, 3).astype(float)
+        b, c = a + d, a + 2.5 * d
+        if rng.random() < 0.5:
+            k = rng.integers(0, 3)
+            c[k] = np.nextafter(c[k], np.inf)
+        A = [Fraction(x) for x in a]
+        B = [Fraction(x) for x in b]
+        C = [Fraction(x) for x in c]
+        u = [B[k] - A[k] for k in range(3)]
+        v = [C[k] - A[k] for k in range(3)]
+        cross = [u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]]
+        assert oracle.collinear(a, b, c) == int(all(x == 0 for x in cross))
+
+
+def test_quality_sentinel(oracle):
+    t = syn.REGULAR_TET.reshape(12).copy()
+    inv = t.reshape(4, 3)[[1, 0, 2, 3]].reshape(12)
+    flat = t.copy()
+    flat[11] = 0.0  # p3 on the plane of p0, p1, p2
+    E, _, _, F = oracle.amips_batch_soa(_aos_to_soa([t, inv, flat]), quality=True)
+    assert abs(E[0] - 3.0) < 1e-14 and F[0] == 0
+    assert E[1] == 1e50 and F[1] == 1
+    assert E[2] == 1e50 and F[2] == 1
+
+
+# ------------------------------------------------------------- sampling ----
+def test_sample_triangle_matches_reference_golden(oracle):
+    g = golden("sample_ref.npz")
+    sd = float(g["sd"])
+    for i, t in enumerate(g["tris"]):
+        want = g["samples"][g["offsets"][i]:g["offsets"][i + 1]]
+        got = oracle.sample_triangle(t, sd)
+        assert got.shape == want.shape, i
+        assert np.array_equal(got, want), i
+
+
+def test_sample_triangle_matches_reference_live(oracle, reflib):
+    rng = np.random.default_rng(31)
+    sd = 0.01
+    for _ in range(300):
+        a = rng.random(3)
+        t = np.concatenate([a, a + rng.normal(size=3) * rng.uniform(0.001, 0.3),
+                            a + rng.normal(size=3) * rng.uniform(0.001, 0.3)])
+        assert np.array_equal(oracle.sample_triangle(t, sd), reflib.sample_triangle(t, sd))
+
+
+# ------------------------------------------------------------- envelope ----
+def test_point_envelope_matches_reference_golden(oracle):
+    g = golden("envelope_ref.npz")
+    eps2 = float(g["eps"]) ** 2
+    S = oracle.surface(g["V"], g["F"])
+    got = S.points_out(g["P"], eps2)
+    assert np.array_equal(got, g["point_out"])
+    brute = np.array([S.point_out_brute(p, eps2) for p in g["P"][:500]], np.uint8)
+    assert np.array_equal(brute, g["point_out"][:500])
+
+
+def test_face_envelope_matches_reference_golden(oracle):
+    g = golden("envelope_ref.npz")
+    eps2 = float(g["eps"]) ** 2
+    S = oracle.surface(g["V"], g["F"])
+    got = S.faces_out(g["faces"], eps2, float(g["sd"]))
+    assert np.array_equal(got, g["face_out"])
+
+
+def test_envelope_matches_reference_live(oracle, reflib):
+    V, F = syn.displaced_sphere(seed=9, n_lon=80, n_rings=40)
+    eps = 3e-3
+    P = syn.envelope_points(V, F, 20000, eps, seed=10)
+    a = oracle.surface(V, F).points_out(P, eps * eps, nthreads=4)
+    b = reflib.surface(V, F).points_out(P, eps * eps, nthreads=4)
+    assert np.array_equal(a, b)
+    assert 0.3 < a.mean() < 0.7
+
+
+def test_degenerate_face_is_not_out(oracle):
+    V, F = syn.displaced_sphere(seed=9, n_lon=20, n_rings=10)
+    S = oracle.surface(V, F)
+    far = np.array([5.0, 5.0, 5.0, 6.0, 6.0, 6.0, 7.0, 7.0, 7.0])  # collinear, far away
+    assert S.faces_out(far[None], 1e-6, 0.01)[0] == 0
+    tri = np.array([5.0, 5.0, 5.0, 6.0, 6.0, 6.0, 7.0, 7.0, 7.5])
+    assert S.faces_out(tri[None], 1e-6, 0.01)[0] == 1
+
+
+# ------------------------------------------------------------------ QR ----
+def test_qr_solve_matches_numpy(oracle):
+    rng = np.random.default_rng(12)
+    for _ in range(200):
+        A = rng.normal(size=(3, 3))
+        A = A @ A.T + 0.1 * np.eye(3)
+        b = rng.normal(size=3)
+        x = oracle.qr_solve3(A, b)
+        assert np.allclose(x, np.linalg.solve(A, b), rtol=1e-10, atol=1e-12)
+
+
+def test_qr_rank_deficient_gives_finite(oracle):
+    A = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [1.0, 0.0, 1.0]])
+    x = oracle.qr_solve3(A, np.array([1.0, 2.0, 1.0]))
+    assert np.all(np.isfinite(x))
+    assert np.allclose(A @ x, [1.0, 2.0, 1.0], atol=1e-12)
+
+
+# --------------------------------------------------------------- Newton ----
+def test_newton_star_decreases_energy(oracle):
+    xyz, off, tets, cen = syn.star_batch(60, seed=14)
+    out, moved = oracle.newton_stars(xyz, off, tets, cen)
+    assert moved.sum() > 0
+    for s in range(60):
+        T = tets[off[s]:off[s + 1]]
+        X = xyz.copy()
+        before = oracle.amips_batch_soa(np.ascontiguousarray(X[T].reshape(-1, 12).T), quality=False)[0].sum()
+        X[cen[s]] = out[s]
+        after = oracle.amips_batch_soa(np.ascontiguousarray(X[T].reshape(-1, 12).T), quality=False)[0].sum()
+        if moved[s]:
+            assert after < before
+        # never inverts a tet
+        flips = oracle.amips_batch_soa(np.ascontiguousarray(X[T].reshape(-1, 12).T))[3]
+        assert flips.sum() == 0 or not moved[s]

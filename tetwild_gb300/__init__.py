@@ -1,0 +1,365 @@
+"""tetwild_gb300 -- GB300 (sm_103a) kernels for TetWild's mesh-optimisation
+query path, behind a C-ABI (include/tw_gb300.h).
+
+``Context`` is a thin ctypes binding of that ABI (numpy in, numpy out);
+``LocalOperations`` and ``VertexSmoother`` mirror the reference classes'
+method names (LocalOperations.h:69-111, VertexSmoother.h:28-30) over it.
+
+There is no CPU fallback: if libtw_gb300.so is missing or no GPU is present,
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "Context", "LocalOperations", "VertexSmoother", "TetWildGpuError", "load_library",
+    "library_path", "TW_OK", "TW_NEEDS_EXACT_HOST", "TW_ENERGY_RAW", "TW_ENERGY_QUALITY",
+    "TW_SURFACE_INPUT", "TW_SURFACE_BOUNDARY", "MAX_ENERGY", "EXPORTED_SYMBOLS",
+]
+
+TW_OK = 0
+TW_NEEDS_EXACT_HOST = 1
+TW_ERR_ARG = -1
+TW_ERR_CUDA = -2
+TW_ERR_OOM = -3
+TW_ERR_NO_SURFACE = -4
+TW_ERR_NO_MESH = -5
+TW_ERR_TIMEOUT = -6
+TW_ENERGY_RAW = 0
+TW_ENERGY_QUALITY = 1
+TW_SURFACE_INPUT = 0
+TW_SURFACE_BOUNDARY = 1
+MAX_ENERGY = 1e50  # State.h:29
+
+_PKG = Path(__file__).resolve().parent
+
+
+def library_path() -> Path:
+    return _PKG / "libtw_gb300.so"
+
+
+class TetWildGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tw error {code}: {msg}")
+        self.code = code
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_SZ = ctypes.c_size_t
+
+# name -> argtypes (restype int unless noted)
+_SIGS = {
+    "tw_ctx_create": [_I, _SZ, ctypes.POINTER(_P)],
+    "tw_ctx_destroy": [_P],
+    "tw_last_error": [_P],
+    "tw_set_params": [_P, _D, _D, _I, _I],
+    "tw_stream": [_P, ctypes.POINTER(_P)],
+    "tw_synchronize": [_P],
+    "tw_memory_used": [_P, ctypes.POINTER(_SZ)],
+    "tw_amips_soa": [_P, _P, _I64, _I, _P, _P, _P, _P],
+    "tw_amips_soa_device": [_P, _P, _I64, _I, _P, _P, _P, _P],
+    "tw_mesh_upload": [_P, _P, _I32, _P],
+    "tw_mesh_update_vertices": [_P, _P, _P, _P, _I32],
+    "tw_tet_quality": [_P, _P, _I64, _P, _P, _P],
+    "tw_tet_quality_device": [_P, _P, _I64, _P, _P, _P],
+    "tw_surface_upload": [_P, _P, _I32, _P, _I32, _I],
+    "tw_envelope_points": [_P, _P, _I64, _I, _P],
+    "tw_envelope_points_device": [_P, _P, _I64, _I, _P],
+    "tw_envelope_faces": [_P, _P, _I64, _P],
+    "tw_envelope_faces_device": [_P, _P, _I64, _P],
+    "tw_sample_triangle": [_P, _P, _D, _P, _I64, ctypes.POINTER(_I64)],
+    "tw_newton_stars": [_P, _P, _P, _P, _I32, _P, _P],
+    "tw_host_alloc": [_SZ, ctypes.POINTER(_P)],
+    "tw_host_free": [_P],
+    "tw_probe_peaks": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D)],
+}
+EXPORTED_SYMBOLS = tuple(_SIGS)
+
+_LIB = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libtw_gb300.so (built in-tree by tetwild_gb300/build.py)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise TetWildGpuError(TW_ERR_CUDA, f"{path} is not built; run __graft_entry__.build()")
+    lib = ctypes.CDLL(str(path))
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_char_p if name == "tw_last_error" else _I
+    _LIB = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    return a.ctypes.data
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class Context:
+    """One device context: surfaces, resident mesh, scratch and streams."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = load_library()
+        h = _P()
+        st = self.lib.tw_ctx_create(device, hbm_budget_bytes, ctypes.byref(h))
+        if st != TW_OK:
+            raise TetWildGpuError(st, "tw_ctx_create failed (no usable CUDA device?)")
+        self.h = h
+        self.eps_2 = 0.0
+        self.sampling_dist = 0.0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tw_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, allow=(TW_OK,)):
+        if st not in allow:
+            msg = self.lib.tw_last_error(self.h)
+            raise TetWildGpuError(st, msg.decode() if msg else "")
+        return st
+
+    # -- params / streams -------------------------------------------------------
+    def set_params(self, eps_2: float, sampling_dist: float, newton_max_step: int = 15,
+                   newton_max_it: int = 20):
+        self._check(self.lib.tw_set_params(self.h, eps_2, sampling_dist, newton_max_step,
+                                           newton_max_it))
+        self.eps_2 = eps_2
+        self.sampling_dist = sampling_dist
+
+    def stream(self) -> int:
+        s = _P()
+        self._check(self.lib.tw_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def synchronize(self):
+        self._check(self.lib.tw_synchronize(self.h))
+
+    def memory_used(self) -> int:
+        b = _SZ()
+        self._check(self.lib.tw_memory_used(self.h, ctypes.byref(b)))
+        return b.value
+
+    # -- AMIPS --------------------------------------------------------------------
+    def amips(self, T_soa, mode=TW_ENERGY_QUALITY, energy=True, jacobian=True, hessian=True,
+              flip=True):
+        """T_soa: [12, n] float64.  Returns dict of E [n], J [3,n], H [9,n], flip [n]."""
+        T = _c(T_soa, np.float64)
+        if T.ndim != 2 or T.shape[0] != 12:
+            raise ValueError("T_soa must have shape [12, n]")
+        n = T.shape[1]
+        out = {}
+        E = np.empty(n) if energy else None
+        J = np.empty((3, n)) if jacobian else None
+        H = np.empty((9, n)) if hessian else None
+        F = np.empty(n, np.uint8) if flip else None
+        self._check(self.lib.tw_amips_soa(self.h, _ptr(T), n, mode, _ptr(E), _ptr(J), _ptr(H),
+                                          _ptr(F)))
+        if energy:
+            out["E"] = E
+        if jacobian:
+            out["J"] = J
+        if hessian:
+            out["H"] = H
+        if flip:
+            out["flip"] = F
+        return out
+
+    def amips_device(self, T_ptr: int, n: int, mode: int, E_ptr, J_ptr, H_ptr, flip_ptr):
+        """Device-pointer variant; asynchronous on the context stream."""
+        self._check(self.lib.tw_amips_soa_device(self.h, T_ptr, n, mode, E_ptr, J_ptr, H_ptr,
+                                                 flip_ptr))
+
+    # -- resident mesh -------------------------------------------------------------
+    def mesh_upload(self, xyz, rounded=None):
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        R = None if rounded is None else _c(rounded, np.uint8)
+        self._check(self.lib.tw_mesh_upload(self.h, _ptr(X), X.shape[0], _ptr(R)))
+
+    def mesh_update_vertices(self, ids, xyz, rounded=None):
+        I = _c(ids, np.int32)
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        R = None if rounded is None else _c(rounded, np.uint8)
+        self._check(self.lib.tw_mesh_update_vertices(self.h, _ptr(I), _ptr(X), _ptr(R), I.size))
+
+    def tet_quality(self, tets):
+        """Returns (energy [n], flip [n], needs_host [n], status)."""
+        T = _c(tets, np.int32).reshape(-1, 4)
+        n = T.shape[0]
+        E = np.empty(n)
+        F = np.empty(n, np.uint8)
+        N = np.empty(n, np.uint8)
+        st = self._check(self.lib.tw_tet_quality(self.h, _ptr(T), n, _ptr(E), _ptr(F), _ptr(N)),
+                         allow=(TW_OK, TW_NEEDS_EXACT_HOST))
+        return E, F, N, st
+
+    # -- envelope --------------------------------------------------------------------
+    def surface_upload(self, V, F, which=TW_SURFACE_INPUT):
+        Vv = _c(V, np.float64).reshape(-1, 3)
+        Ff = _c(F, np.int32).reshape(-1, 3)
+        self._check(self.lib.tw_surface_upload(self.h, _ptr(Vv), Vv.shape[0], _ptr(Ff),
+                                               Ff.shape[0], which))
+
+    def envelope_points(self, P, which=TW_SURFACE_INPUT):
+        X = _c(P, np.float64).reshape(-1, 3)
+        out = np.empty(X.shape[0], np.uint8)
+        self._check(self.lib.tw_envelope_points(self.h, _ptr(X), X.shape[0], which, _ptr(out)))
+        return out
+
+    def envelope_points_device(self, P_ptr: int, n: int, out_ptr: int, which=TW_SURFACE_INPUT):
+        self._check(self.lib.tw_envelope_points_device(self.h, P_ptr, n, which, out_ptr))
+
+    def envelope_faces(self, tris):
+        X = _c(tris, np.float64).reshape(-1, 9)
+        out = np.empty(X.shape[0], np.uint8)
+        self._check(self.lib.tw_envelope_faces(self.h, _ptr(X), X.shape[0], _ptr(out)))
+        return out
+
+    def envelope_faces_device(self, tris_ptr: int, n: int, out_ptr: int):
+        self._check(self.lib.tw_envelope_faces_device(self.h, tris_ptr, n, out_ptr))
+
+    def sample_triangle(self, tri9, sampling_dist, cap=1 << 20):
+        t = _c(tri9, np.float64).reshape(9)
+        out = np.empty((cap, 3))
+        cnt = _I64()
+        self._check(self.lib.tw_sample_triangle(self.h, _ptr(t), sampling_dist, _ptr(out), cap,
+                                                ctypes.byref(cnt)))
+        return out[: min(cnt.value, cap)].copy(), cnt.value
+
+    # -- Newton -----------------------------------------------------------------------
+    def newton_stars(self, star_off, tets, centers):
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        C = _c(centers, np.int32)
+        ns = C.size
+        out = np.empty((ns, 3))
+        moved = np.empty(ns, np.uint8)
+        self._check(self.lib.tw_newton_stars(self.h, _ptr(O), _ptr(T), _ptr(C), ns, _ptr(out),
+                                             _ptr(moved)))
+        return out, moved
+
+    # -- misc ---------------------------------------------------------------------------
+    def probe_peaks(self):
+        a, b = _D(), _D()
+        self._check(self.lib.tw_probe_peaks(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory (tw_host_alloc) for fast copies."""
+
+    def __init__(self, shape, dtype):
+        self.lib = load_library()
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        p = _P()
+        st = self.lib.tw_host_alloc(max(nbytes, 16), ctypes.byref(p))
+        if st != TW_OK:
+            raise TetWildGpuError(st, "tw_host_alloc failed")
+        self.p = p
+        buf = (ctypes.c_char * max(nbytes, 16)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if getattr(self, "p", None):
+            self.array = None
+            self.lib.tw_host_free(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class LocalOperations:
+    """Mirror of the reference's LocalOperations query methods (LocalOperations.h:69-111)
+    over a resident mesh and surface trees, batched.
+
+    tet_vertices: [nv, 3] float64 (TetVertex::posf), rounded: [nv] (is_rounded).
+    """
+
+    def __init__(self, ctx: Context, tet_vertices, rounded=None):
+        self.ctx = ctx
+        self.ctx.mesh_upload(tet_vertices, rounded)
+
+    # static AMIPS routines, batched over [n,12] tets (LocalOperations.h:109-111)
+    def comformalAMIPSEnergy_new(self, T):
+        T = np.atleast_2d(np.asarray(T, np.float64))
+        return self.ctx.amips(T.T, TW_ENERGY_RAW, True, False, False, False)["E"]
+
+    def comformalAMIPSJacobian_new(self, T):
+        T = np.atleast_2d(np.asarray(T, np.float64))
+        return self.ctx.amips(T.T, TW_ENERGY_RAW, False, True, False, False)["J"].T.copy()
+
+    def comformalAMIPSHessian_new(self, T):
+        T = np.atleast_2d(np.asarray(T, np.float64))
+        return self.ctx.amips(T.T, TW_ENERGY_RAW, False, False, True, False)["H"].T.copy()
+
+    def calTetQualities(self, new_tets):
+        """slim_energy of each tet (LocalOperations.cpp:695-773)."""
+        E, _, needs, st = self.ctx.tet_quality(new_tets)
+        if st == TW_NEEDS_EXACT_HOST:
+            raise TetWildGpuError(st, "tets with unrounded vertices need the host's exact path")
+        return E
+
+    def isFlip(self, new_tets) -> bool:
+        """LocalOperations.cpp:559-573."""
+        _, F, needs, st = self.ctx.tet_quality(new_tets)
+        if st == TW_NEEDS_EXACT_HOST:
+            raise TetWildGpuError(st, "tets with unrounded vertices need the host's exact path")
+        return bool(F.any())
+
+    def isTetFlip(self, t) -> bool:
+        return self.isFlip([t])
+
+    def isPointOutEnvelop(self, p) -> bool:
+        return bool(self.ctx.envelope_points(np.asarray(p).reshape(1, 3), TW_SURFACE_INPUT)[0])
+
+    def isPointOutBoundaryEnvelop(self, p) -> bool:
+        return bool(self.ctx.envelope_points(np.asarray(p).reshape(1, 3), TW_SURFACE_BOUNDARY)[0])
+
+    def isFaceOutEnvelop(self, tri) -> bool:
+        return bool(self.ctx.envelope_faces(np.asarray(tri).reshape(1, 9))[0])
+
+
+class VertexSmoother(LocalOperations):
+    """Mirror of VertexSmoother::NewtonsMethod (VertexSmoother.cpp:465-542), batched over
+    independent stars: star i is centre ``centers[i]`` with tets
+    ``tets[star_off[i]:star_off[i+1]]`` in the caller's order."""
+
+    def NewtonsMethod(self, star_off, tets, centers):
+        return self.ctx.newton_stars(star_off, tets, centers)

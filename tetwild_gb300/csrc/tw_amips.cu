@@ -1,0 +1,134 @@
+// tw_amips.cu -- batched AMIPS energy/gradient/Hessian and exact orientation.
+//
+// k_amips_soa: one tet per thread over the energy_ispc SoA layout
+// (energy.ispc:7-65): 12 coalesced FP64 loads per tet, E/J/H written SoA.
+// The orientation filter (FP64) runs first; the rare exact fallback is an
+// out-of-line call.  The FP64 pipe, not HBM, bounds this kernel on GB300.
+//
+// k_tet_quality_idx: calTetQualities over ids into the resident mesh
+// (LocalOperations.cpp:695-773): gathers the 4 vertices, orientation, energy
+// with the calTetQuality_AMIPS sentinel.
+#include <utility>
+
+#include "tw_device.cuh"
+#include "tw_internal.h"
+
+namespace tw {
+
+template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
+__global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T, int64_t n,
+                                                   double* __restrict__ E,
+                                                   double* __restrict__ J,
+                                                   double* __restrict__ H,
+                                                   uint8_t* __restrict__ flip,
+                                                   unsigned long long* __restrict__ exact_count) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double t[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
+        int ori = 1;
+        if (WF || QUAL) {
+            int ex = 0;
+            ori = orient3d(t, t + 3, t + 6, t + 9, &ex);
+            if (ex) atomicAdd(exact_count, 1ULL);
+        }
+        double jv[3], hv[9];
+        double e;
+        if (WJ || WH) {
+            e = amips_egh(t, WJ ? jv : nullptr, WH ? hv : nullptr);
+        } else {
+            e = amips_energy(t);
+        }
+        if (WE) E[i] = QUAL ? quality_from(ori, e) : e;
+        if (WF) flip[i] = (uint8_t)(ori != 1);
+        if (WJ) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+        }
+        if (WH) {
+#pragma unroll
+            for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+        }
+    }
+}
+
+int grid_for(int64_t n, int block, int blocks_per_sm) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int64_t need = (n + block - 1) / block;
+    int64_t cap = (int64_t)sms * blocks_per_sm;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+using AmipsKernel = void (*)(const double*, int64_t, double*, double*, double*, uint8_t*,
+                             unsigned long long*);
+
+template <int BITS>
+static AmipsKernel pick_amips() {
+    return k_amips_soa<(BITS & 1) != 0, (BITS & 2) != 0, (BITS & 4) != 0, (BITS & 8) != 0,
+                       (BITS & 16) != 0>;
+}
+
+template <int... B>
+static AmipsKernel amips_table(int bits, std::integer_sequence<int, B...>) {
+    static const AmipsKernel table[] = {pick_amips<B>()...};
+    return table[bits];
+}
+
+void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
+                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s) {
+    if (n <= 0) return;
+    int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
+               ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
+    AmipsKernel k = amips_table(bits, std::make_integer_sequence<int, 32>{});
+    const int block = 256;
+    int grid = grid_for(n, block, 8);
+    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, exact_count);
+}
+
+__global__ void __launch_bounds__(256) k_tet_quality_idx(
+    const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,
+    const double* __restrict__ vy, const double* __restrict__ vz,
+    const uint8_t* __restrict__ rounded, double* __restrict__ E, uint8_t* __restrict__ flip,
+    uint8_t* __restrict__ needs_host, unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        int4 tv = __ldg(tets + i);
+        int id[4] = {tv.x, tv.y, tv.z, tv.w};
+        double t[12];
+        bool all_rounded = true;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            t[3 * j] = __ldg(vx + id[j]);
+            t[3 * j + 1] = __ldg(vy + id[j]);
+            t[3 * j + 2] = __ldg(vz + id[j]);
+            if (rounded) all_rounded = all_rounded && (__ldg(rounded + id[j]) != 0);
+        }
+        int ex = 0;
+        int ori = orient3d(t, t + 3, t + 6, t + 9, &ex);
+        if (ex) atomicAdd(counters, 1ULL);
+        if (E) E[i] = quality_from(ori, amips_energy(t));
+        if (flip) flip[i] = (uint8_t)(ori != 1);
+        if (needs_host) needs_host[i] = (uint8_t)(!all_rounded);
+        if (!all_rounded) atomicAdd(counters + 1, 1ULL);
+    }
+}
+
+void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                            const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
+                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0) return;
+    const int block = 256;
+    k_tet_quality_idx<<<grid_for(n, block, 8), block, 0, s>>>(
+        reinterpret_cast<const int4*>(tets), n, vx, vy, vz, rounded, E, flip, needs_host,
+        counters);
+}
+
+}  // namespace tw

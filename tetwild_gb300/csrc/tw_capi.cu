@@ -1,0 +1,649 @@
+// tw_capi.cu -- the extern "C" boundary (include/tw_gb300.h).
+//
+// Host-pointer calls run a chunked pipeline over three streams: chunk k is
+// copied in, computed and copied out on stream k % 3, so host<->device
+// copies of one chunk overlap the kernels of the others.  _device calls
+// enqueue one kernel on the context stream and return.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "tw_device.cuh"
+#include "tw_internal.h"
+
+namespace tw {
+
+int fail(tw_ctx* c, int code, const std::string& msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int cuda_fail(tw_ctx* c, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return fail(c, e == cudaErrorMemoryAllocation ? TW_ERR_OOM : TW_ERR_CUDA, m);
+}
+
+int dev_alloc(tw_ctx* c, size_t bytes, void** out) {
+    *out = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (c->budget && c->used + bytes > c->budget)
+        return fail(c, TW_ERR_OOM, "HBM budget of the context exceeded");
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(c, e, "cudaMalloc");
+    }
+    c->used += bytes;
+    return TW_OK;
+}
+
+void dev_free(tw_ctx* c, void* p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    if (bytes == 0) bytes = 16;
+    c->used -= std::min(c->used, bytes);
+}
+
+int ensure(tw_ctx* c, int slot, size_t bytes, void** out) {
+    Buffer& b = c->scratch[slot];
+    if (b.cap < bytes) {
+        if (b.ptr) dev_free(c, b.ptr, b.cap);
+        b.ptr = nullptr;
+        b.cap = 0;
+        size_t want = bytes + bytes / 8;
+        int st = dev_alloc(c, want, &b.ptr);
+        if (st != TW_OK) return st;
+        b.cap = want;
+    }
+    *out = b.ptr;
+    return TW_OK;
+}
+
+// ---- pipe peak probes -------------------------------------------------------
+__global__ void k_fp64_probe(double* out, int iters) {
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+    double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+    const double b = 0.999999, cc = 1e-12;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, cc); a1 = fma(a1, b, cc); a2 = fma(a2, b, cc); a3 = fma(a3, b, cc);
+        a4 = fma(a4, b, cc); a5 = fma(a5, b, cc); a6 = fma(a6, b, cc); a7 = fma(a7, b, cc);
+    }
+    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 12345.678) out[0] = s;  // keeps the loop live
+}
+__global__ void k_fp32_probe(float* out, int iters) {
+    float a0 = threadIdx.x * 1e-6f, a1 = a0 + 1e-6f, a2 = a0 + 2e-6f, a3 = a0 + 3e-6f;
+    float a4 = a0 + 4e-6f, a5 = a0 + 5e-6f, a6 = a0 + 6e-6f, a7 = a0 + 7e-6f;
+    const float b = 0.9999f, cc = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fmaf(a0, b, cc); a1 = fmaf(a1, b, cc); a2 = fmaf(a2, b, cc); a3 = fmaf(a3, b, cc);
+        a4 = fmaf(a4, b, cc); a5 = fmaf(a5, b, cc); a6 = fmaf(a6, b, cc); a7 = fmaf(a7, b, cc);
+    }
+    float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 12345.678f) out[0] = s;
+}
+void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s) {
+    k_fp64_probe<<<blocks, 256, 0, s>>>(out, iters);
+}
+void launch_fp32_probe(float* out, int iters, int blocks, cudaStream_t s) {
+    k_fp32_probe<<<blocks, 256, 0, s>>>(out, iters);
+}
+
+__global__ void k_aos_to_soa(const double* __restrict__ xyz, int32_t n, double* __restrict__ x,
+                             double* __restrict__ y, double* __restrict__ z) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = xyz[3 * (int64_t)i];
+    y[i] = xyz[3 * (int64_t)i + 1];
+    z[i] = xyz[3 * (int64_t)i + 2];
+}
+__global__ void k_scatter_vertices(const int32_t* __restrict__ ids, const double* __restrict__ xyz,
+                                   const uint8_t* __restrict__ rnd, int32_t n, int32_t nv,
+                                   double* __restrict__ x, double* __restrict__ y,
+                                   double* __restrict__ z, uint8_t* __restrict__ rounded,
+                                   int* __restrict__ bad) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t v = ids[i];
+    if (v < 0 || v >= nv) {
+        atomicExch(bad, 1);
+        return;
+    }
+    x[v] = xyz[3 * (int64_t)i];
+    y[v] = xyz[3 * (int64_t)i + 1];
+    z[v] = xyz[3 * (int64_t)i + 2];
+    if (rnd) rounded[v] = rnd[i];
+}
+__global__ void k_check_ids(const int32_t* __restrict__ ids, int64_t n, int32_t lim,
+                            int* __restrict__ bad) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t v = ids[i];
+    if (v < 0 || v >= lim) atomicExch(bad, 1);
+}
+
+}  // namespace tw
+
+using namespace tw;
+
+namespace {
+
+constexpr int kNumPipe = 3;
+
+struct Guard {
+    explicit Guard(int dev) { cudaSetDevice(dev); }
+};
+
+// scratch slot layout: pipelines use slots [0, kNumPipe), misc uses 6, 7
+int sync_status(tw_ctx* c, const char* where) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->copy_in);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->copy_out);
+    if (e != cudaSuccess) return cuda_fail(c, e, where);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, where);
+    // device-side error word (counters[2]): read and clear
+    unsigned long long err = 0;
+    e = cudaMemcpy(&err, c->counters + 2, sizeof(err), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, where);
+    if (err) {
+        cudaMemset(c->counters + 2, 0, sizeof(err));
+        std::string m = std::string(where) + ": ";
+        if (err & 1ULL) m += "surface traversal exceeded its bounds (corrupt tree); ";
+        if (err & 2ULL) m += "a face exceeds the per-row sample bound (4e6 samples); ";
+        return fail(c, TW_ERR_ARG, m);
+    }
+    return TW_OK;
+}
+
+cudaStream_t pipe_stream(tw_ctx* c, int k) {
+    if (k == 0) return c->stream;
+    return k == 1 ? c->copy_in : c->copy_out;
+}
+
+int64_t chunk_len(int64_t n, size_t bytes_per_item) {
+    // ~96 MB of inputs+outputs per chunk, at least 64k items
+    int64_t c = (int64_t)((96ull << 20) / std::max<size_t>(bytes_per_item, 1));
+    c = std::max<int64_t>(c, 65536);
+    c = (c + 255) & ~int64_t(255);
+    return std::min(c, std::max<int64_t>(n, 1));
+}
+
+}  // namespace
+
+extern "C" {
+
+int tw_ctx_create(int device, size_t hbm_budget_bytes, tw_ctx** out) {
+    if (!out) return TW_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return TW_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) return TW_ERR_ARG;
+    Guard g(device);
+    tw_ctx* c = new tw_ctx();
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return TW_ERR_CUDA;
+    }
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    void* cnt = nullptr;
+    if (dev_alloc(c, 8 * sizeof(unsigned long long), &cnt) != TW_OK) {
+        tw_ctx_destroy(c);
+        return TW_ERR_OOM;
+    }
+    c->counters = (unsigned long long*)cnt;
+    cudaMemset(c->counters, 0, 8 * sizeof(unsigned long long));
+    *out = c;
+    return TW_OK;
+}
+
+int tw_ctx_destroy(tw_ctx* c) {
+    if (!c) return TW_ERR_ARG;
+    Guard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_in) cudaStreamSynchronize(c->copy_in);
+    if (c->copy_out) cudaStreamSynchronize(c->copy_out);
+    for (auto& S : c->surf) free_surface(c, S);
+    dev_free(c, c->vx, sizeof(double) * (size_t)c->nv);
+    dev_free(c, c->vy, sizeof(double) * (size_t)c->nv);
+    dev_free(c, c->vz, sizeof(double) * (size_t)c->nv);
+    dev_free(c, c->rounded, (size_t)c->nv);
+    for (auto& b : c->scratch) dev_free(c, b.ptr, b.cap);
+    dev_free(c, c->counters, 8 * sizeof(unsigned long long));
+    for (auto& ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->copy_in) cudaStreamDestroy(c->copy_in);
+    if (c->copy_out) cudaStreamDestroy(c->copy_out);
+    delete c;
+    return TW_OK;
+}
+
+const char* tw_last_error(const tw_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int tw_set_params(tw_ctx* c, double eps_2, double sampling_dist, int newton_max_step,
+                  int newton_max_it) {
+    if (!c) return TW_ERR_ARG;
+    if (!(eps_2 >= 0.0) || !(sampling_dist >= 0.0) || newton_max_step < 0 || newton_max_it < 0)
+        return fail(c, TW_ERR_ARG, "tw_set_params: negative or NaN parameter");
+    c->eps2 = eps_2;
+    c->sampling_dist = sampling_dist;
+    c->newton_max_step = newton_max_step;
+    c->newton_max_it = newton_max_it;
+    return TW_OK;
+}
+
+int tw_stream(tw_ctx* c, void** s) {
+    if (!c || !s) return TW_ERR_ARG;
+    *s = (void*)c->stream;
+    return TW_OK;
+}
+
+int tw_synchronize(tw_ctx* c) {
+    if (!c) return TW_ERR_ARG;
+    Guard g(c->device);
+    return sync_status(c, "tw_synchronize");
+}
+
+int tw_memory_used(const tw_ctx* c, size_t* bytes) {
+    if (!c || !bytes) return TW_ERR_ARG;
+    *bytes = c->used;
+    return TW_OK;
+}
+
+// ---- AMIPS -------------------------------------------------------------------
+int tw_amips_soa_device(tw_ctx* c, const double* T, int64_t n, int mode, double* E, double* J,
+                        double* H, uint8_t* flip) {
+    if (!c || n < 0 || (n > 0 && !T)) return TW_ERR_ARG;
+    if (mode != TW_ENERGY_RAW && mode != TW_ENERGY_QUALITY)
+        return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
+    Guard g(c->device);
+    launch_amips_soa(T, n, mode, E, J, H, flip, c->counters, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_amips_soa_device");
+    return TW_OK;
+}
+
+int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, double* J,
+                 double* H, uint8_t* flip) {
+    if (!c || n < 0 || (n > 0 && !T)) return TW_ERR_ARG;
+    if (mode != TW_ENERGY_RAW && mode != TW_ENERGY_QUALITY)
+        return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    const size_t per = 96 + (E ? 8 : 0) + (J ? 24 : 0) + (H ? 72 : 0) + (flip ? 1 : 0);
+    const int64_t C = chunk_len(n, per);
+    double* dT[kNumPipe];
+    double *dE[kNumPipe], *dJ[kNumPipe], *dH[kNumPipe];
+    uint8_t* dF[kNumPipe];
+    for (int k = 0; k < kNumPipe; ++k) {
+        void* p = nullptr;
+        int st = ensure(c, k, (size_t)C * per + 1024, &p);
+        if (st != TW_OK) return st;
+        char* q = (char*)p;
+        dT[k] = (double*)q; q += 96 * (size_t)C;
+        dE[k] = E ? (double*)q : nullptr; q += E ? 8 * (size_t)C : 0;
+        dJ[k] = J ? (double*)q : nullptr; q += J ? 24 * (size_t)C : 0;
+        dH[k] = H ? (double*)q : nullptr; q += H ? 72 * (size_t)C : 0;
+        dF[k] = flip ? (uint8_t*)q : nullptr;
+    }
+    int64_t chunk = 0;
+    for (int64_t i0 = 0; i0 < n; i0 += C, ++chunk) {
+        const int k = (int)(chunk % kNumPipe);
+        cudaStream_t s = pipe_stream(c, k);
+        const int64_t len = std::min<int64_t>(C, n - i0);
+        for (int comp = 0; comp < 12; ++comp)
+            cudaMemcpyAsync(dT[k] + comp * len, T + comp * n + i0, 8 * (size_t)len,
+                            cudaMemcpyHostToDevice, s);
+        launch_amips_soa(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s);
+        if (E) cudaMemcpyAsync(E + i0, dE[k], 8 * (size_t)len, cudaMemcpyDeviceToHost, s);
+        if (J)
+            for (int comp = 0; comp < 3; ++comp)
+                cudaMemcpyAsync(J + comp * n + i0, dJ[k] + comp * len, 8 * (size_t)len,
+                                cudaMemcpyDeviceToHost, s);
+        if (H)
+            for (int comp = 0; comp < 9; ++comp)
+                cudaMemcpyAsync(H + comp * n + i0, dH[k] + comp * len, 8 * (size_t)len,
+                                cudaMemcpyDeviceToHost, s);
+        if (flip) cudaMemcpyAsync(flip + i0, dF[k], (size_t)len, cudaMemcpyDeviceToHost, s);
+    }
+    return sync_status(c, "tw_amips_soa");
+}
+
+// ---- resident mesh -------------------------------------------------------------
+int tw_mesh_upload(tw_ctx* c, const double* xyz, int32_t nv, const uint8_t* rounded) {
+    if (!c || nv < 0 || (nv > 0 && !xyz)) return TW_ERR_ARG;
+    Guard g(c->device);
+    dev_free(c, c->vx, 8 * (size_t)c->nv);
+    dev_free(c, c->vy, 8 * (size_t)c->nv);
+    dev_free(c, c->vz, 8 * (size_t)c->nv);
+    dev_free(c, c->rounded, (size_t)c->nv);
+    c->vx = c->vy = c->vz = nullptr;
+    c->rounded = nullptr;
+    c->nv = 0;
+    if (nv == 0) return TW_OK;
+    void *x, *y, *z, *r, *tmp;
+    int st;
+    if ((st = dev_alloc(c, 8 * (size_t)nv, &x)) != TW_OK) return st;
+    if ((st = dev_alloc(c, 8 * (size_t)nv, &y)) != TW_OK) return st;
+    if ((st = dev_alloc(c, 8 * (size_t)nv, &z)) != TW_OK) return st;
+    if ((st = dev_alloc(c, (size_t)nv, &r)) != TW_OK) return st;
+    c->vx = (double*)x;
+    c->vy = (double*)y;
+    c->vz = (double*)z;
+    c->rounded = (uint8_t*)r;
+    c->nv = nv;
+    if ((st = ensure(c, 6, 24 * (size_t)nv, &tmp)) != TW_OK) return st;
+    cudaMemcpyAsync(tmp, xyz, 24 * (size_t)nv, cudaMemcpyHostToDevice, c->stream);
+    k_aos_to_soa<<<(nv + 255) / 256, 256, 0, c->stream>>>((const double*)tmp, nv, c->vx, c->vy,
+                                                          c->vz);
+    if (rounded)
+        cudaMemcpyAsync(c->rounded, rounded, (size_t)nv, cudaMemcpyHostToDevice, c->stream);
+    else
+        cudaMemsetAsync(c->rounded, 1, (size_t)nv, c->stream);
+    return sync_status(c, "tw_mesh_upload");
+}
+
+int tw_mesh_update_vertices(tw_ctx* c, const int32_t* ids, const double* xyz,
+                            const uint8_t* rounded, int32_t n) {
+    if (!c || n < 0 || (n > 0 && (!ids || !xyz))) return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    void* tmp;
+    const size_t bytes = 4 * (size_t)n + 24 * (size_t)n + (size_t)n + 64;
+    int st = ensure(c, 6, bytes, &tmp);
+    if (st != TW_OK) return st;
+    char* q = (char*)tmp;
+    int32_t* dids = (int32_t*)q; q += ((4 * (size_t)n + 15) & ~size_t(15));
+    double* dxyz = (double*)q; q += 24 * (size_t)n;
+    uint8_t* drnd = rounded ? (uint8_t*)q : nullptr;
+    int* bad = (int*)(c->counters + 7);
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemcpyAsync(dids, ids, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dxyz, xyz, 24 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    if (rounded) cudaMemcpyAsync(drnd, rounded, (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    k_scatter_vertices<<<(n + 255) / 256, 256, 0, c->stream>>>(dids, dxyz, drnd, n, c->nv, c->vx,
+                                                               c->vy, c->vz, c->rounded, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_mesh_update_vertices");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "vertex id out of range");
+    return TW_OK;
+}
+
+int tw_tet_quality_device(tw_ctx* c, const int32_t* tets, int64_t n, double* energy,
+                          uint8_t* flip, uint8_t* needs_host) {
+    if (!c || n < 0 || (n > 0 && !tets)) return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    launch_tet_quality_idx(tets, n, c->vx, c->vy, c->vz, c->rounded, energy, flip, needs_host,
+                           c->counters, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_tet_quality_device");
+    return TW_OK;
+}
+
+int tw_tet_quality(tw_ctx* c, const int32_t* tets, int64_t n, double* energy, uint8_t* flip,
+                   uint8_t* needs_host) {
+    if (!c || n < 0 || (n > 0 && !tets)) return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    void* p;
+    const size_t bytes = 16 * (size_t)n + 8 * (size_t)n + 2 * (size_t)n + 256;
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dt = (int32_t*)q; q += 16 * (size_t)n;
+    double* dE = (double*)q; q += 8 * (size_t)n;
+    uint8_t* dF = (uint8_t*)q; q += (size_t)n;
+    uint8_t* dN = (uint8_t*)q;
+    int* bad = (int*)(c->counters + 7);
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(c->counters + 1, 0, sizeof(unsigned long long), c->stream);
+    cudaMemcpyAsync(dt, tets, 16 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    k_check_ids<<<(unsigned)((4 * n + 255) / 256), 256, 0, c->stream>>>(dt, 4 * n, c->nv, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_tet_quality");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "tet vertex id out of range");
+    launch_tet_quality_idx(dt, n, c->vx, c->vy, c->vz, c->rounded, energy ? dE : nullptr,
+                           flip ? dF : nullptr, dN, c->counters, c->stream);
+    unsigned long long unrounded = 0;
+    cudaMemcpyAsync(&unrounded, c->counters + 1, sizeof(unrounded), cudaMemcpyDeviceToHost,
+                    c->stream);
+    if (energy) cudaMemcpyAsync(energy, dE, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (flip) cudaMemcpyAsync(flip, dF, (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (needs_host) cudaMemcpyAsync(needs_host, dN, (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_tet_quality");
+    if (st != TW_OK) return st;
+    return unrounded ? TW_NEEDS_EXACT_HOST : TW_OK;
+}
+
+// ---- envelope -------------------------------------------------------------------
+int tw_surface_upload(tw_ctx* c, const double* V, int32_t nv, const int32_t* F, int32_t nf,
+                      int which) {
+    if (!c || nv < 0 || nf < 0 || (nv > 0 && !V) || (nf > 0 && !F)) return TW_ERR_ARG;
+    if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY)
+        return fail(c, TW_ERR_ARG, "unknown surface");
+    Guard g(c->device);
+    if (nf == 0) {
+        free_surface(c, c->surf[which]);
+        return TW_OK;
+    }
+    void *dV = nullptr, *dF = nullptr;
+    int st = dev_alloc(c, 24 * (size_t)nv, &dV);
+    if (st != TW_OK) return st;
+    st = dev_alloc(c, 12 * (size_t)nf, &dF);
+    if (st != TW_OK) {
+        dev_free(c, dV, 24 * (size_t)nv);
+        return st;
+    }
+    cudaMemcpyAsync(dV, V, 24 * (size_t)nv, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dF, F, 12 * (size_t)nf, cudaMemcpyHostToDevice, c->stream);
+    st = build_surface(c, c->surf[which], (const double*)dV, nv, (const int32_t*)dF, nf, c->stream);
+    dev_free(c, dV, 24 * (size_t)nv);
+    dev_free(c, dF, 12 * (size_t)nf);
+    return st;
+}
+
+int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, uint8_t* out) {
+    if (!c || n < 0 || (n > 0 && (!P || !out))) return TW_ERR_ARG;
+    if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
+    if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    Guard g(c->device);
+    launch_env_points(c->surf[which], P, n, c->eps2, out, c->counters + 2, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
+    return TW_OK;
+}
+
+int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t* out) {
+    if (!c || n < 0 || (n > 0 && (!P || !out))) return TW_ERR_ARG;
+    if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
+    if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    const int64_t C = chunk_len(n, 25);
+    double* dP[kNumPipe];
+    uint8_t* dO[kNumPipe];
+    for (int k = 0; k < kNumPipe; ++k) {
+        void* p;
+        int st = ensure(c, k, 25 * (size_t)C + 256, &p);
+        if (st != TW_OK) return st;
+        dP[k] = (double*)p;
+        dO[k] = (uint8_t*)p + 24 * (size_t)C;
+    }
+    int64_t chunk = 0;
+    for (int64_t i0 = 0; i0 < n; i0 += C, ++chunk) {
+        const int k = (int)(chunk % kNumPipe);
+        cudaStream_t s = pipe_stream(c, k);
+        const int64_t len = std::min<int64_t>(C, n - i0);
+        cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
+        launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->counters + 2, s);
+        cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
+    }
+    return sync_status(c, "tw_envelope_points");
+}
+
+int tw_envelope_faces_device(tw_ctx* c, const double* tris, int64_t n, uint8_t* out) {
+    if (!c || n < 0 || (n > 0 && (!tris || !out))) return TW_ERR_ARG;
+    if (c->surf[TW_SURFACE_INPUT].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    if (!(c->sampling_dist > 0.0)) return fail(c, TW_ERR_ARG, "sampling_dist must be > 0");
+    Guard g(c->device);
+    launch_env_faces(c->surf[TW_SURFACE_INPUT], tris, n, c->eps2, c->sampling_dist, out,
+                     c->counters + 2, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_faces_device");
+    return TW_OK;
+}
+
+int tw_envelope_faces(tw_ctx* c, const double* tris, int64_t n, uint8_t* out) {
+    if (!c || n < 0 || (n > 0 && (!tris || !out))) return TW_ERR_ARG;
+    if (c->surf[TW_SURFACE_INPUT].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    if (!(c->sampling_dist > 0.0)) return fail(c, TW_ERR_ARG, "sampling_dist must be > 0");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    void* p;
+    int st = ensure(c, 7, 73 * (size_t)n + 256, &p);
+    if (st != TW_OK) return st;
+    double* dT = (double*)p;
+    uint8_t* dO = (uint8_t*)p + 72 * (size_t)n;
+    cudaMemcpyAsync(dT, tris, 72 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    launch_env_faces(c->surf[TW_SURFACE_INPUT], dT, n, c->eps2, c->sampling_dist, dO,
+                     c->counters + 2, c->stream);
+    cudaMemcpyAsync(out, dO, (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_envelope_faces");
+}
+
+int tw_sample_triangle(tw_ctx* c, const double* tri9, double sd, double* out, int64_t cap,
+                       int64_t* count) {
+    if (!c || !tri9 || !count || cap < 0 || (cap > 0 && !out) || !(sd > 0.0)) return TW_ERR_ARG;
+    Guard g(c->device);
+    void* p;
+    int st = ensure(c, 7, 72 + 8 + 24 * (size_t)cap + 256, &p);
+    if (st != TW_OK) return st;
+    double* dt = (double*)p;
+    int64_t* dc = (int64_t*)((char*)p + 72);
+    double* dout = (double*)((char*)p + 80);
+    cudaMemcpyAsync(dt, tri9, 72, cudaMemcpyHostToDevice, c->stream);
+    launch_sample_triangle(dt, sd, dout, cap, dc, c->stream);
+    cudaMemcpyAsync(count, dc, 8, cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_sample_triangle");
+    if (st != TW_OK) return st;
+    if (*count < 0) return fail(c, TW_ERR_ARG, "face exceeds the per-row sample bound (4e6)");
+    int64_t k = std::min(*count, cap);
+    if (k > 0) {
+        cudaMemcpy(out, dout, 24 * (size_t)k, cudaMemcpyDeviceToHost);
+        return sync_status(c, "tw_sample_triangle");
+    }
+    return TW_OK;
+}
+
+// ---- Newton stars -----------------------------------------------------------------
+int tw_newton_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets, const int32_t* centers,
+                    int32_t nstars, double* out, uint8_t* moved) {
+    if (!c || nstars < 0 || (nstars > 0 && (!star_off || !tets || !centers || !out || !moved)))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (nstars == 0) return TW_OK;
+    for (int32_t i = 0; i < nstars; ++i)
+        if (star_off[i + 1] < star_off[i]) return fail(c, TW_ERR_ARG, "star offsets decrease");
+    if (star_off[0] != 0) return fail(c, TW_ERR_ARG, "star offsets must start at 0");
+    const int64_t nt = star_off[nstars];
+    Guard g(c->device);
+    void* p;
+    const size_t bytes = 4 * (size_t)(nstars + 1) + 16 * (size_t)nt + 4 * (size_t)nstars +
+                         24 * (size_t)nstars + (size_t)nstars + 1024;
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    char* q = (char*)p;
+    int32_t* doff = (int32_t*)q; q += align(4 * (size_t)(nstars + 1));
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)nt);
+    int32_t* dc = (int32_t*)q; q += align(4 * (size_t)nstars);
+    double* dout = (double*)q; q += align(24 * (size_t)nstars);
+    uint8_t* dm = (uint8_t*)q;
+    int* bad = (int*)(c->counters + 7);
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemcpyAsync(doff, star_off, 4 * (size_t)(nstars + 1), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dc, centers, 4 * (size_t)nstars, cudaMemcpyHostToDevice, c->stream);
+    if (nt > 0)
+        k_check_ids<<<(unsigned)((4 * nt + 255) / 256), 256, 0, c->stream>>>(dt, 4 * nt, c->nv, bad);
+    k_check_ids<<<(unsigned)((nstars + 255) / 256), 256, 0, c->stream>>>(dc, nstars, c->nv, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_newton_stars");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "star vertex id out of range");
+    launch_newton_stars(c->vx, c->vy, c->vz, doff, dt, dc, nstars, c->newton_max_step,
+                        c->newton_max_it, dout, dm, c->stream);
+    cudaMemcpyAsync(out, dout, 24 * (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(moved, dm, (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_newton_stars");
+}
+
+// ---- misc ---------------------------------------------------------------------------
+int tw_host_alloc(size_t bytes, void** out) {
+    if (!out) return TW_ERR_ARG;
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return TW_ERR_OOM;
+    }
+    return TW_OK;
+}
+
+int tw_host_free(void* p) {
+    if (!p) return TW_OK;
+    return cudaFreeHost(p) == cudaSuccess ? TW_OK : TW_ERR_CUDA;
+}
+
+int tw_probe_peaks(tw_ctx* c, double* fp64_tflops, double* fp32_tflops) {
+    if (!c || !fp64_tflops || !fp32_tflops) return TW_ERR_ARG;
+    Guard g(c->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    void* p;
+    int st = ensure(c, 6, 64, &p);
+    if (st != TW_OK) return st;
+    const int blocks = sms * 8;
+    const int it64 = 4096, it32 = 65536;
+    float ms = 0.0f;
+    double best64 = 0.0, best32 = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(c->ev[0], c->stream);
+        launch_fp64_probe((double*)p, it64, blocks, c->stream);
+        cudaEventRecord(c->ev[1], c->stream);
+        launch_fp32_probe((float*)p, it32, blocks, c->stream);
+        cudaEventRecord(c->ev[2], c->stream);
+        cudaEventSynchronize(c->ev[2]);
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        double f64 = 2.0 * 8.0 * it64 * (double)blocks * 256.0 / (ms * 1e-3) / 1e12;
+        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+        double f32 = 2.0 * 8.0 * it32 * (double)blocks * 256.0 / (ms * 1e-3) / 1e12;
+        best64 = std::max(best64, f64);
+        best32 = std::max(best32, f32);
+    }
+    *fp64_tflops = best64;
+    *fp32_tflops = best32;
+    return sync_status(c, "tw_probe_peaks");
+}
+
+}  // extern "C"

@@ -1,0 +1,406 @@
+// tw_device.cuh -- device arithmetic of the TetWild query path on sm_103a.
+//
+// Every routine evaluates the same operations in the same order as the CPU
+// oracle, and all translation units are compiled with -fmad=false, so FP64
+// results are bit-identical to the oracle's and every decision derived from
+// them (orientation sign, envelope in/out, Newton accept/reject) matches.
+#pragma once
+
+#include <cstdint>
+
+namespace tw {
+
+constexpr double kMaxEnergy = 1e50;                    // State.h:29
+constexpr double kIsq3 = 0.57735026918962576451;       // 1/sqrt(3)
+constexpr double kIsq6 = 0.40824829046386301637;       // 1/sqrt(6)
+constexpr double kTwoThirds = 0.66666666666666662966;
+constexpr double kTenNinths = 1.1111111111111111605;
+constexpr double kEps = 1.1102230246251565404e-16;     // 2^-53
+constexpr double kO3dBound = (7.0 + 56.0 * kEps) * kEps;  // Shewchuk 1997, orient3d stage A
+
+// ---------------------------------------------------------------------------
+// x^(-1/3) for x >= 0: exponent reduction to m in [1,8), three binary32 and
+// two binary64 Newton-Raphson steps on y^-3 = m, exact rescale by 2^-q.
+// Replaces pow(pow(det,2), -0.333333333333333) (LocalOperations.cpp:78-80).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double icbrt(double x) {
+    if (!(x == x)) return x;
+    if (x <= 0.0) return (x == 0.0) ? __longlong_as_double(0x7ff0000000000000LL)
+                                    : __longlong_as_double(0x7ff8000000000000LL);
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    int e = (int)((u >> 52) & 0x7ff);
+    if (e == 0x7ff) return 0.0;  // +inf (NaN handled above)
+    int ebias = 0;
+    if (e == 0) {
+        x = x * 18014398509481984.0;
+        u = (unsigned long long)__double_as_longlong(x);
+        e = (int)((u >> 52) & 0x7ff);
+        ebias = -54;
+    }
+    int ex = e - 1023 + ebias;
+    int q = (ex >= 0) ? ex / 3 : -((-ex + 2) / 3);
+    int rem = ex - 3 * q;
+    double m = __longlong_as_double((long long)((u & 0x000fffffffffffffULL) |
+                                                ((unsigned long long)(1023 + rem) << 52)));
+    float mf = __double2float_rn(m);
+    float yf = 0.9318f - 0.06015f * mf;
+    const float third_f = 0.333333343f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float y3 = (yf * yf) * yf;
+        float t = 1.0f - mf * y3;
+        yf = yf + (yf * t) * third_f;
+    }
+    double y = (double)yf;
+    const double third = 0.33333333333333331483;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        double y3 = (y * y) * y;
+        double t = 1.0 - m * y3;
+        y = y + (y * t) * third;
+    }
+    double s = __longlong_as_double((long long)((unsigned long long)(1023 - q) << 52));
+    return y * s;
+}
+
+struct V3 {
+    double x, y, z;
+};
+__device__ __forceinline__ double dot3(const V3& u, const V3& v) {
+    return (u.x * v.x + u.y * v.y) + u.z * v.z;
+}
+__device__ __forceinline__ V3 cross3(const V3& u, const V3& v) {
+    return V3{u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x};
+}
+
+// Rows of the map from the regular tet (closed form of the generated
+// expressions in LocalOperations.cpp:28-291):
+//   a = p0 - p3, b = (p0 - 2p1 + p3)/sqrt3, c = (p0 + p1 + p3 - 3p2)/sqrt6.
+__device__ __forceinline__ void amips_frame(const double* T, V3& a, V3& b, V3& c) {
+    double av[3], bv[3], cv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double x0 = T[k], x1 = T[3 + k], x2 = T[6 + k], x3 = T[9 + k];
+        av[k] = x0 - x3;
+        bv[k] = ((x0 - x1) + (x3 - x1)) * kIsq3;
+        cv[k] = (((x0 - x2) + (x1 - x2)) + (x3 - x2)) * kIsq6;
+    }
+    a = V3{av[0], av[1], av[2]};
+    b = V3{bv[0], bv[1], bv[2]};
+    c = V3{cv[0], cv[1], cv[2]};
+}
+
+// comformalAMIPSEnergy_new (LocalOperations.cpp:28-81): N * (D^2)^(-1/3).
+__device__ __forceinline__ double amips_energy(const double* T) {
+    V3 a, b, c;
+    amips_frame(T, a, b, c);
+    double N = (dot3(a, a) + dot3(b, b)) + dot3(c, c);
+    V3 bc = cross3(b, c);
+    double D = dot3(a, bc);
+    return N * icbrt(D * D);
+}
+
+// Energy, gradient (:83-147) and Hessian (:149-291) w.r.t. vertex 0 in one
+// pass.  J and H are written only when the pointers are non-null.
+__device__ __forceinline__ double amips_egh(const double* T, double* J, double* H) {
+    V3 a, b, c;
+    amips_frame(T, a, b, c);
+    double N = (dot3(a, a) + dot3(b, b)) + dot3(c, c);
+    V3 bc = cross3(b, c);
+    double D = dot3(a, bc);
+    double r = icbrt(D * D);
+    double E = N * r;
+    if (J || H) {
+        V3 ca = cross3(c, a), ab = cross3(a, b);
+        double g[3], gN[3];
+        g[0] = (bc.x + kIsq3 * ca.x) + kIsq6 * ab.x;
+        g[1] = (bc.y + kIsq3 * ca.y) + kIsq6 * ab.y;
+        g[2] = (bc.z + kIsq3 * ca.z) + kIsq6 * ab.z;
+        gN[0] = 2.0 * ((a.x + kIsq3 * b.x) + kIsq6 * c.x);
+        gN[1] = 2.0 * ((a.y + kIsq3 * b.y) + kIsq6 * c.y);
+        gN[2] = 2.0 * ((a.z + kIsq3 * b.z) + kIsq6 * c.z);
+        double invD = 1.0 / D;
+        if (J) {
+            double t = (kTwoThirds * N) * invD;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) J[k] = r * (gN[k] - t * g[k]);
+        }
+        if (H) {
+            double s1 = (kTwoThirds * r) * invD;
+            double s2 = (((kTenNinths * N) * r) * invD) * invD;
+            double r3 = 3.0 * r;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = i; j < 3; ++j) {
+                    double base = (i == j) ? r3 : 0.0;
+                    double h = (base - s1 * (gN[i] * g[j] + g[i] * gN[j])) + s2 * (g[i] * g[j]);
+                    H[i * 3 + j] = h;
+                    H[j * 3 + i] = h;
+                }
+        }
+    }
+    return E;
+}
+
+// ---------------------------------------------------------------------------
+// Exact orientation: CGAL::orientation(p,q,r,s) = sign det[q-p, r-p, s-p].
+// Floating-point filter with Shewchuk's stage-A bound, then exact
+// expansion arithmetic (Two-Sum / Two-Diff / fma Two-Product,
+// Grow-Expansion and Scale-Expansion with zero elimination).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(double a, double b, double& x, double& y) {
+    double s = a + b, bv = s - a, av = s - bv, br = b - bv, ar = a - av;
+    x = s;
+    y = ar + br;
+}
+__device__ __forceinline__ void two_diff(double a, double b, double& x, double& y) {
+    double d = a - b, bv = a - d, av = d + bv, br = bv - b, ar = a - av;
+    x = d;
+    y = ar + br;
+}
+__device__ __forceinline__ void fast_two_sum(double a, double b, double& x, double& y) {
+    double s = a + b, bv = s - a;
+    x = s;
+    y = b - bv;
+}
+__device__ __forceinline__ void two_prod(double a, double b, double& x, double& y) {
+    double p = a * b;
+    x = p;
+    y = fma(a, b, -p);
+}
+__device__ __forceinline__ int exp_grow(const double* e, int n, double b, double* h) {
+    double Q = b, hh;
+    int k = 0;
+    for (int i = 0; i < n; ++i) {
+        two_sum(Q, e[i], Q, hh);
+        if (hh != 0.0) h[k++] = hh;
+    }
+    if (Q != 0.0 || k == 0) h[k++] = Q;
+    return k;
+}
+__device__ __forceinline__ int exp_sum(const double* e, int n, const double* f, int m, double* h,
+                                       double* tmp) {
+    int k = n;
+    for (int i = 0; i < n; ++i) h[i] = e[i];
+    for (int j = 0; j < m; ++j) {
+        k = exp_grow(h, k, f[j], tmp);
+        for (int i = 0; i < k; ++i) h[i] = tmp[i];
+    }
+    return k;
+}
+__device__ __forceinline__ int exp_scale(const double* e, int n, double b, double* h) {
+    double Q, hh, p1, p0, sum;
+    int k = 0;
+    two_prod(e[0], b, Q, hh);
+    if (hh != 0.0) h[k++] = hh;
+    for (int i = 1; i < n; ++i) {
+        two_prod(e[i], b, p1, p0);
+        two_sum(Q, p0, sum, hh);
+        if (hh != 0.0) h[k++] = hh;
+        fast_two_sum(p1, sum, Q, hh);
+        if (hh != 0.0) h[k++] = hh;
+    }
+    if (Q != 0.0 || k == 0) h[k++] = Q;
+    return k;
+}
+__device__ __forceinline__ int exp_mul22(const double* x, int nx, const double* y, int ny,
+                                         double* h) {
+    double t0[4], t1[4], tmp[8];
+    int k0 = exp_scale(y, ny, x[0], t0);
+    if (nx == 1) {
+        for (int i = 0; i < k0; ++i) h[i] = t0[i];
+        return k0;
+    }
+    int k1 = exp_scale(y, ny, x[1], t1);
+    return exp_sum(t0, k0, t1, k1, h, tmp);
+}
+__device__ __forceinline__ int exp_diff(double a, double b, double* e) {
+    double x, y;
+    two_diff(a, b, x, y);
+    if (y == 0.0) {
+        e[0] = x;
+        return 1;
+    }
+    e[0] = y;
+    e[1] = x;
+    return 2;
+}
+__device__ __forceinline__ int exp_minor(const double* u1, int n1, const double* v2, int m2,
+                                         const double* u2, int n2, const double* v1, int m1,
+                                         double* h) {
+    double p[8], q[8], tmp[16];
+    int kp = exp_mul22(u1, n1, v2, m2, p);
+    int kq = exp_mul22(u2, n2, v1, m1, q);
+    for (int i = 0; i < kq; ++i) q[i] = -q[i];
+    return exp_sum(p, kp, q, kq, h, tmp);
+}
+
+// Rare path (the filter failed): kept out of line so the hot kernels do not
+// carry its local-memory arrays.
+static __device__ __noinline__ int orient3d_exact(const double* p, const double* q,
+                                                  const double* r, const double* s) {
+    double u[3][2], v[3][2], w[3][2];
+    int nu[3], nv[3], nw[3];
+    for (int k = 0; k < 3; ++k) {
+        nu[k] = exp_diff(q[k], p[k], u[k]);
+        nv[k] = exp_diff(r[k], p[k], v[k]);
+        nw[k] = exp_diff(s[k], p[k], w[k]);
+    }
+    double m[16], t0[32], t1[32], term[64], acc[192], acc2[192], tmp[192];
+    int nacc = 0;
+    const int ia[3] = {1, 2, 0}, ib[3] = {2, 0, 1};
+    for (int k = 0; k < 3; ++k) {
+        int i = ia[k], j = ib[k];
+        int nm = exp_minor(v[i], nv[i], w[j], nw[j], v[j], nv[j], w[i], nw[i], m);
+        int k0 = exp_scale(m, nm, u[k][0], t0);
+        int nt;
+        if (nu[k] == 2) {
+            int k1 = exp_scale(m, nm, u[k][1], t1);
+            nt = exp_sum(t0, k0, t1, k1, term, tmp);
+        } else {
+            for (int z = 0; z < k0; ++z) term[z] = t0[z];
+            nt = k0;
+        }
+        if (nacc == 0) {
+            for (int z = 0; z < nt; ++z) acc[z] = term[z];
+            nacc = nt;
+        } else {
+            nacc = exp_sum(acc, nacc, term, nt, acc2, tmp);
+            for (int z = 0; z < nacc; ++z) acc[z] = acc2[z];
+        }
+    }
+    double top = acc[nacc - 1];
+    return (top > 0.0) - (top < 0.0);
+}
+
+// Returns +1 POSITIVE, 0 COPLANAR (or non-finite input), -1 NEGATIVE.
+// *exact_used is set when the filter could not decide.
+__device__ __forceinline__ int orient3d(const double* p, const double* q, const double* r,
+                                        const double* s, int* exact_used = nullptr) {
+    double ux = q[0] - p[0], uy = q[1] - p[1], uz = q[2] - p[2];
+    double vx = r[0] - p[0], vy = r[1] - p[1], vz = r[2] - p[2];
+    double wx = s[0] - p[0], wy = s[1] - p[1], wz = s[2] - p[2];
+    double vywz = vy * wz, vzwy = vz * wy;
+    double vzwx = vz * wx, vxwz = vx * wz;
+    double vxwy = vx * wy, vywx = vy * wx;
+    double det = (ux * (vywz - vzwy) + uy * (vzwx - vxwz)) + uz * (vxwy - vywx);
+    double perm = (fabs(ux) * (fabs(vywz) + fabs(vzwy)) + fabs(uy) * (fabs(vzwx) + fabs(vxwz))) +
+                  fabs(uz) * (fabs(vxwy) + fabs(vywx));
+    double bound = kO3dBound * perm;
+    if (det > bound) return 1;
+    if (-det > bound) return -1;
+    // Non-finite coordinates make det or perm non-finite: report COPLANAR.
+    if (!isfinite(perm) || !isfinite(det)) return 0;
+    bool finite_in = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        finite_in = finite_in && isfinite(p[k]) && isfinite(q[k]) && isfinite(r[k]) && isfinite(s[k]);
+    if (!finite_in) return 0;
+    if (exact_used) *exact_used = 1;
+    return orient3d_exact(p, q, r, s);
+}
+
+// calTetQuality_AMIPS (LocalOperations.cpp:862-884) sentinel rule.
+__device__ __forceinline__ double quality_from(int ori, double e) {
+    if (ori != 1) return kMaxEnergy;
+    if (isinf(e) || isnan(e) || e <= 0.0) return kMaxEnergy;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// Point-triangle squared distance, Ericson's Voronoi-region closest point
+// (Real-Time Collision Detection, 2005, sec. 5.1.5); degenerate face region
+// falls back to the three edges.  Same operation order as the oracle.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double seg_sqdist(const V3& p, const V3& a, const V3& b) {
+    V3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
+    V3 ap{p.x - a.x, p.y - a.y, p.z - a.z};
+    double t = dot3(ap, ab), l = dot3(ab, ab);
+    V3 q;
+    if (t <= 0.0 || l <= 0.0) {
+        q = a;
+    } else if (t >= l) {
+        q = b;
+    } else {
+        double s = t / l;
+        q = V3{a.x + s * ab.x, a.y + s * ab.y, a.z + s * ab.z};
+    }
+    V3 d{p.x - q.x, p.y - q.y, p.z - q.z};
+    return dot3(d, d);
+}
+
+__device__ __forceinline__ double point_tri_sqdist(const V3& p, const V3& a, const V3& b,
+                                                   const V3& c) {
+    V3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
+    V3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
+    V3 ap{p.x - a.x, p.y - a.y, p.z - a.z};
+    V3 q;
+    double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) {
+        q = a;
+    } else {
+        V3 bp{p.x - b.x, p.y - b.y, p.z - b.z};
+        double d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+        if (d3 >= 0.0 && d4 <= d3) {
+            q = b;
+        } else {
+            double vc = d1 * d4 - d3 * d2;
+            if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+                double v = d1 / (d1 - d3);
+                q = V3{a.x + v * ab.x, a.y + v * ab.y, a.z + v * ab.z};
+            } else {
+                V3 cp{p.x - c.x, p.y - c.y, p.z - c.z};
+                double d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+                if (d6 >= 0.0 && d5 <= d6) {
+                    q = c;
+                } else {
+                    double vb = d5 * d2 - d1 * d6;
+                    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+                        double w = d2 / (d2 - d6);
+                        q = V3{a.x + w * ac.x, a.y + w * ac.y, a.z + w * ac.z};
+                    } else {
+                        double va = d3 * d6 - d5 * d4;
+                        double d43 = d4 - d3, d56 = d5 - d6;
+                        if (va <= 0.0 && d43 >= 0.0 && d56 >= 0.0) {
+                            double w = d43 / (d43 + d56);
+                            q = V3{b.x + w * (c.x - b.x), b.y + w * (c.y - b.y),
+                                   b.z + w * (c.z - b.z)};
+                        } else {
+                            double den = (va + vb) + vc;
+                            if (!(den > 0.0)) {
+                                double best = seg_sqdist(p, a, b);
+                                double d = seg_sqdist(p, b, c);
+                                if (d < best) best = d;
+                                d = seg_sqdist(p, c, a);
+                                if (d < best) best = d;
+                                return best;
+                            }
+                            double inv = 1.0 / den;
+                            double v = vb * inv, w = vc * inv;
+                            q = V3{(a.x + ab.x * v) + ac.x * w, (a.y + ab.y * v) + ac.y * w,
+                                   (a.z + ab.z * v) + ac.z * w};
+                        }
+                    }
+                }
+            }
+        }
+    }
+    V3 d{p.x - q.x, p.y - q.y, p.z - q.z};
+    return dot3(d, d);
+}
+
+// Outside part of point_box_signed_squared_distance (mesh_AABB.cpp:201-220).
+__device__ __forceinline__ double point_box_sqdist(const V3& p, const double* lo,
+                                                   const double* hi) {
+    double r = 0.0;
+    if (p.x < lo[0]) { double d = p.x - lo[0]; r += d * d; }
+    else if (p.x > hi[0]) { double d = p.x - hi[0]; r += d * d; }
+    if (p.y < lo[1]) { double d = p.y - lo[1]; r += d * d; }
+    else if (p.y > hi[1]) { double d = p.y - hi[1]; r += d * d; }
+    if (p.z < lo[2]) { double d = p.z - lo[2]; r += d * d; }
+    else if (p.z > hi[2]) { double d = p.z - hi[2]; r += d * d; }
+    return r;
+}
+
+}  // namespace tw

@@ -1,0 +1,450 @@
+// tw_envelope.cu -- envelope tests against the device LBVH.
+//
+// Decision (isPointOutEnvelop, LocalOperations.cpp:1034-1044): a point is
+// out iff every facet f has sqdist(p, f) > eps2.  The traversal stops at the
+// first facet with sqdist <= eps2, as facet_in_envelope_recursive does
+// (mesh_AABB.cpp:482-548), and skips a child box only when its squared
+// distance exceeds (eps + tau)^2 with tau = 64 * 2^-53 * max|coord|, which
+// covers the rounding of both the box distance and the facet distance: no
+// facet that tests <= eps2 is ever skipped, so the decision equals the
+// brute-force decision over all facets.
+//
+// Faces (isFaceOutEnvelop_sampling, :1046-1109): a warp per face; the lanes
+// generate sampleTriangle's samples (Common.cpp:143-228) with the same
+// arithmetic as the reference order, each lane first retests the facet that
+// held its previous sample (the reference's prev_facet hint, :1080-1083),
+// and the warp stops at the first sample that is out.
+#include "tw_device.cuh"
+#include "tw_internal.h"
+
+namespace tw {
+
+constexpr int kStack = 64;  // > max depth of a 30-bit LBVH with index tie-break (63)
+
+__device__ __forceinline__ double prune_threshold(const V3& p, double eps2, double scale) {
+    double m = scale;
+    m = fmax(m, fabs(p.x));
+    m = fmax(m, fabs(p.y));
+    m = fmax(m, fabs(p.z));
+    double eps = sqrt(eps2);
+    double tau = 64.0 * kEps * m + 4.0 * kEps * eps;
+    return (eps + tau) * (eps + tau);
+}
+
+__device__ __forceinline__ double leaf_sqdist(const double* __restrict__ tri, int32_t leaf,
+                                              const V3& p) {
+    const double* t = tri + 9 * (int64_t)leaf;
+    V3 a{__ldg(t + 0), __ldg(t + 1), __ldg(t + 2)};
+    V3 b{__ldg(t + 3), __ldg(t + 4), __ldg(t + 5)};
+    V3 c{__ldg(t + 6), __ldg(t + 7), __ldg(t + 8)};
+    return point_tri_sqdist(p, a, b, c);
+}
+
+constexpr int32_t kTraversalError = -2;
+
+// Returns the leaf index of a facet within eps2 of p, -1 if none, or
+// kTraversalError if the walk exceeded its bounds (a tree that is not a
+// tree); every internal node is visited at most once per query.
+__device__ __forceinline__ int32_t find_facet_within(const BvhNode* __restrict__ nodes,
+                                                     const double* __restrict__ tri, int32_t nf,
+                                                     const V3& p, double eps2, double thr) {
+    if (nf == 1) return leaf_sqdist(tri, 0, p) <= eps2 ? 0 : -1;
+    int32_t stack[kStack];
+    int sp = 0;
+    int32_t cur = 0;
+    for (int32_t iter = 0; iter < nf; ++iter) {
+        if ((uint32_t)cur >= (uint32_t)(nf - 1)) return kTraversalError;
+        const double2* nd = reinterpret_cast<const double2*>(nodes + cur);
+        double2 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+        double2 q3 = __ldg(nd + 3), q4 = __ldg(nd + 4), q5 = __ldg(nd + 5);
+        int2 ch = __ldg(reinterpret_cast<const int2*>(nd + 6));
+        double lo0[3] = {q0.x, q0.y, q1.x}, hi0[3] = {q1.y, q2.x, q2.y};
+        double lo1[3] = {q3.x, q3.y, q4.x}, hi1[3] = {q4.y, q5.x, q5.y};
+        double d0 = point_box_sqdist(p, lo0, hi0);
+        double d1 = point_box_sqdist(p, lo1, hi1);
+        bool h0 = d0 <= thr, h1 = d1 <= thr;
+        if (h0 && ch.x < 0) {
+            if ((uint32_t)(~ch.x) >= (uint32_t)nf) return kTraversalError;
+            if (leaf_sqdist(tri, ~ch.x, p) <= eps2) return ~ch.x;
+            h0 = false;
+        }
+        if (h1 && ch.y < 0) {
+            if ((uint32_t)(~ch.y) >= (uint32_t)nf) return kTraversalError;
+            if (leaf_sqdist(tri, ~ch.y, p) <= eps2) return ~ch.y;
+            h1 = false;
+        }
+        if (h0 && h1) {
+            if (sp >= kStack) return kTraversalError;
+            int32_t nearc = (d0 <= d1) ? ch.x : ch.y;
+            int32_t farc = (d0 <= d1) ? ch.y : ch.x;
+            stack[sp++] = farc;
+            cur = nearc;
+        } else if (h0) {
+            cur = ch.x;
+        } else if (h1) {
+            cur = ch.y;
+        } else {
+            if (sp == 0) return -1;
+            cur = stack[--sp];
+        }
+    }
+    return kTraversalError;
+}
+
+__global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P, int64_t n,
+                                                    const BvhNode* __restrict__ nodes,
+                                                    const double* __restrict__ tri, int32_t nf,
+                                                    double scale, double eps2,
+                                                    uint8_t* __restrict__ out,
+                                                    unsigned long long* __restrict__ err) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
+        double thr = prune_threshold(p, eps2, scale);
+        int32_t f = find_facet_within(nodes, tri, nf, p, eps2, thr);
+        if (f == kTraversalError) atomicOr(err, 1ULL);
+        out[i] = (uint8_t)(f == -1);
+    }
+}
+
+void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
+                       unsigned long long* err, cudaStream_t s) {
+    if (n <= 0) return;
+    const int block = 128;
+    k_env_points<<<grid_for(n, block, 16), block, 0, s>>>(P, n, S.nodes, S.tri, S.nf, S.scale,
+                                                          eps2, out, err);
+}
+
+// ---------------------------------------------------------------------------
+// sampleTriangle arithmetic (geogram vec3 semantics, as in the oracle).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3 vsub(const V3& a, const V3& b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 vadd(const V3& a, const V3& b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 vmul(const V3& a, double s) { return V3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 smul(double s, const V3& a) { return V3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V3 vdiv(const V3& a, double s) { return V3{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double vlen2(const V3& a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+__device__ __forceinline__ double vlen(const V3& a) { return sqrt(vlen2(a)); }
+__device__ __forceinline__ double vdist(const V3& a, const V3& b) { return vlen(vsub(a, b)); }
+__device__ __forceinline__ V3 vnormalize(const V3& a) {
+    double s = vlen(a);
+    if (s > 1e-30) s = 1.0 / s;
+    return smul(s, a);
+}
+__device__ __forceinline__ int trunc_int(double x) {
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0) return 2147483647;
+    if (x <= -2147483648.0) return -2147483647 - 1;
+    return (int)x;
+}
+
+// The per-face constants of sampleTriangle.
+struct SampleHeader {
+    V3 vs[3];
+    V3 v0, v1, v2, n01, n02, n12;
+    double ls[3];
+    int max_i;
+    double N;           // base-row bound after the N == int(N) adjustment
+    int trivial;        // N <= 1: the three vertices only
+    int M;              // number of candidate rows (M < 1: base row, v1, v2 only)
+    double sin_v0, tan_v0, sin_v1;
+    double NE, NF;      // edge bounds after the N == int(N) adjustment
+    int hasE, hasF;     // the reference samples an edge only when its raw N > 1
+    V3 nE, nF;          // edge directions v1->v2, v2->v0
+};
+
+__device__ __forceinline__ void sample_header(const double* t, double sd, SampleHeader& h) {
+    const double sqrt3_2 = sqrt(3.0) / 2.0;
+    h.vs[0] = V3{t[0], t[1], t[2]};
+    h.vs[1] = V3{t[3], t[4], t[5]};
+    h.vs[2] = V3{t[6], t[7], t[8]};
+    for (int i = 0; i < 3; ++i) h.ls[i] = vlen2(vsub(h.vs[i], h.vs[(i + 1) % 3]));
+    int max_i = 0;
+    for (int i = 1; i < 3; ++i)
+        if (!(h.ls[i] < h.ls[max_i])) max_i = i;
+    h.max_i = max_i;
+    double N = sqrt(h.ls[max_i]) / sd;
+    h.trivial = (N <= 1) ? 1 : 0;
+    h.M = 0;
+    if (h.trivial) return;
+    if (N == (double)trunc_int(N)) N -= 1;
+    h.N = N;
+    h.v0 = h.vs[max_i];
+    h.v1 = h.vs[(max_i + 1) % 3];
+    h.v2 = h.vs[(max_i + 2) % 3];
+    h.n01 = vnormalize(vsub(h.v1, h.v0));
+    double hh = vdist(vadd(vdiv(smul(dot3(vsub(h.v2, h.v0), vsub(h.v1, h.v0)), vsub(h.v1, h.v0)),
+                               h.ls[max_i]),
+                          h.v0),
+                     h.v2);
+    h.M = trunc_int(hh / (sqrt3_2 * sd));
+    if (h.M < 1) return;
+    h.n02 = vnormalize(vsub(h.v2, h.v0));
+    h.n12 = vnormalize(vsub(h.v2, h.v1));
+    double cr0 = vlen(cross3(vsub(h.v2, h.v0), vsub(h.v1, h.v0)));
+    double cr1 = vlen(cross3(vsub(h.v2, h.v1), vsub(h.v0, h.v1)));
+    h.sin_v0 = cr0 / (vdist(h.v0, h.v2) * vdist(h.v0, h.v1));
+    h.tan_v0 = cr0 / dot3(vsub(h.v2, h.v0), vsub(h.v1, h.v0));
+    h.sin_v1 = cr1 / (vdist(h.v1, h.v2) * vdist(h.v0, h.v1));
+    double NE = sqrt(h.ls[(max_i + 1) % 3]) / sd;
+    h.hasE = NE > 1;
+    if (h.hasE && NE == (double)trunc_int(NE)) NE -= 1;
+    h.NE = NE;
+    h.nE = vnormalize(vsub(h.v2, h.v1));
+    double NF = sqrt(h.ls[(max_i + 2) % 3]) / sd;
+    h.hasF = NF > 1;
+    if (h.hasF && NF == (double)trunc_int(NF)) NF -= 1;
+    h.NF = NF;
+    h.nF = vnormalize(vsub(h.v0, h.v2));
+}
+
+// Row m (1 <= m <= M): start point v and last index N1; returns false when
+// the row triggers the reference's break (distance(v0_m, v1_m) <= sd).
+__device__ __forceinline__ bool sample_row(const SampleHeader& h, double sd, int m, V3& v, int& N1) {
+    const double sqrt3_2 = sqrt(3.0) / 2.0;
+    int n = trunc_int(sqrt3_2 / h.tan_v0 * m + 0.5);
+    int n1 = trunc_int(sqrt3_2 / h.tan_v0 * m);
+    if (m % 2 == 0 && n == n1) n += 1;
+    V3 v0_m = vadd(h.v0, smul((double)m * sqrt3_2 * sd / h.sin_v0, h.n02));
+    V3 v1_m = vadd(h.v1, smul((double)m * sqrt3_2 * sd / h.sin_v1, h.n12));
+    if (vdist(v0_m, v1_m) <= sd) return false;
+    double delta_d = (((double)n + (m % 2) / 2.0) - (double)m * sqrt3_2 / h.tan_v0) * sd;
+    v = vadd(v0_m, smul(delta_d, h.n01));
+    N1 = trunc_int(vdist(v, v1_m) / sd);
+    return true;
+}
+__device__ __forceinline__ V3 row_point(const SampleHeader& h, const V3& v, double sd, int i) {
+    return vadd(v, vmul(smul((double)i, h.n01), sd));
+}
+__device__ __forceinline__ V3 base_point(const SampleHeader& h, double sd, int n) {
+    return vadd(h.v0, vmul(vmul(h.n01, sd), (double)n));
+}
+__device__ __forceinline__ V3 edge_point(const V3& o, const V3& dir, double sd, int n) {
+    return vadd(o, vmul(vmul(dir, sd), (double)n));
+}
+// number of integers n with lo <= n <= N (N a double), lo >= 0
+__device__ __forceinline__ int count_upto(double N, int lo) {
+    if (!(N >= (double)lo)) return 0;
+    double f = floor(N);
+    if (f > 2147483000.0) f = 2147483000.0;
+    return (int)f - lo + 1;
+}
+
+// Exact collinearity (Triangle_3f::is_degenerate): the three 2x2 minors of
+// [a - c, b - c] vanish.
+__device__ __forceinline__ bool minor2_zero(double px, double py, double qx, double qy, double rx,
+                                            double ry) {
+    double a[2], b[2], c[2], d[2], m[16];
+    int na = exp_diff(px, rx, a), nb = exp_diff(qy, ry, b);
+    int nc = exp_diff(py, ry, c), nd = exp_diff(qx, rx, d);
+    int k = exp_minor(a, na, b, nb, c, nc, d, nd, m);
+    return m[k - 1] == 0.0;
+}
+__device__ __noinline__ bool tri_collinear(const double* t) {
+    if (!minor2_zero(t[0], t[1], t[3], t[4], t[6], t[7])) return false;
+    if (!minor2_zero(t[0], t[2], t[3], t[5], t[6], t[8])) return false;
+    return minor2_zero(t[1], t[2], t[4], t[5], t[7], t[8]);
+}
+
+struct FaceCtx {
+    const BvhNode* nodes;
+    const double* tri;
+    int32_t nf;
+    double scale, eps2;
+    unsigned long long* err;
+};
+
+// Largest per-face sample grid the kernel accepts (about 4e6 samples per edge
+// row); a larger face would keep one warp busy for seconds, so it is flagged
+// as an error instead.
+constexpr double kMaxSamplesPerRow = 4.0e6;
+
+__device__ __forceinline__ bool header_too_large(const SampleHeader& h) {
+    if (h.trivial) return false;
+    if (!(h.N <= kMaxSamplesPerRow)) return true;
+    if (h.M > (int)kMaxSamplesPerRow) return true;
+    if (h.M >= 1 && h.hasE && !(h.NE <= kMaxSamplesPerRow)) return true;
+    if (h.M >= 1 && h.hasF && !(h.NF <= kMaxSamplesPerRow)) return true;
+    return false;
+}
+
+// Per-lane sample test with the facet hint.
+__device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_t& hint) {
+    if (hint >= 0 && leaf_sqdist(F.tri, hint, p) <= F.eps2) return false;
+    int32_t f = find_facet_within(F.nodes, F.tri, F.nf, p, F.eps2, prune_threshold(p, F.eps2, F.scale));
+    if (f == kTraversalError) {
+        atomicOr(F.err, 1ULL);
+        return false;
+    }
+    if (f < 0) return true;
+    hint = f;
+    return false;
+}
+
+__global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tris, int64_t n,
+                                                   FaceCtx F, double sd, uint8_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t f = warp; f < n; f += nwarps) {
+        double t[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) t[k] = __ldg(tris + 9 * f + k);
+        if (tri_collinear(t)) {
+            if (lane == 0) out[f] = 0;
+            continue;
+        }
+        SampleHeader h;
+        sample_header(t, sd, h);
+        if (header_too_large(h)) {
+            if (lane == 0) {
+                atomicOr(F.err, 2ULL);
+                out[f] = 1;
+            }
+            continue;
+        }
+        int32_t hint = -1;
+        bool out_found = false;
+        if (h.trivial) {
+            if (lane < 3) out_found = sample_out(F, h.vs[lane], hint);
+            out_found = __any_sync(0xffffffffu, out_found);
+            if (lane == 0) out[f] = out_found ? 1 : 0;
+            continue;
+        }
+        // Row break: first m in [1, M] with distance(v0_m, v1_m) <= sd.
+        int mstop = h.M + 1;
+        if (h.M >= 1) {
+            for (int base = 1; base <= h.M; base += 32) {
+                int m = base + lane;
+                V3 v;
+                int N1 = 0;
+                bool brk = (m <= h.M) && !sample_row(h, sd, m, v, N1);
+                unsigned bal = __ballot_sync(0xffffffffu, brk);
+                if (bal) {
+                    mstop = base + __ffs(bal) - 1;
+                    break;
+                }
+            }
+        }
+        const int NA = count_upto(h.N, 0);
+        const int NE = (h.M >= 1 && h.hasE) ? count_upto(h.NE, 1) : 0;
+        const int NF = (h.M >= 1 && h.hasF) ? count_upto(h.NF, 1) : 0;
+        // Work list per lane: phase 0 base row (strided), 1 vertices v1/v2,
+        // 2 rows (one row per lane at a time), 3 edge v1->v2, 4 edge v2->v0.
+        int phase = 0, idx = lane, row = 1 + lane, rpos = 0, rN1 = -1;
+        V3 rv{0.0, 0.0, 0.0};
+        while (true) {
+            bool have = false;
+            V3 p{0.0, 0.0, 0.0};
+            while (!have && phase < 5) {
+                if (phase == 0) {
+                    if (idx < NA) { p = base_point(h, sd, idx); idx += 32; have = true; }
+                    else { phase = 1; }
+                } else if (phase == 1) {
+                    phase = 2;
+                    if (lane == 0) { p = h.v1; have = true; }
+                    else if (lane == 1) { p = h.v2; have = true; }
+                } else if (phase == 2) {
+                    if (rpos <= rN1) { p = row_point(h, rv, sd, rpos); ++rpos; have = true; }
+                    else if (row < mstop) {
+                        int N1 = -1;
+                        sample_row(h, sd, row, rv, N1);
+                        if (N1 > (int)kMaxSamplesPerRow) {
+                            atomicOr(F.err, 2ULL);
+                            N1 = -1;
+                        }
+                        rN1 = N1;
+                        rpos = 0;
+                        row += 32;
+                    } else { phase = 3; idx = 1 + lane; }
+                } else if (phase == 3) {
+                    if (idx <= NE) { p = edge_point(h.v1, h.nE, sd, idx); idx += 32; have = true; }
+                    else { phase = 4; idx = 1 + lane; }
+                } else {
+                    if (idx <= NF) { p = edge_point(h.v2, h.nF, sd, idx); idx += 32; have = true; }
+                    else { phase = 5; }
+                }
+            }
+            bool o = have ? sample_out(F, p, hint) : false;
+            if (__any_sync(0xffffffffu, o)) { out_found = true; break; }
+            if (__all_sync(0xffffffffu, !have)) break;
+        }
+        if (lane == 0) out[f] = out_found ? 1 : 0;
+    }
+}
+
+void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
+                      uint8_t* out, unsigned long long* err, cudaStream_t s) {
+    if (n <= 0) return;
+    const int block = 128;
+    int64_t warps_needed = n;
+    int grid = grid_for(warps_needed * 32, block, 16);
+    FaceCtx F{S.nodes, S.tri, S.nf, S.scale, eps2, err};
+    k_env_faces<<<grid, block, 0, s>>>(tris, n, F, sd, out);
+}
+
+// One thread generates the full sample list in the reference order with the
+// same helpers (for checking the device sampling arithmetic).  *count = -1
+// when the face exceeds the per-row sample bound.
+__global__ void k_sample_triangle(const double* __restrict__ t, double sd, double* out,
+                                  int64_t cap, int64_t* count) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    {
+        double tv[9];
+        for (int k = 0; k < 9; ++k) tv[k] = t[k];
+        SampleHeader h;
+        sample_header(tv, sd, h);
+        if (header_too_large(h)) {
+            *count = -1;
+            return;
+        }
+    }
+    int64_t cnt = 0;
+    auto emit = [&](const V3& p) {
+        if (cnt < cap) {
+            out[3 * cnt] = p.x;
+            out[3 * cnt + 1] = p.y;
+            out[3 * cnt + 2] = p.z;
+        }
+        ++cnt;
+    };
+    double tv[9];
+    for (int k = 0; k < 9; ++k) tv[k] = t[k];
+    SampleHeader h;
+    sample_header(tv, sd, h);
+    if (h.trivial) {
+        for (int i = 0; i < 3; ++i) emit(h.vs[i]);
+        *count = cnt;
+        return;
+    }
+    for (int n = 0; n <= h.N; ++n) emit(base_point(h, sd, n));
+    emit(h.v1);
+    if (h.M < 1) {
+        emit(h.v2);
+        *count = cnt;
+        return;
+    }
+    for (int m = 1; m <= h.M; ++m) {
+        V3 v;
+        int N1;
+        if (!sample_row(h, sd, m, v, N1)) break;
+        if (N1 > (int)kMaxSamplesPerRow) {
+            *count = -1;
+            return;
+        }
+        for (int i = 0; i <= N1; ++i) emit(row_point(h, v, sd, i));
+    }
+    emit(h.v2);
+    if (h.hasE)
+        for (int n = 1; n <= h.NE; ++n) emit(edge_point(h.v1, h.nE, sd, n));
+    if (h.hasF)
+        for (int n = 1; n <= h.NF; ++n) emit(edge_point(h.v2, h.nF, sd, n));
+    *count = cnt;
+}
+
+void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
+                            int64_t* count, cudaStream_t s) {
+    k_sample_triangle<<<1, 32, 0, s>>>(tri, sd, out, cap, count);
+}
+
+}  // namespace tw

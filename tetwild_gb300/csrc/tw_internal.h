@@ -1,0 +1,113 @@
+// tw_internal.h -- host-side declarations shared by the .cu files of
+// libtw_gb300.so (not part of the public C-ABI; see include/tw_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/tw_gb300.h"
+
+namespace tw {
+
+// Surface BVH (LBVH, Karras 2012) resident in HBM.  Node i (internal,
+// 0 <= i < nf-1) stores the boxes of both children and their indices; a
+// child index c >= 0 is an internal node, c < 0 is leaf ~c.  Leaves are the
+// facets in Morton order; tri holds their 9 coordinates (72 B per facet).
+struct alignas(16) BvhNode {
+    double lo0[3], hi0[3];
+    double lo1[3], hi1[3];
+    int32_t child[2];
+    int32_t pad[6];
+};
+static_assert(sizeof(BvhNode) == 128, "BvhNode must be one 128-byte line");
+
+struct Surface {
+    int32_t nf = 0;
+    BvhNode* nodes = nullptr;   // nf-1 internal nodes (none when nf == 1)
+    double* tri = nullptr;      // 9 * nf, Morton order
+    int32_t* facet_id = nullptr;  // input facet index of each leaf
+    double scale = 0.0;         // max |coordinate| over the surface
+    size_t bytes = 0;
+};
+
+// Device memory block owned by a context, grown on demand.
+struct Buffer {
+    void* ptr = nullptr;
+    size_t cap = 0;
+};
+
+}  // namespace tw
+
+struct tw_ctx {
+    int device = 0;
+    size_t budget = 0;     // bytes of HBM the context may hold (0 = unlimited)
+    size_t used = 0;       // bytes currently held
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_in = nullptr;
+    cudaStream_t copy_out = nullptr;
+    cudaEvent_t ev[8] = {};
+    double eps2 = 0.0;
+    double sampling_dist = 0.0;
+    int newton_max_step = 15;
+    int newton_max_it = 20;
+    tw::Surface surf[2];   // TW_SURFACE_INPUT, TW_SURFACE_BOUNDARY
+    // resident mesh vertices (SoA) and rounded flags
+    double* vx = nullptr;
+    double* vy = nullptr;
+    double* vz = nullptr;
+    uint8_t* rounded = nullptr;
+    int32_t nv = 0;
+    size_t mesh_bytes = 0;
+    tw::Buffer scratch[8];
+    unsigned long long* counters = nullptr;   // device: [0] exact-path count, [1..] spare
+    std::string last_error;
+};
+
+namespace tw {
+
+// Error helpers (implemented in tw_capi.cu).
+int fail(tw_ctx* c, int code, const std::string& msg);
+int cuda_fail(tw_ctx* c, cudaError_t e, const char* where);
+int ensure(tw_ctx* c, int slot, size_t bytes, void** out);
+int dev_alloc(tw_ctx* c, size_t bytes, void** out);
+void dev_free(tw_ctx* c, void* p, size_t bytes);
+
+// Grid size for grid-stride kernels: a multiple of the SM count.
+int grid_for(int64_t n, int block, int blocks_per_sm);
+
+// ---- launchers (tw_amips.cu) ----
+void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
+                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s);
+void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                            const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
+                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s);
+
+// ---- launchers (tw_lbvh.cu) ----
+int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int32_t* dF,
+                  int32_t nf, cudaStream_t s);
+void free_surface(tw_ctx* c, Surface& S);
+
+// ---- launchers (tw_envelope.cu) ----
+// err: device word; bit 0 = traversal exceeded its bounds, bit 1 = a face
+// exceeded the per-row sample bound.
+void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
+                       unsigned long long* err, cudaStream_t s);
+void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
+                      uint8_t* out, unsigned long long* err, cudaStream_t s);
+void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
+                            int64_t* count, cudaStream_t s);
+
+// ---- launchers (tw_newton.cu) ----
+void launch_newton_stars(const double* vx, const double* vy, const double* vz,
+                         const int32_t* star_off, const int32_t* tets, const int32_t* centers,
+                         int32_t nstars, int max_step, int max_it, double* out, uint8_t* moved,
+                         cudaStream_t s);
+
+// ---- peak probes (tw_capi.cu) ----
+void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);
+void launch_fp32_probe(float* out, int iters, int blocks, cudaStream_t s);
+
+}  // namespace tw

@@ -1,0 +1,248 @@
+"""Seeded synthetic inputs with the shapes of the benchmark workloads.
+
+The reference benchmarks on Thingi10k models, which are not available here;
+these generators produce inputs with the stated shapes, sizes and value
+distributions instead:
+
+* ``energy_batch``: regular tets of edge 0.01, centres uniform in the unit
+  cube, uniformly random rotations, every vertex perturbed by N(0, 0.1 edge).
+* ``displaced_sphere``: a lat-long sphere (500 longitudes, 100 latitude rings
+  plus two poles: 100,000 triangles) with radius 1 + sum of real spherical
+  harmonics of degree <= 8, coefficients N(0, 0.02).
+* ``envelope_points``: points uniform by area on a surface, offset along the
+  facet normal by U(-2 eps, 2 eps).
+* ``icosphere``: subdivided icosahedron, vertices jittered radially.
+* ``torus``: lat-long torus.
+* ``star_batch``: independent one-ring stars (a centre vertex and a fan of
+  tets to a jittered convex polyhedron around it), tets per star
+  Poisson(24) clamped to [4, 96].
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+REGULAR_TET = np.array(
+    [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.5, math.sqrt(3.0) / 2.0, 0.0],
+     [0.5, math.sqrt(3.0) / 6.0, math.sqrt(2.0 / 3.0)]])
+
+
+def random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform rotations from normalised Gaussian quaternions, [n, 3, 3]."""
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def energy_batch(n: int, seed: int = 0, edge: float = 0.01, sigma_rel: float = 0.1,
+                 chunk: int = 1 << 20) -> np.ndarray:
+    """SoA [12, n] float64 (the energy_ispc layout)."""
+    rng = np.random.default_rng(seed)
+    T = np.empty((12, n))
+    base = REGULAR_TET * edge
+    base = base - base.mean(0)
+    for i0 in range(0, n, chunk):
+        m = min(chunk, n - i0)
+        R = random_rotations(rng, m)
+        c = rng.random((m, 1, 3))
+        pts = np.einsum("nij,kj->nki", R, base) + c + rng.normal(0.0, sigma_rel * edge, (m, 4, 3))
+        T[:, i0:i0 + m] = pts.reshape(m, 12).T
+    return T
+
+
+def _real_sh_grid(theta: np.ndarray, phi: np.ndarray, lmax: int, coef: dict) -> np.ndarray:
+    """sum_{l<=lmax, |m|<=l} c_lm Y_lm(theta, phi), real orthonormal harmonics, evaluated by
+    the standard associated-Legendre recurrences."""
+    x = np.cos(theta)
+    s = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+    out = np.zeros(np.broadcast(theta, phi).shape)
+    # P[l][m] for m >= 0, Condon-Shortley phase omitted (real basis)
+    P = {}
+    P[(0, 0)] = np.ones_like(x)
+    for m in range(1, lmax + 1):
+        P[(m, m)] = P[(m - 1, m - 1)] * (2 * m - 1) * s
+    for m in range(0, lmax):
+        P[(m + 1, m)] = x * (2 * m + 1) * P[(m, m)]
+    for m in range(0, lmax + 1):
+        for l in range(m + 2, lmax + 1):
+            P[(l, m)] = ((2 * l - 1) * x * P[(l - 1, m)] - (l + m - 1) * P[(l - 2, m)]) / (l - m)
+    for l in range(0, lmax + 1):
+        for m in range(-l, l + 1):
+            am = abs(m)
+            K = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - am) / math.factorial(l + am))
+            if m == 0:
+                Y = K * P[(l, 0)]
+            elif m > 0:
+                Y = math.sqrt(2.0) * K * P[(l, am)] * np.cos(am * phi)
+            else:
+                Y = math.sqrt(2.0) * K * P[(l, am)] * np.sin(am * phi)
+            out = out + coef[(l, m)] * Y
+    return out
+
+
+def displaced_sphere(seed: int = 0, n_lon: int = 500, n_rings: int = 100, lmax: int = 8,
+                     sigma: float = 0.02):
+    """(V [nv,3], F [nf,3]); nf = 2*n_lon*(n_rings-1) + 2*n_lon (100,000 by default)."""
+    rng = np.random.default_rng(seed)
+    coef = {(l, m): rng.normal(0.0, sigma) for l in range(0, lmax + 1) for m in range(-l, l + 1)}
+    j = np.arange(1, n_rings + 1)
+    theta = math.pi * j / (n_rings + 1)
+    phi = 2 * math.pi * np.arange(n_lon) / n_lon
+    TH, PH = np.meshgrid(theta, phi, indexing="ij")
+    r = 1.0 + _real_sh_grid(TH, PH, lmax, coef)
+    ring = np.stack([r * np.sin(TH) * np.cos(PH), r * np.sin(TH) * np.sin(PH), r * np.cos(TH)], -1)
+    rn = 1.0 + _real_sh_grid(np.array([0.0]), np.array([0.0]), lmax, coef)[0]
+    rs = 1.0 + _real_sh_grid(np.array([math.pi]), np.array([0.0]), lmax, coef)[0]
+    V = np.concatenate([ring.reshape(-1, 3), [[0.0, 0.0, rn]], [[0.0, 0.0, -rs]]])
+    north = n_rings * n_lon
+    south = north + 1
+    F = []
+    idx = lambda a, b: a * n_lon + (b % n_lon)
+    for a in range(n_rings - 1):
+        for b in range(n_lon):
+            v00, v01, v10, v11 = idx(a, b), idx(a, b + 1), idx(a + 1, b), idx(a + 1, b + 1)
+            F.append((v00, v10, v11))
+            F.append((v00, v11, v01))
+    for b in range(n_lon):
+        F.append((north, idx(0, b), idx(0, b + 1)))
+        F.append((south, idx(n_rings - 1, b + 1), idx(n_rings - 1, b)))
+    return V, np.asarray(F, np.int32)
+
+
+def envelope_points(V: np.ndarray, F: np.ndarray, n: int, eps: float, seed: int = 1,
+                    chunk: int = 1 << 21) -> np.ndarray:
+    """[n, 3] points uniform by area on (V, F), offset along the facet normal by U(-2eps, 2eps)."""
+    rng = np.random.default_rng(seed)
+    A, B, C = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    nrm = np.cross(B - A, C - A)
+    area = np.linalg.norm(nrm, axis=1)
+    unit = nrm / np.maximum(area, 1e-300)[:, None]
+    cdf = np.cumsum(area)
+    cdf /= cdf[-1]
+    P = np.empty((n, 3))
+    for i0 in range(0, n, chunk):
+        m = min(chunk, n - i0)
+        f = np.minimum(np.searchsorted(cdf, rng.random(m)), len(F) - 1)
+        u, v = rng.random(m), rng.random(m)
+        flip = u + v > 1
+        u[flip], v[flip] = 1 - u[flip], 1 - v[flip]
+        off = rng.uniform(-2 * eps, 2 * eps, m)
+        P[i0:i0 + m] = A[f] + u[:, None] * (B[f] - A[f]) + v[:, None] * (C[f] - A[f]) + off[:, None] * unit[f]
+    return P
+
+
+def icosphere(subdiv: int = 3, radius: float = 1.0, jitter: float = 1e-3, seed: int = 0):
+    """Subdivided icosahedron (subdiv 3: 642 vertices, 1,280 triangles), jittered radially by
+    N(0, jitter)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+         (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    V = [np.array(v, float) / np.linalg.norm(v) for v in V]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+         (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = V[a] + V[b]
+                V.append(m / np.linalg.norm(m))
+                cache[key] = len(V) - 1
+            return cache[key]
+
+        F2 = []
+        for a, b, c in F:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            F2 += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        F = F2
+    V = np.asarray(V) * radius
+    rng = np.random.default_rng(seed)
+    V = V * (1.0 + rng.normal(0.0, jitter, (len(V), 1)) / radius)
+    return V, np.asarray(F, np.int32)
+
+
+def torus(R: float = 1.0, r: float = 0.3, n_major: int = 64, n_minor: int = 32):
+    u = 2 * math.pi * np.arange(n_major) / n_major
+    v = 2 * math.pi * np.arange(n_minor) / n_minor
+    U, W = np.meshgrid(u, v, indexing="ij")
+    V = np.stack([(R + r * np.cos(W)) * np.cos(U), (R + r * np.cos(W)) * np.sin(U), r * np.sin(W)], -1)
+    V = V.reshape(-1, 3)
+    F = []
+    for i in range(n_major):
+        for j in range(n_minor):
+            a = i * n_minor + j
+            b = ((i + 1) % n_major) * n_minor + j
+            c = ((i + 1) % n_major) * n_minor + (j + 1) % n_minor
+            d = i * n_minor + (j + 1) % n_minor
+            F.append((a, b, c))
+            F.append((a, c, d))
+    return V, np.asarray(F, np.int32)
+
+
+def _fib_dirs(k: int) -> np.ndarray:
+    i = np.arange(k) + 0.5
+    z = 1 - 2 * i / k
+    rr = np.sqrt(np.maximum(0, 1 - z * z))
+    ph = math.pi * (1 + math.sqrt(5)) * i
+    return np.stack([rr * np.cos(ph), rr * np.sin(ph), z], -1)
+
+
+def star_batch(nstars: int, seed: int = 0, mean_tets: float = 24.0, lo: int = 4, hi: int = 96,
+               radius: float = 0.01, jitter_rel: float = 0.1, centres=None):
+    """Independent stars sharing no vertices.
+
+    Star i: centre vertex c_i and k = tets/2 + 2 ring points on a jittered sphere of the given
+    radius around it; the convex hull of the ring points (scipy qhull) gives 2k - 4 facets, each
+    fanned to the centre as one tet oriented POSITIVE; then every vertex (centre included) is
+    jittered by N(0, jitter_rel * radius).  Returns (xyz [nv,3], star_off [ns+1], tets [nt,4],
+    centers [ns]).  ``centres`` ([ns,3]) places the stars (default: uniform in the unit cube).
+    """
+    from scipy.spatial import ConvexHull
+
+    rng = np.random.default_rng(seed)
+    ntet = np.clip(rng.poisson(mean_tets, nstars), lo, hi)
+    ntet += ntet % 2  # 2k - 4 is even
+    ntet = np.clip(ntet, lo, hi)
+    if centres is None:
+        centres = rng.random((nstars, 3))
+    hull_cache = {}
+    xyz, off, tets, cen = [], [0], [], []
+    nv = 0
+    for s in range(nstars):
+        k = int(ntet[s]) // 2 + 2
+        if k not in hull_cache:
+            d = _fib_dirs(k)
+            hull_cache[k] = (d, ConvexHull(d).simplices.astype(np.int32))
+        d, simp = hull_cache[k]
+        R = random_rotations(rng, 1)[0]
+        ring = centres[s] + radius * (d @ R.T)
+        c = centres[s]
+        pts = np.vstack([c[None], ring])
+        pts = pts + rng.normal(0.0, jitter_rel * radius, pts.shape)
+        ci = nv
+        for f in simp:
+            a, b, cc = (ci + 1 + int(f[0]), ci + 1 + int(f[1]), ci + 1 + int(f[2]))
+            # orient (centre, a, b, cc) POSITIVE on the unjittered geometry
+            p0, pa, pb, pc = c, ring[f[0]], ring[f[1]], ring[f[2]]
+            det = np.dot(pa - p0, np.cross(pb - p0, pc - p0))
+            tets.append((ci, a, b, cc) if det > 0 else (ci, a, cc, b))
+        xyz.append(pts)
+        nv += len(pts)
+        off.append(len(tets))
+        cen.append(ci)
+    return (np.vstack(xyz), np.asarray(off, np.int32), np.asarray(tets, np.int32),
+            np.asarray(cen, np.int32))
