@@ -33,8 +33,9 @@ def test_amips_energy_batch_bitwise(ctx, oracle):
     assert np.array_equal(g["E"], E)
     assert _same_or_both_nonfinite(g["J"], J)
     assert _same_or_both_nonfinite(g["H"], H)
-    # sanity of the workload: a few percent inverted or flat
-    assert 0.001 < F.mean() < 0.2
+    # sanity of the workload: ~5% near-degenerate (AMIPS energy > 3.5, the
+    # optimum being 3); N(0, 0.1 edge) perturbations invert none
+    assert 0.03 < (E > 3.5).mean() < 0.08
 
 
 def test_amips_raw_mode_and_partial_outputs(ctx, oracle):
