@@ -48,6 +48,7 @@ extern "C" {
 #define TW_ERR_NO_SURFACE (-4)
 #define TW_ERR_NO_MESH (-5)
 #define TW_ERR_TIMEOUT (-6)
+#define TW_ERR_TOO_LARGE (-7)    /* request exceeds a fixed capacity (tw_amips_soa_noalloc) */
 
 /* AMIPS output modes */
 #define TW_ENERGY_RAW 0          /* comformalAMIPSEnergy_new value            */
@@ -87,6 +88,26 @@ TW_API int tw_amips_soa(tw_ctx* ctx, const double* T, int64_t n, int mode, doubl
                  double* H, uint8_t* flip);
 TW_API int tw_amips_soa_device(tw_ctx* ctx, const double* T, int64_t n, int mode, double* E,
                         double* J, double* H, uint8_t* flip);
+
+/* ---- AMIPS batch that allocates nothing -----------------------------------------
+ * No counterpart in the reference (TetWild has no GPU code): this is an extra
+ * entry point for callers that cannot let a library allocate device memory,
+ * such as a host program whose allocator reserves all free HBM at start-up,
+ * or one that must not stall its other streams on the device-wide
+ * synchronisation of cudaFree.  Same inputs, outputs and results as
+ * tw_amips_soa, for at most TW_NOALLOC_MAX_TETS tets per call (larger n
+ * returns TW_ERR_TOO_LARGE); needs no context.  It calls no cudaMalloc or
+ * cudaFree: its scratch is a fixed device array of TW_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this library holds until the process exits.  The
+ * first call on a device looks up that array's address (make it before any
+ * stream capture).  All calls on a device share the array, so calls whose
+ * work overlaps on the GPU race: serialise them.  cuda_stream may be NULL
+ * (the legacy default stream); the call waits for its stream before
+ * returning.                                                                 */
+#define TW_NOALLOC_MAX_TETS 65536
+#define TW_NOALLOC_SCRATCH_BYTES (201 * TW_NOALLOC_MAX_TETS + 256)
+TW_API int tw_amips_soa_noalloc(const double* T, int64_t n, int mode, double* E, double* J,
+                                double* H, uint8_t* flip, void* cuda_stream);
 
 /* ---- resident mesh -----------------------------------------------------------
  * The tet-mesh vertex array (TetVertex::posf / is_rounded,

@@ -29,6 +29,7 @@ TW_ERR_OOM = -3
 TW_ERR_NO_SURFACE = -4
 TW_ERR_NO_MESH = -5
 TW_ERR_TIMEOUT = -6
+TW_ERR_TOO_LARGE = -7
 TW_ENERGY_RAW = 0
 TW_ENERGY_QUALITY = 1
 TW_SURFACE_INPUT = 0
@@ -66,6 +67,7 @@ _SIGS = {
     "tw_memory_used": [_P, ctypes.POINTER(_SZ)],
     "tw_amips_soa": [_P, _P, _I64, _I, _P, _P, _P, _P],
     "tw_amips_soa_device": [_P, _P, _I64, _I, _P, _P, _P, _P],
+    "tw_amips_soa_noalloc": [_P, _I64, _I, _P, _P, _P, _P, _P],
     "tw_mesh_upload": [_P, _P, _I32, _P],
     "tw_mesh_update_vertices": [_P, _P, _P, _P, _I32],
     "tw_tet_quality": [_P, _P, _I64, _P, _P, _P],

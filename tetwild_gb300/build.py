@@ -26,7 +26,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fvisibility=hidden", f"-I{ROOT / 'include'}", f"-I{CSRC}",
     "--expt-relaxed-constexpr",
 ]
-SOURCES = ["tw_amips.cu", "tw_lbvh.cu", "tw_envelope.cu", "tw_newton.cu", "tw_capi.cu"]
+SOURCES = ["tw_amips.cu", "tw_lbvh.cu", "tw_envelope.cu", "tw_newton.cu", "tw_capi.cu",
+           "tw_noalloc.cu"]
 
 
 def nvcc() -> str:
