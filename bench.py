@@ -48,6 +48,14 @@ CPU_SAMPLE_TETS = N_TETS
 CPU_SAMPLE_POINTS = N_POINTS
 
 
+def set_sizes(tets: int, points: int):
+    """Profiling runs use a smaller case of the same workload; the benchmark line
+    always uses the default sizes."""
+    global N_TETS, N_POINTS, CPU_SAMPLE_TETS, CPU_SAMPLE_POINTS
+    N_TETS, N_POINTS = tets, points
+    CPU_SAMPLE_TETS, CPU_SAMPLE_POINTS = tets, points
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -277,7 +285,7 @@ def run_ours(args):
     value = ws * q_step * args.steps / (dev_ms * 1e-3)
 
     # e2e: the same step through the C-ABI with pinned host buffers
-    e2e = run_e2e(ctx, T, P, args, ws)
+    e2e = None if args.no_e2e else run_e2e(ctx, T, P, args, ws)
 
     hbm_peak, peak_kind = measured_peaks()
     ma, me = statistics.mean(t_amips), statistics.mean(t_env)
@@ -419,7 +427,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--tets", type=int, default=N_TETS, help="smaller case for profiling only")
+    ap.add_argument("--points", type=int, default=N_POINTS, help="smaller case for profiling only")
     args = ap.parse_args()
+    set_sizes(args.tets, args.points)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
