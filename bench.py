@@ -38,7 +38,7 @@ sys.path.insert(0, str(ROOT))
 N_TETS = 4_000_000
 N_POINTS = 10_000_000
 EPS = 1e-3
-METRIC = "AMIPS+envelope queries/s (plain FP64, 0 decision mismatches)"
+METRIC = "AMIPS+envelope queries/s vs plain FP64 GPU at 0 decision mismatches; p99 ms"
 UNIT = "queries/s"
 BYTES_PER_TET = 96 + 8 + 24 + 72 + 1     # coords in; E, J, H, flip out
 BYTES_PER_POINT = 24 + 1                 # point in; decision out
@@ -77,6 +77,8 @@ class ClockSampler:
         self.lines = []
 
     def __enter__(self):
+        if self.device < 0:
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
@@ -259,36 +261,44 @@ def run_ours(args):
         if ev:
             ev[2].record(stream)
 
-    for _ in range(args.warmup):
-        step()
-    ctx.synchronize()
-
-    # correctness gate on this very workload: a sample of each output vs the oracle
-    mism = check_sample(T, P, V, F, dE, dFl, dO)
-
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    barrier(ws)
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            step(evs[k])
+    def measure(mode, clocks=True):
+        """W warm-up steps, a correctness gate on this workload, then exactly K timed steps."""
+        ctx.set_precision(mode)
+        for _ in range(args.warmup):
+            step()
         ctx.synchronize()
+        mism = check_sample(T, P, V, F, dE, dFl, dO)
+        ctx.reset_stats()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        barrier(ws)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    t_amips = [evs[k][0].elapsed_time(evs[k][1]) for k in range(args.steps)]
-    t_env = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
-    step_ms = [a + b for a, b in zip(t_amips, t_env)]
-    dev_ms = sum(step_ms)
-    dev_ms = max_over_ranks(dev_ms, ws)
-    q_step = N_TETS + N_POINTS
-    value = ws * q_step * args.steps / (dev_ms * 1e-3)
+        with ClockSampler(dev if clocks else -1) as clk:
+            t0 = time.perf_counter()
+            for k in range(args.steps):
+                step(evs[k])
+            ctx.synchronize()
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        t_amips = [evs[k][0].elapsed_time(evs[k][1]) for k in range(args.steps)]
+        t_env = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
+        step_ms = [a + b for a, b in zip(t_amips, t_env)]
+        dev_ms = max_over_ranks(sum(step_ms), ws)
+        st = ctx.stats()
+        return {"value": ws * (N_TETS + N_POINTS) * args.steps / (dev_ms * 1e-3),
+                "ms_per_step": dev_ms / args.steps, "step_ms": step_ms,
+                "t_amips": statistics.mean(t_amips), "t_env": statistics.mean(t_env),
+                "mism": mism, "stats": st, "clocks": clk.summary() if clocks else None,
+                "wall": wall}
 
-    # e2e: the same step through the C-ABI with pinned host buffers
+    plain = measure(tw.TW_PRECISION_FP64)
+    cert = measure(tw.TW_PRECISION_FP32_CERTIFIED)
+    value = cert["value"]
+
+    # e2e: the same step (certified mode) through the C-ABI with pinned host buffers
     e2e = None if args.no_e2e else run_e2e(ctx, T, P, args, ws)
 
     hbm_peak, peak_kind = measured_peaks()
-    ma, me = statistics.mean(t_amips), statistics.mean(t_env)
+    ma, me = cert["t_amips"], cert["t_env"]
     if me >= ma:
         dom = {"kernel": "k_env_points", "ms": me, "bytes": BYTES_PER_POINT * N_POINTS,
                "units": N_POINTS, "per_unit": BYTES_PER_POINT}
@@ -301,33 +311,46 @@ def run_ours(args):
     if traffic and traffic.get("bytes_per_unit"):
         traffic_bytes = traffic["bytes_per_unit"] * dom["units"]
     flops_per_tet = 260.0   # FP64 operations per tet (orientation filter + E/J/H), static count
-    fp64_achieved = flops_per_tet * N_TETS / (ma * 1e-3) / 1e12
-
-    clocks = clk.summary()
+    fp64_achieved = flops_per_tet * N_TETS / (plain["t_amips"] * 1e-3) / 1e12
+    cst = cert["stats"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": cert["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "isolated query batches, FP64 plain: energy 4M tets "
-                               "(orientation + AMIPS E/J/H) + envelope 10M points vs a 100k-tri "
-                               "displaced sphere, eps=1e-3",
+        "config": {"workload": "isolated query batches: energy 4M tets (orientation + AMIPS "
+                               "E/J/H) + envelope 10M points vs a 100k-tri displaced sphere, "
+                               "eps=1e-3; certified FP32 mode (decisions identical to FP64)",
                    "tets": N_TETS, "points": N_POINTS, "surface_tris": int(len(F)),
                    "l2": "inputs larger than L2 (384 MB tets, 240 MB points); no flush",
                    "parallelism": f"replicas x{ws}"},
-        "p50_ms": float(np.percentile(step_ms, 50)), "p99_ms": float(np.percentile(step_ms, 99)),
-        "kernels_ms": {"k_amips_soa": ma, "k_env_points": me},
-        "decision_mismatches": mism,
+        "p50_ms": float(np.percentile(cert["step_ms"], 50)),
+        "p99_ms": float(np.percentile(cert["step_ms"], 99)),
+        "kernels_ms": {"amips_step": ma, "envelope_step": me},
+        "decision_mismatches": cert["mism"],
+        "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"],
+                       "kernels_ms": {"amips_step": plain["t_amips"],
+                                      "envelope_step": plain["t_env"]},
+                       "decision_mismatches": plain["mism"],
+                       "p99_ms": float(np.percentile(plain["step_ms"], 99)),
+                       "speedup_of_value": value / plain["value"]},
+        "precision": {"env_facet_tests": cst["env_facet_tests"],
+                      "env_facet_fp64": cst["env_facet_fp64"],
+                      "env_recheck_fraction": cst["env_facet_fp64"] / max(1, cst["env_facet_tests"]),
+                      "amips_tets": cst["amips_tets"], "amips_fp64": cst["amips_fp64"],
+                      "amips_recheck_fraction": cst["amips_fp64"] / max(1, cst["amips_tets"]),
+                      "exact_orientations": cst["exact_orientations"]},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "traffic": traffic_bytes, "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_unit": dom["per_unit"]},
-        "fp64_pipe": {"kernel": "k_amips_soa", "achieved_tflops": fp64_achieved,
+        "fp64_pipe": {"kernel": "k_amips_soa (plain FP64)", "achieved_tflops": fp64_achieved,
                       "peak_tflops_measured": fp64_tflops, "frac": fp64_achieved / fp64_tflops,
                       "flops_per_tet": flops_per_tet, "fp32_peak_tflops_measured": fp32_tflops},
         "e2e": e2e,
-        "gpu_launches": 2 * args.steps,
-        "clocks": clocks,
-        "wall_s_timed": wall,
+        "gpu_launches": 3 * args.steps,
+        "gpu_launches_note": "per step: k_amips_soa, k_point_codes, k_env_points (+4 CUB radix-sort kernels)",
+        "clocks": cert["clocks"],
+        "wall_s_timed": cert["wall"],
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle.oracle import default_threads

@@ -54,6 +54,12 @@ extern "C" {
 #define TW_ENERGY_RAW 0          /* comformalAMIPSEnergy_new value            */
 #define TW_ENERGY_QUALITY 1      /* calTetQuality_AMIPS value (1e50 sentinel) */
 
+/* arithmetic modes (tw_set_precision) */
+#define TW_PRECISION_FP64 0            /* every query in binary64 (default)        */
+#define TW_PRECISION_FP32_CERTIFIED 1  /* binary32 bulk with certified error bounds;
+                                          binary64 recomputation inside the band:
+                                          decisions identical to TW_PRECISION_FP64 */
+
 /* surfaces */
 #define TW_SURFACE_INPUT 0       /* geo_sf_tree (MeshRefinement.cpp:209)      */
 #define TW_SURFACE_BOUNDARY 1    /* geo_b_tree  (MeshRefinement.cpp:213)      */
@@ -74,6 +80,25 @@ TW_API int tw_stream(tw_ctx* ctx, void** cuda_stream);
 TW_API int tw_synchronize(tw_ctx* ctx);
 /* Device bytes currently held by the context (mesh, surfaces, scratch).   */
 TW_API int tw_memory_used(const tw_ctx* ctx, size_t* bytes);
+
+/* ---- precision mode and statistics -----------------------------------------------
+ * No counterpart in the reference (its arithmetic is binary64 throughout).
+ * TW_PRECISION_FP32_CERTIFIED evaluates the bulk in binary32 and recomputes
+ * in binary64 every query whose binary32 result falls inside a certified
+ * error band (envelope: facets whose certified lower distance bound does not
+ * exceed eps; AMIPS: tets whose certified relative error bound exceeds
+ * 1e-5), so every decision equals the binary64 one.                         */
+TW_API int tw_set_precision(tw_ctx* ctx, int mode);
+typedef struct tw_stats {
+    uint64_t exact_orientations;   /* orientation signs that needed the exact path */
+    uint64_t env_queries;          /* envelope points and face samples queried      */
+    uint64_t env_facet_tests;      /* facets reached by the traversals              */
+    uint64_t env_facet_fp64;       /* of those, evaluated in binary64               */
+    uint64_t amips_tets;           /* tets evaluated by the AMIPS kernels           */
+    uint64_t amips_fp64;           /* of those, recomputed in binary64 (certified)  */
+} tw_stats;
+TW_API int tw_get_stats(tw_ctx* ctx, tw_stats* out);
+TW_API int tw_reset_stats(tw_ctx* ctx);
 
 /* ---- AMIPS energy / gradient / Hessian -------------------------------------
  * Replaces: LocalOperations::comformalAMIPSEnergy_new (LocalOperations.cpp:28,

@@ -56,8 +56,22 @@ _I64 = ctypes.c_int64
 _D = ctypes.c_double
 _SZ = ctypes.c_size_t
 
+TW_PRECISION_FP64 = 0
+TW_PRECISION_FP32_CERTIFIED = 1
+
+_STAT_FIELDS = ("exact_orientations", "env_queries", "env_facet_tests", "env_facet_fp64",
+                "amips_tets", "amips_fp64")
+
+
+class TwStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in _STAT_FIELDS]
+
+
 # name -> argtypes (restype int unless noted)
 _SIGS = {
+    "tw_set_precision": [_P, _I],
+    "tw_get_stats": [_P, ctypes.POINTER(TwStats)],
+    "tw_reset_stats": [_P],
     "tw_ctx_create": [_I, _SZ, ctypes.POINTER(_P)],
     "tw_ctx_destroy": [_P],
     "tw_last_error": [_P],
@@ -173,6 +187,18 @@ class Context:
         b = _SZ()
         self._check(self.lib.tw_memory_used(self.h, ctypes.byref(b)))
         return b.value
+
+    def set_precision(self, mode: int):
+        """TW_PRECISION_FP64 or TW_PRECISION_FP32_CERTIFIED (same decisions)."""
+        self._check(self.lib.tw_set_precision(self.h, mode))
+
+    def stats(self) -> dict:
+        s = TwStats()
+        self._check(self.lib.tw_get_stats(self.h, ctypes.byref(s)))
+        return {f: int(getattr(s, f)) for f in _STAT_FIELDS}
+
+    def reset_stats(self):
+        self._check(self.lib.tw_reset_stats(self.h))
 
     # -- AMIPS --------------------------------------------------------------------
     def amips(self, T_soa, mode=TW_ENERGY_QUALITY, energy=True, jacobian=True, hessian=True,

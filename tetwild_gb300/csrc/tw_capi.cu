@@ -136,7 +136,8 @@ struct Guard {
     explicit Guard(int dev) { cudaSetDevice(dev); }
 };
 
-// scratch slot layout: pipelines use slots [0, kNumPipe), misc uses 6, 7
+// scratch slot layout: pipelines use slots [0, kNumPipe), their point-ordering
+// scratch [3, 3 + kNumPipe), misc uses 6, 7
 int sync_status(tw_ctx* c, const char* where) {
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->copy_in);
@@ -144,12 +145,12 @@ int sync_status(tw_ctx* c, const char* where) {
     if (e != cudaSuccess) return cuda_fail(c, e, where);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, where);
-    // device-side error word (counters[2]): read and clear
+    // device-side error word: read and clear
     unsigned long long err = 0;
-    e = cudaMemcpy(&err, c->counters + 2, sizeof(err), cudaMemcpyDeviceToHost);
+    e = cudaMemcpy(&err, c->counters + kCntError, sizeof(err), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, where);
     if (err) {
-        cudaMemset(c->counters + 2, 0, sizeof(err));
+        cudaMemset(c->counters + kCntError, 0, sizeof(err));
         std::string m = std::string(where) + ": ";
         if (err & 1ULL) m += "surface traversal exceeded its bounds (corrupt tree); ";
         if (err & 2ULL) m += "a face exceeds the per-row sample bound (4e6 samples); ";
@@ -198,12 +199,12 @@ int tw_ctx_create(int device, size_t hbm_budget_bytes, tw_ctx** out) {
     }
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     void* cnt = nullptr;
-    if (dev_alloc(c, 8 * sizeof(unsigned long long), &cnt) != TW_OK) {
+    if (dev_alloc(c, kNumCounters * sizeof(unsigned long long), &cnt) != TW_OK) {
         tw_ctx_destroy(c);
         return TW_ERR_OOM;
     }
     c->counters = (unsigned long long*)cnt;
-    cudaMemset(c->counters, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(c->counters, 0, kNumCounters * sizeof(unsigned long long));
     *out = c;
     return TW_OK;
 }
@@ -220,7 +221,7 @@ int tw_ctx_destroy(tw_ctx* c) {
     dev_free(c, c->vz, sizeof(double) * (size_t)c->nv);
     dev_free(c, c->rounded, (size_t)c->nv);
     for (auto& b : c->scratch) dev_free(c, b.ptr, b.cap);
-    dev_free(c, c->counters, 8 * sizeof(unsigned long long));
+    dev_free(c, c->counters, kNumCounters * sizeof(unsigned long long));
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -260,6 +261,42 @@ int tw_memory_used(const tw_ctx* c, size_t* bytes) {
     if (!c || !bytes) return TW_ERR_ARG;
     *bytes = c->used;
     return TW_OK;
+}
+
+int tw_set_precision(tw_ctx* c, int mode) {
+    if (!c) return TW_ERR_ARG;
+    if (mode != TW_PRECISION_FP64 && mode != TW_PRECISION_FP32_CERTIFIED)
+        return fail(c, TW_ERR_ARG, "tw_set_precision: unknown mode");
+    c->precision = mode;
+    return TW_OK;
+}
+
+int tw_get_stats(tw_ctx* c, tw_stats* out) {
+    if (!c || !out) return TW_ERR_ARG;
+    Guard g(c->device);
+    int st = sync_status(c, "tw_get_stats");
+    if (st != TW_OK) return st;
+    unsigned long long h[kNumCounters] = {};
+    cudaError_t e = cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_get_stats");
+    out->exact_orientations = h[kCntExactOrient];
+    out->env_queries = h[kCntEnvQueries];
+    out->env_facet_tests = h[kCntEnvFacetTests];
+    out->env_facet_fp64 = h[kCntEnvFp64];
+    out->amips_tets = h[kCntAmipsTets];
+    out->amips_fp64 = h[kCntAmipsFp64];
+    return TW_OK;
+}
+
+int tw_reset_stats(tw_ctx* c) {
+    if (!c) return TW_ERR_ARG;
+    Guard g(c->device);
+    int st = sync_status(c, "tw_reset_stats");
+    if (st != TW_OK) return st;
+    const int keep[] = {kCntExactOrient, kCntEnvQueries, kCntEnvFacetTests, kCntEnvFp64,
+                        kCntAmipsTets, kCntAmipsFp64};
+    for (int k : keep) cudaMemset(c->counters + k, 0, sizeof(unsigned long long));
+    return sync_status(c, "tw_reset_stats");
 }
 
 // ---- AMIPS -------------------------------------------------------------------
@@ -466,7 +503,11 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
     if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
     if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
     Guard g(c->device);
-    launch_env_points(c->surf[which], P, n, c->eps2, out, c->counters + 2, c->stream);
+    void* sort = nullptr;
+    int st = ensure(c, 3, env_sort_scratch_bytes(n), &sort);
+    if (st != TW_OK) return st;
+    launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters, sort,
+                      c->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
     return TW_OK;
@@ -481,12 +522,15 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
     const int64_t C = chunk_len(n, 25);
     double* dP[kNumPipe];
     uint8_t* dO[kNumPipe];
+    void* dS[kNumPipe];
     for (int k = 0; k < kNumPipe; ++k) {
         void* p;
         int st = ensure(c, k, 25 * (size_t)C + 256, &p);
         if (st != TW_OK) return st;
         dP[k] = (double*)p;
         dO[k] = (uint8_t*)p + 24 * (size_t)C;
+        st = ensure(c, 3 + k, env_sort_scratch_bytes(C), &dS[k]);
+        if (st != TW_OK) return st;
     }
     int64_t chunk = 0;
     for (int64_t i0 = 0; i0 < n; i0 += C, ++chunk) {
@@ -494,7 +538,8 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         cudaStream_t s = pipe_stream(c, k);
         const int64_t len = std::min<int64_t>(C, n - i0);
         cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
-        launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->counters + 2, s);
+        launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->precision, c->counters,
+                          dS[k], s);
         cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
     }
     return sync_status(c, "tw_envelope_points");
@@ -506,7 +551,7 @@ int tw_envelope_faces_device(tw_ctx* c, const double* tris, int64_t n, uint8_t* 
     if (!(c->sampling_dist > 0.0)) return fail(c, TW_ERR_ARG, "sampling_dist must be > 0");
     Guard g(c->device);
     launch_env_faces(c->surf[TW_SURFACE_INPUT], tris, n, c->eps2, c->sampling_dist, out,
-                     c->counters + 2, c->stream);
+                     c->precision, c->counters, c->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_faces_device");
     return TW_OK;
@@ -525,7 +570,7 @@ int tw_envelope_faces(tw_ctx* c, const double* tris, int64_t n, uint8_t* out) {
     uint8_t* dO = (uint8_t*)p + 72 * (size_t)n;
     cudaMemcpyAsync(dT, tris, 72 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
     launch_env_faces(c->surf[TW_SURFACE_INPUT], dT, n, c->eps2, c->sampling_dist, dO,
-                     c->counters + 2, c->stream);
+                     c->precision, c->counters, c->stream);
     cudaMemcpyAsync(out, dO, (size_t)n, cudaMemcpyDeviceToHost, c->stream);
     return sync_status(c, "tw_envelope_faces");
 }

@@ -66,6 +66,16 @@ __device__ __forceinline__ double icbrt(double x) {
 struct V3 {
     double x, y, z;
 };
+
+// Spreads the low 10 bits of v so that bit k moves to bit 3k (one axis of a
+// 30-bit Morton code).
+__device__ __forceinline__ uint32_t morton_expand10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
 __device__ __forceinline__ double dot3(const V3& u, const V3& v) {
     return (u.x * v.x + u.y * v.y) + u.z * v.z;
 }

@@ -14,6 +14,8 @@
 // arithmetic as the reference order, each lane first retests the facet that
 // held its previous sample (the reference's prev_facet hint, :1080-1083),
 // and the warp stops at the first sample that is out.
+#include <cub/device/device_radix_sort.cuh>
+
 #include "tw_device.cuh"
 #include "tw_internal.h"
 
@@ -42,13 +44,185 @@ __device__ __forceinline__ double leaf_sqdist(const double* __restrict__ tri, in
 
 constexpr int32_t kTraversalError = -2;
 
+// ---------------------------------------------------------------------------
+// Certified binary32 culling (TW_PRECISION_FP32_CERTIFIED).
+//
+// Boxes: binary32 copies rounded outward; the point is rounded to binary32
+// (error <= 2^-24 M per coordinate, M = max |coordinate|); a child is
+// skipped only when its computed squared distance exceeds
+// (eps (1 + 2^-20) + tau32)^2, tau32 = 2^-21 M + 2^-20 eps, which covers the
+// point rounding (sqrt3 2^-24 M) and the rounding of the distance (3 u eps).
+//
+// Facets: d(p, f)^2 >= h^2 + max(0, max_e s_e)^2, with h the distance of p to
+// the facet's plane and s_e the signed distance of p to the in-plane
+// half-plane of edge e (the facet lies in the plane and inside every edge's
+// half-plane, and the plane and a half-plane boundary are orthogonal).  h and
+// s_e are evaluated in binary32 from r = p - a (rounded from FP64) with the
+// stored unit normals; their error is below 8 u |r|_1 (+ 8 u |c_e|), u = 2^-24
+// (rounding of r: u|r|_1, of the normal: u|r|_1, of the 3-term dot: 3.01 u|r|_1,
+// of the offset and the subtraction: 2u(|r|_1 + |c_e|)).  The facet is
+// skipped only when the lower bound computed from (|h| - delta)+ and
+// (s_e - delta_e)+ exceeds eps^2 (1 + 2^-18), rounded up: then the exact
+// distance exceeds eps by far more than the error of the FP64 evaluation, so
+// the FP64 test would also have found d^2 > eps^2.  Every other facet is
+// evaluated in FP64 exactly as in TW_PRECISION_FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
+
+__device__ __forceinline__ float box_thr32(const V3& p, double eps2, double scale) {
+    double m = scale;
+    m = fmax(m, fabs(p.x));
+    m = fmax(m, fabs(p.y));
+    m = fmax(m, fabs(p.z));
+    double eps = sqrt(eps2);
+    double tau = 4.76837158203125e-07 * m + 9.5367431640625e-07 * eps;
+    double e = eps * (1.0 + 9.5367431640625e-07) + tau;
+    return round_up_f(e * e);
+}
+
+__device__ __forceinline__ float point_box_sqdist32(float px, float py, float pz, const float* lo,
+                                                    const float* hi) {
+    float r = 0.0f;
+    if (px < lo[0]) { float d = lo[0] - px; r = d * d; }
+    else if (px > hi[0]) { float d = px - hi[0]; r = d * d; }
+    if (py < lo[1]) { float d = lo[1] - py; r = r + d * d; }
+    else if (py > hi[1]) { float d = py - hi[1]; r = r + d * d; }
+    if (pz < lo[2]) { float d = lo[2] - pz; r = r + d * d; }
+    else if (pz > hi[2]) { float d = pz - hi[2]; r = r + d * d; }
+    return r;
+}
+
+// True when facet f is certainly farther than eps from p (see above).
+__device__ __forceinline__ bool facet_certainly_out(const FacetCull* __restrict__ cull, int32_t f,
+                                                    const V3& p, float eps2hi) {
+    const float4* q = reinterpret_cast<const float4*>(cull + f);
+    const double2* qd = reinterpret_cast<const double2*>(cull + f);
+    double2 a01 = __ldg(qd);
+    float4 w1 = __ldg(q + 1);  // a.z (as two floats), n.x, n.y
+    float4 w2 = __ldg(q + 2);  // n.z, ne0.xyz
+    float4 w3 = __ldg(q + 3);  // ne1.xyz, ne2.x
+    float4 w4 = __ldg(q + 4);  // ne2.yz, c0, c1
+    float4 w5 = __ldg(q + 5);  // c2, ok, pad
+    if (__float_as_uint(w5.y) == 0u) return false;
+    double az = __ldg(reinterpret_cast<const double*>(cull + f) + 2);
+    float rx = __double2float_rn(p.x - a01.x);
+    float ry = __double2float_rn(p.y - a01.y);
+    float rz = __double2float_rn(p.z - az);
+    float R1 = fabsf(rx) + fabsf(ry) + fabsf(rz);
+    const float k8u = 4.76837158203125e-07f;  // 8 * 2^-24
+    float h = fmaf(w2.x, rz, fmaf(w1.w, ry, w1.z * rx));
+    float hl = fmaxf(fabsf(h) - k8u * R1, 0.0f);
+    float s0 = fmaf(w2.w, rz, fmaf(w2.z, ry, w2.y * rx)) - w4.z;
+    float s1 = fmaf(w3.z, rz, fmaf(w3.y, ry, w3.x * rx)) - w4.w;
+    float s2 = fmaf(w4.y, rz, fmaf(w4.x, ry, w3.w * rx)) - w5.x;
+    s0 -= k8u * (R1 + fabsf(w4.z));
+    s1 -= k8u * (R1 + fabsf(w4.w));
+    s2 -= k8u * (R1 + fabsf(w5.x));
+    float sl = fmaxf(fmaxf(s0, s1), fmaxf(s2, 0.0f));
+    float L2 = fmaf(sl, sl, hl * hl);
+    return L2 > eps2hi;
+}
+
+struct TravStats {
+    uint32_t facets = 0;  // facets reached
+    uint32_t fp64 = 0;    // facets evaluated in FP64
+};
+
+// FP32-culled traversal; decisions identical to find_facet_within (FP64).
+__device__ __forceinline__ int32_t find_facet_within32(const BvhNode32* __restrict__ nodes,
+                                                       const FacetCull* __restrict__ cull,
+                                                       const double* __restrict__ tri, int32_t nf,
+                                                       const V3& p, double eps2, float thr32,
+                                                       float eps2hi, TravStats& st) {
+    if (nf == 1) {
+        ++st.facets;
+        if (facet_certainly_out(cull, 0, p, eps2hi)) return -1;
+        ++st.fp64;
+        return leaf_sqdist(tri, 0, p) <= eps2 ? 0 : -1;
+    }
+    const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
+                pz = __double2float_rn(p.z);
+    int32_t stack[kStack];
+    int sp = 0;
+    int32_t cur = 0;
+    for (int32_t iter = 0; iter < nf; ++iter) {
+        if ((uint32_t)cur >= (uint32_t)(nf - 1)) return kTraversalError;
+        const float4* nd = reinterpret_cast<const float4*>(nodes + cur);
+        float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+        int4 q3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
+        float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
+        float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
+        int2 ch = make_int2(q3.x, q3.y);
+        float d0 = point_box_sqdist32(px, py, pz, lo0, hi0);
+        float d1 = point_box_sqdist32(px, py, pz, lo1, hi1);
+        bool h0 = d0 <= thr32, h1 = d1 <= thr32;
+        if (h0 && ch.x < 0) {
+            int32_t lf = ~ch.x;
+            if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
+            ++st.facets;
+            if (!facet_certainly_out(cull, lf, p, eps2hi)) {
+                ++st.fp64;
+                if (leaf_sqdist(tri, lf, p) <= eps2) return lf;
+            }
+            h0 = false;
+        }
+        if (h1 && ch.y < 0) {
+            int32_t lf = ~ch.y;
+            if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
+            ++st.facets;
+            if (!facet_certainly_out(cull, lf, p, eps2hi)) {
+                ++st.fp64;
+                if (leaf_sqdist(tri, lf, p) <= eps2) return lf;
+            }
+            h1 = false;
+        }
+        if (h0 && h1) {
+            if (sp >= kStack) return kTraversalError;
+            int32_t nearc = (d0 <= d1) ? ch.x : ch.y;
+            int32_t farc = (d0 <= d1) ? ch.y : ch.x;
+            stack[sp++] = farc;
+            cur = nearc;
+        } else if (h0) {
+            cur = ch.x;
+        } else if (h1) {
+            cur = ch.y;
+        } else {
+            if (sp == 0) return -1;
+            cur = stack[--sp];
+        }
+    }
+    return kTraversalError;
+}
+
+// One atomic per warp for the traversal statistics.
+__device__ __forceinline__ void flush_stats(const TravStats& st, unsigned long long* counters,
+                                            uint32_t queries) {
+    unsigned long long a = st.facets, b = st.fp64, q = queries;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicAdd(counters + kCntEnvFacetTests, a);
+        if (b) atomicAdd(counters + kCntEnvFp64, b);
+        if (q) atomicAdd(counters + kCntEnvQueries, q);
+    }
+}
+
 // Returns the leaf index of a facet within eps2 of p, -1 if none, or
 // kTraversalError if the walk exceeded its bounds (a tree that is not a
 // tree); every internal node is visited at most once per query.
 __device__ __forceinline__ int32_t find_facet_within(const BvhNode* __restrict__ nodes,
                                                      const double* __restrict__ tri, int32_t nf,
-                                                     const V3& p, double eps2, double thr) {
-    if (nf == 1) return leaf_sqdist(tri, 0, p) <= eps2 ? 0 : -1;
+                                                     const V3& p, double eps2, double thr,
+                                                     TravStats& st) {
+    if (nf == 1) {
+        ++st.facets;
+        ++st.fp64;
+        return leaf_sqdist(tri, 0, p) <= eps2 ? 0 : -1;
+    }
     int32_t stack[kStack];
     int sp = 0;
     int32_t cur = 0;
@@ -65,11 +239,15 @@ __device__ __forceinline__ int32_t find_facet_within(const BvhNode* __restrict__
         bool h0 = d0 <= thr, h1 = d1 <= thr;
         if (h0 && ch.x < 0) {
             if ((uint32_t)(~ch.x) >= (uint32_t)nf) return kTraversalError;
+            ++st.facets;
+            ++st.fp64;
             if (leaf_sqdist(tri, ~ch.x, p) <= eps2) return ~ch.x;
             h0 = false;
         }
         if (h1 && ch.y < 0) {
             if ((uint32_t)(~ch.y) >= (uint32_t)nf) return kTraversalError;
+            ++st.facets;
+            ++st.fp64;
             if (leaf_sqdist(tri, ~ch.y, p) <= eps2) return ~ch.y;
             h1 = false;
         }
@@ -91,28 +269,145 @@ __device__ __forceinline__ int32_t find_facet_within(const BvhNode* __restrict__
     return kTraversalError;
 }
 
-__global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P, int64_t n,
-                                                    const BvhNode* __restrict__ nodes,
-                                                    const double* __restrict__ tri, int32_t nf,
-                                                    double scale, double eps2,
-                                                    uint8_t* __restrict__ out,
-                                                    unsigned long long* __restrict__ err) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
-        double thr = prune_threshold(p, eps2, scale);
-        int32_t f = find_facet_within(nodes, tri, nf, p, eps2, thr);
-        if (f == kTraversalError) atomicOr(err, 1ULL);
-        out[i] = (uint8_t)(f == -1);
-    }
+// Query i of the launch is point order[i] (order == nullptr: point i).  With
+// the points in Morton order, the lanes of a warp query neighbouring points
+// and walk the same nodes: the warp stays converged and the nodes it reads
+// are shared in L1.
+struct EnvTree {
+    const BvhNode* nodes;
+    const BvhNode32* nodes32;
+    const FacetCull* cull;
+    const double* tri;
+    int32_t nf;
+    double scale;
+};
+
+template <bool FP32>
+__device__ __forceinline__ int32_t query_point(const EnvTree& T, const V3& p, double eps2,
+                                               float eps2hi, TravStats& st) {
+    if (FP32)
+        return find_facet_within32(T.nodes32, T.cull, T.tri, T.nf, p, eps2,
+                                   box_thr32(p, eps2, T.scale), eps2hi, st);
+    return find_facet_within(T.nodes, T.tri, T.nf, p, eps2, prune_threshold(p, eps2, T.scale), st);
 }
 
+__device__ __forceinline__ float eps2_hi(double eps2) {
+    return round_up_f(eps2 * (1.0 + 3.814697265625e-06));  // eps^2 (1 + 2^-18)
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P,
+                                                    const int32_t* __restrict__ order, int64_t n,
+                                                    EnvTree T, double eps2,
+                                                    uint8_t* __restrict__ out,
+                                                    unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const float e2hi = eps2_hi(eps2);
+    TravStats st;
+    uint32_t nq = 0;
+    // every lane runs the same number of iterations so the final warp
+    // reduction of the statistics is converged
+    const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t base0 = first - (threadIdx.x & 31);
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + (threadIdx.x & 31);
+        if (i < n) {
+            const int64_t j = order ? (int64_t)__ldg(order + i) : i;
+            V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
+            int32_t f = query_point<FP32>(T, p, eps2, e2hi, st);
+            if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
+            out[j] = (uint8_t)(f == -1);
+            ++nq;
+        }
+    }
+    flush_stats(st, counters, nq);
+}
+
+// 30-bit Morton code of each query point on the tree's centroid grid
+// (points outside the grid clamp to its faces).
+__global__ void k_point_codes(const double* __restrict__ P, int64_t n, double lx, double ly,
+                              double lz, double sx, double sy, double sz,
+                              uint32_t* __restrict__ codes, int32_t* __restrict__ idx) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double c[3] = {(__ldg(P + 3 * i) - lx) * sx, (__ldg(P + 3 * i + 1) - ly) * sy,
+                   (__ldg(P + 3 * i + 2) - lz) * sz};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = c[k] * 1024.0;
+        v = fmin(fmax(v, 0.0), 1023.0);  // NaN -> 0
+        q[k] = (uint32_t)v;
+    }
+    codes[i] = (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
+    idx[i] = (int32_t)i;
+}
+
+struct SortLayout {
+    uint32_t* codes;
+    uint32_t* codes2;
+    int32_t* idx;
+    int32_t* idx2;
+    void* temp;
+    size_t temp_bytes;
+};
+
+static size_t cub_sort_bytes(int64_t n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (int32_t*)nullptr, (int32_t*)nullptr, (int)n, 0, 30);
+    return b;
+}
+
+static SortLayout sort_layout(void* base, int64_t n) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    char* q = static_cast<char*>(base);
+    SortLayout L;
+    L.codes = (uint32_t*)q; q += al(4 * (size_t)n);
+    L.codes2 = (uint32_t*)q; q += al(4 * (size_t)n);
+    L.idx = (int32_t*)q; q += al(4 * (size_t)n);
+    L.idx2 = (int32_t*)q; q += al(4 * (size_t)n);
+    L.temp = q;
+    L.temp_bytes = cub_sort_bytes(n);
+    return L;
+}
+
+size_t env_sort_scratch_bytes(int64_t n) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    return 4 * al(4 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
+}
+
+// Batches below this size are traversed in input order (sorting would cost
+// more than it saves).
+constexpr int64_t kSortMin = 4096;
+
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
-                       unsigned long long* err, cudaStream_t s) {
+                       int precision, unsigned long long* counters, void* sort_scratch,
+                       cudaStream_t s) {
     if (n <= 0) return;
     const int block = 128;
-    k_env_points<<<grid_for(n, block, 16), block, 0, s>>>(P, n, S.nodes, S.tri, S.nf, S.scale,
-                                                          eps2, out, err);
+    const int32_t* order = nullptr;
+    if (sort_scratch && n >= kSortMin && n <= INT32_MAX) {
+        SortLayout L = sort_layout(sort_scratch, n);
+        double sc[3];
+        for (int k = 0; k < 3; ++k) {
+            double ext = S.hi[k] - S.lo[k];
+            sc[k] = ext > 0.0 ? 1.0 / ext : 0.0;
+        }
+        k_point_codes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+            P, n, S.lo[0], S.lo[1], S.lo[2], sc[0], sc[1], sc[2], L.codes, L.idx);
+        size_t tb = L.temp_bytes;
+        cub::DeviceRadixSort::SortPairs(L.temp, tb, L.codes, L.codes2, L.idx, L.idx2, (int)n, 0, 30,
+                                        s);
+        order = L.idx2;
+    }
+    EnvTree T{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale};
+    if (precision == TW_PRECISION_FP32_CERTIFIED)
+        k_env_points<true><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, eps2, out,
+                                                                    counters);
+    else
+        k_env_points<false><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, eps2, out,
+                                                                     counters);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,11 +542,10 @@ __device__ __noinline__ bool tri_collinear(const double* t) {
 }
 
 struct FaceCtx {
-    const BvhNode* nodes;
-    const double* tri;
-    int32_t nf;
-    double scale, eps2;
-    unsigned long long* err;
+    EnvTree T;
+    double eps2;
+    float eps2hi;
+    unsigned long long* counters;
 };
 
 // Largest per-face sample grid the kernel accepts (about 4e6 samples per edge
@@ -269,11 +563,20 @@ __device__ __forceinline__ bool header_too_large(const SampleHeader& h) {
 }
 
 // Per-lane sample test with the facet hint.
-__device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_t& hint) {
-    if (hint >= 0 && leaf_sqdist(F.tri, hint, p) <= F.eps2) return false;
-    int32_t f = find_facet_within(F.nodes, F.tri, F.nf, p, F.eps2, prune_threshold(p, F.eps2, F.scale));
+template <bool FP32>
+__device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_t& hint,
+                                           TravStats& st) {
+    if (hint >= 0) {
+        ++st.facets;
+        bool skip = FP32 && facet_certainly_out(F.T.cull, hint, p, F.eps2hi);
+        if (!skip) {
+            ++st.fp64;
+            if (leaf_sqdist(F.T.tri, hint, p) <= F.eps2) return false;
+        }
+    }
+    int32_t f = query_point<FP32>(F.T, p, F.eps2, F.eps2hi, st);
     if (f == kTraversalError) {
-        atomicOr(F.err, 1ULL);
+        atomicOr(F.counters + kCntError, 1ULL);
         return false;
     }
     if (f < 0) return true;
@@ -281,11 +584,14 @@ __device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_
     return false;
 }
 
+template <bool FP32>
 __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tris, int64_t n,
                                                    FaceCtx F, double sd, uint8_t* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    TravStats st;
+    uint32_t nq = 0;
     for (int64_t f = warp; f < n; f += nwarps) {
         double t[9];
 #pragma unroll
@@ -298,7 +604,7 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
         sample_header(t, sd, h);
         if (header_too_large(h)) {
             if (lane == 0) {
-                atomicOr(F.err, 2ULL);
+                atomicOr(F.counters + kCntError, 2ULL);
                 out[f] = 1;
             }
             continue;
@@ -306,7 +612,10 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
         int32_t hint = -1;
         bool out_found = false;
         if (h.trivial) {
-            if (lane < 3) out_found = sample_out(F, h.vs[lane], hint);
+            if (lane < 3) {
+                out_found = sample_out<FP32>(F, h.vs[lane], hint, st);
+                ++nq;
+            }
             out_found = __any_sync(0xffffffffu, out_found);
             if (lane == 0) out[f] = out_found ? 1 : 0;
             continue;
@@ -350,7 +659,7 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
                         int N1 = -1;
                         sample_row(h, sd, row, rv, N1);
                         if (N1 > (int)kMaxSamplesPerRow) {
-                            atomicOr(F.err, 2ULL);
+                            atomicOr(F.counters + kCntError, 2ULL);
                             N1 = -1;
                         }
                         rN1 = N1;
@@ -365,22 +674,34 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
                     else { phase = 5; }
                 }
             }
-            bool o = have ? sample_out(F, p, hint) : false;
+            bool o = false;
+            if (have) {
+                o = sample_out<FP32>(F, p, hint, st);
+                ++nq;
+            }
             if (__any_sync(0xffffffffu, o)) { out_found = true; break; }
             if (__all_sync(0xffffffffu, !have)) break;
         }
         if (lane == 0) out[f] = out_found ? 1 : 0;
     }
+    flush_stats(st, F.counters, nq);
 }
 
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
-                      uint8_t* out, unsigned long long* err, cudaStream_t s) {
+                      uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0) return;
     const int block = 128;
     int64_t warps_needed = n;
     int grid = grid_for(warps_needed * 32, block, 16);
-    FaceCtx F{S.nodes, S.tri, S.nf, S.scale, eps2, err};
-    k_env_faces<<<grid, block, 0, s>>>(tris, n, F, sd, out);
+    FaceCtx F{EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale}, eps2, 0.0f, counters};
+    if (precision == TW_PRECISION_FP32_CERTIFIED) {
+        F.eps2hi = (float)(eps2 * (1.0 + 3.814697265625e-06));
+        if ((double)F.eps2hi < eps2 * (1.0 + 3.814697265625e-06))
+            F.eps2hi = nextafterf(F.eps2hi, INFINITY);
+        k_env_faces<true><<<grid, block, 0, s>>>(tris, n, F, sd, out);
+    } else {
+        k_env_faces<false><<<grid, block, 0, s>>>(tris, n, F, sd, out);
+    }
 }
 
 // One thread generates the full sample list in the reference order with the

@@ -24,14 +24,48 @@ struct alignas(16) BvhNode {
 };
 static_assert(sizeof(BvhNode) == 128, "BvhNode must be one 128-byte line");
 
+// The same tree with binary32 boxes rounded outward (lo down, hi up), for the
+// FP32 culling of the certified precision mode: 64 bytes per node.
+struct alignas(16) BvhNode32 {
+    float lo0[3], hi0[3];
+    float lo1[3], hi1[3];
+    int32_t child[2];
+    int32_t pad[2];
+};
+static_assert(sizeof(BvhNode32) == 64, "BvhNode32 must be 64 bytes");
+
+// Per-facet data for a certified FP32 lower bound of the point-facet
+// distance: vertex a (FP64), unit normal n and the three in-plane outward
+// edge normals ne[e] with offsets c[e] = ne[e] . (v_e - a), all rounded to
+// binary32 from FP64.  ok = 0 for facets whose normal is not accurate to far
+// better than binary32 (degenerate or sliver facets): they are never culled.
+struct alignas(16) FacetCull {
+    double a[3];
+    float n[3];
+    float ne[3][3];
+    float c[3];
+    uint32_t ok;
+    float pad[2];
+};
+static_assert(sizeof(FacetCull) == 96, "FacetCull must be 96 bytes");
+
 struct Surface {
     int32_t nf = 0;
     BvhNode* nodes = nullptr;   // nf-1 internal nodes (none when nf == 1)
+    BvhNode32* nodes32 = nullptr;
+    FacetCull* cull = nullptr;  // per leaf (Morton order)
     double* tri = nullptr;      // 9 * nf, Morton order
     int32_t* facet_id = nullptr;  // input facet index of each leaf
     double scale = 0.0;         // max |coordinate| over the surface
+    double lo[3] = {0, 0, 0};   // box of the facet centroids (Morton grid of the tree;
+    double hi[3] = {0, 0, 0};   // query points are ordered on the same grid)
     size_t bytes = 0;
 };
+
+// Device scratch for ordering query points along the Morton curve before
+// traversal: codes, permutation (double-buffered) and the radix-sort
+// temporaries.  Sized by env_sort_scratch_bytes(n).
+size_t env_sort_scratch_bytes(int64_t n);
 
 // Device memory block owned by a context, grown on demand.
 struct Buffer {
@@ -61,10 +95,25 @@ struct tw_ctx {
     uint8_t* rounded = nullptr;
     int32_t nv = 0;
     size_t mesh_bytes = 0;
+    int precision = TW_PRECISION_FP64;
     tw::Buffer scratch[8];
-    unsigned long long* counters = nullptr;   // device: [0] exact-path count, [1..] spare
+    // device counters, see the kCnt* indices below
+    unsigned long long* counters = nullptr;
     std::string last_error;
 };
+
+namespace tw {
+constexpr int kNumCounters = 16;
+constexpr int kCntExactOrient = 0;    // orientations decided by the exact expansion path
+constexpr int kCntUnrounded = 1;      // tets with an unrounded vertex (per call)
+constexpr int kCntError = 2;          // device error word (bits, see sync_status)
+constexpr int kCntEnvFacetTests = 3;  // facets reached by the traversal
+constexpr int kCntEnvFp64 = 4;        // facets evaluated in FP64
+constexpr int kCntAmipsTets = 5;      // tets evaluated by the AMIPS kernels
+constexpr int kCntAmipsFp64 = 6;      // tets recomputed in FP64 (certified mode)
+constexpr int kCntBad = 7;            // host-visible argument check flag
+constexpr int kCntEnvQueries = 8;     // envelope sample/point queries
+}  // namespace tw
 
 namespace tw {
 
@@ -93,10 +142,15 @@ void free_surface(tw_ctx* c, Surface& S);
 // ---- launchers (tw_envelope.cu) ----
 // err: device word; bit 0 = traversal exceeded its bounds, bit 1 = a face
 // exceeded the per-row sample bound.
+// sort_scratch (env_sort_scratch_bytes(n) bytes) enables Morton-ordered
+// traversal; with nullptr the points are traversed in input order.
+// precision: TW_PRECISION_FP64 or TW_PRECISION_FP32_CERTIFIED; counters is
+// the context's counter array (error word and statistics).
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
-                       unsigned long long* err, cudaStream_t s);
+                       int precision, unsigned long long* counters, void* sort_scratch,
+                       cudaStream_t s);
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
-                      uint8_t* out, unsigned long long* err, cudaStream_t s);
+                      uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
 void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
                             int64_t* count, cudaStream_t s);
 

@@ -76,14 +76,6 @@ __global__ void k_bounds(const double* __restrict__ cen, const double* __restric
     if (threadIdx.x < 7) out[threadIdx.x] = red[threadIdx.x][0];
 }
 
-__device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {
-    v = (v * 0x00010001u) & 0xFF0000FFu;
-    v = (v * 0x00000101u) & 0x0F00F00Fu;
-    v = (v * 0x00000011u) & 0xC30C30C3u;
-    v = (v * 0x00000005u) & 0x49249249u;
-    return v;
-}
-
 __global__ void k_morton(const double* __restrict__ cen, int32_t nf,
                          const double* __restrict__ bounds, uint32_t* __restrict__ codes,
                          int32_t* __restrict__ ids) {
@@ -98,7 +90,7 @@ __global__ void k_morton(const double* __restrict__ cen, int32_t nf,
         s = fmin(fmax(s, 0.0), 1023.0);
         q[k] = (uint32_t)s;
     }
-    codes[f] = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+    codes[f] = (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
     ids[f] = f;
 }
 
@@ -206,8 +198,75 @@ __global__ void k_refit(BvhNode* __restrict__ nodes, double* __restrict__ ibox,
     }
 }
 
+// binary32 copy of the tree with outward-rounded boxes
+__global__ void k_nodes32(const BvhNode* __restrict__ nodes, int32_t ni,
+                          BvhNode32* __restrict__ out) {
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    const BvhNode& N = nodes[i];
+    BvhNode32 M;
+    for (int k = 0; k < 3; ++k) {
+        M.lo0[k] = __double2float_rd(N.lo0[k]);
+        M.hi0[k] = __double2float_ru(N.hi0[k]);
+        M.lo1[k] = __double2float_rd(N.lo1[k]);
+        M.hi1[k] = __double2float_ru(N.hi1[k]);
+    }
+    M.child[0] = N.child[0];
+    M.child[1] = N.child[1];
+    M.pad[0] = M.pad[1] = 0;
+    out[i] = M;
+}
+
+// Culling data of each leaf facet (FacetCull).  The facet is usable for
+// culling only when |ab x ac| > 2^-20 |ab| |ac| (the angle between the edges
+// is not tiny): then the FP64 normal and edge normals are accurate to far
+// better than binary32, which the error bound of the FP32 test assumes.
+__global__ void k_facet_cull(const double* __restrict__ tri, int32_t nf,
+                             FacetCull* __restrict__ out) {
+    int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const double* t = tri + 9 * (int64_t)f;
+    V3 v[3] = {{t[0], t[1], t[2]}, {t[3], t[4], t[5]}, {t[6], t[7], t[8]}};
+    V3 ab{v[1].x - v[0].x, v[1].y - v[0].y, v[1].z - v[0].z};
+    V3 ac{v[2].x - v[0].x, v[2].y - v[0].y, v[2].z - v[0].z};
+    V3 n = cross3(ab, ac);
+    double ln = sqrt(dot3(n, n));
+    double lab = sqrt(dot3(ab, ab)), lac = sqrt(dot3(ac, ac));
+    FacetCull C;
+    C.a[0] = v[0].x;
+    C.a[1] = v[0].y;
+    C.a[2] = v[0].z;
+    C.pad[0] = C.pad[1] = 0.0f;
+    bool ok = ln > 9.5367431640625e-07 * lab * lac && isfinite(ln) && ln > 0.0;
+    V3 un{0.0, 0.0, 0.0};
+    if (ok) un = V3{n.x / ln, n.y / ln, n.z / ln};
+    C.n[0] = (float)un.x;
+    C.n[1] = (float)un.y;
+    C.n[2] = (float)un.z;
+    for (int e = 0; e < 3; ++e) {
+        const V3& p0 = v[e];
+        const V3& p1 = v[(e + 1) % 3];
+        V3 te{p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
+        V3 ne = cross3(te, un);  // outward for a counter-clockwise facet about n
+        double l = sqrt(dot3(ne, ne));
+        if (!(l > 0.0)) ok = false;
+        if (ok) ne = V3{ne.x / l, ne.y / l, ne.z / l};
+        V3 d{p0.x - v[0].x, p0.y - v[0].y, p0.z - v[0].z};
+        double c = ok ? dot3(ne, d) : 0.0;
+        C.ne[e][0] = (float)ne.x;
+        C.ne[e][1] = (float)ne.y;
+        C.ne[e][2] = (float)ne.z;
+        C.c[e] = (float)c;
+    }
+    C.ok = ok ? 1u : 0u;
+    out[f] = C;
+}
+
 void free_surface(tw_ctx* c, Surface& S) {
-    if (S.nodes) dev_free(c, S.nodes, sizeof(BvhNode) * (size_t)(S.nf > 1 ? S.nf - 1 : 1));
+    const size_t ni = (size_t)(S.nf > 1 ? S.nf - 1 : 1);
+    if (S.nodes) dev_free(c, S.nodes, sizeof(BvhNode) * ni);
+    if (S.nodes32) dev_free(c, S.nodes32, sizeof(BvhNode32) * ni);
+    if (S.cull) dev_free(c, S.cull, sizeof(FacetCull) * (size_t)S.nf);
     if (S.tri) dev_free(c, S.tri, sizeof(double) * 9 * (size_t)S.nf);
     if (S.facet_id) dev_free(c, S.facet_id, sizeof(int32_t) * (size_t)S.nf);
     S = Surface{};
@@ -220,7 +279,7 @@ int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int
     const size_t n = (size_t)nf;
     const size_t ni = n > 1 ? n - 1 : 1;
     int st = TW_OK;
-    void *nodes = nullptr, *tri = nullptr, *fid = nullptr;
+    void *nodes = nullptr, *tri = nullptr, *fid = nullptr, *nodes32 = nullptr, *cull = nullptr;
     void *tri_in = nullptr, *cen = nullptr, *codes = nullptr, *codes2 = nullptr, *ids = nullptr,
          *ids2 = nullptr, *leafbox = nullptr, *ibox = nullptr, *ipar = nullptr, *lpar = nullptr,
          *flags = nullptr, *bounds = nullptr, *bad = nullptr, *temp = nullptr;
@@ -232,6 +291,7 @@ int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int
         size_t b;
     } allocs[] = {
         {&nodes, sizeof(BvhNode) * ni}, {&tri, 72 * n},       {&fid, 4 * n},
+        {&nodes32, sizeof(BvhNode32) * ni}, {&cull, sizeof(FacetCull) * n},
         {&tri_in, 72 * n},              {&cen, 24 * n},       {&codes, 4 * n},
         {&codes2, 4 * n},               {&ids, 4 * n},        {&ids2, 4 * n},
         {&leafbox, 48 * n},             {&ibox, 48 * ni},     {&ipar, 4 * ni},
@@ -264,7 +324,9 @@ int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int
                                      (int32_t*)lpar);
             k_refit<<<G, B, 0, s>>>((BvhNode*)nodes, (double*)ibox, (const double*)leafbox,
                                     (const int32_t*)ipar, (const int32_t*)lpar, (int*)flags, nf);
+            k_nodes32<<<G, B, 0, s>>>((const BvhNode*)nodes, nf - 1, (BvhNode32*)nodes32);
         }
+        k_facet_cull<<<G, B, 0, s>>>((const double*)tri, nf, (FacetCull*)cull);
         int hbad = 0;
         double hb[8] = {0};
         cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, s);
@@ -277,11 +339,17 @@ int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int
         } else {
             S.nf = nf;
             S.nodes = (BvhNode*)nodes;
+            S.nodes32 = (BvhNode32*)nodes32;
+            S.cull = (FacetCull*)cull;
             S.tri = (double*)tri;
             S.facet_id = (int32_t*)fid;
             S.scale = hb[6];
-            S.bytes = sizeof(BvhNode) * ni + 76 * n;
-            nodes = tri = fid = nullptr;
+            for (int k = 0; k < 3; ++k) {
+                S.lo[k] = hb[k];
+                S.hi[k] = hb[3 + k];
+            }
+            S.bytes = (sizeof(BvhNode) + sizeof(BvhNode32)) * ni + (76 + sizeof(FacetCull)) * n;
+            nodes = tri = fid = nodes32 = cull = nullptr;
         }
     }
     // release temporaries (and the outputs on failure)
