@@ -111,3 +111,58 @@ def test_certified_faces(ctx, oracle):
     want = oracle.surface(V, F).faces_out(tris, eps * eps, eps, nthreads=8)
     assert np.array_equal(a, want) and np.array_equal(b, want)
     assert st["env_queries"] > len(tris)
+
+
+def _term_scales(T_soa):
+    """Magnitudes of the terms that J and H sum (forward-error scale), per tet."""
+    P = T_soa.T.reshape(-1, 4, 3)
+    a = P[:, 0] - P[:, 3]
+    b = (P[:, 0] - 2 * P[:, 1] + P[:, 3]) / np.sqrt(3)
+    c = (P[:, 0] + P[:, 1] + P[:, 3] - 3 * P[:, 2]) / np.sqrt(6)
+    N = (a * a).sum(1) + (b * b).sum(1) + (c * c).sum(1)
+    D = np.einsum("ij,ij->i", a, np.cross(b, c))
+    g = np.cross(b, c) + np.cross(c, a) / np.sqrt(3) + np.cross(a, b) / np.sqrt(6)
+    gN = 2 * (a + b / np.sqrt(3) + c / np.sqrt(6))
+    r = np.abs(D) ** (-2.0 / 3.0)
+    ng, ngN = np.linalg.norm(g, axis=1), np.linalg.norm(gN, axis=1)
+    sJ = r * (ngN + 2.0 / 3.0 * N / np.abs(D) * ng)
+    sH = 3 * r + 4.0 / 3.0 * r / np.abs(D) * ngN * ng + 10.0 / 9.0 * N * r / D ** 2 * ng ** 2
+    return sJ, sH
+
+
+E_TOL32 = 1e-5  # certified relative energy error of the binary32 mode
+
+
+@pytest.mark.parametrize("sigma", [0.1, 0.35])
+def test_certified_amips_batch(ctx, sigma):
+    T = syn.energy_batch(400_000, seed=31, sigma_rel=sigma)
+    a, b, st = _both_modes(ctx, lambda: ctx.amips(T, tw.TW_ENERGY_QUALITY))
+    assert np.array_equal(a["flip"], b["flip"])
+    sent = a["E"] >= 1e50
+    assert np.array_equal(sent, b["E"] >= 1e50)
+    rel = np.abs(b["E"][~sent] - a["E"][~sent]) / np.abs(a["E"][~sent])
+    assert rel.max() <= E_TOL32, rel.max()
+    sJ, sH = _term_scales(T)
+    ok = ~sent
+    errJ = np.abs(b["J"] - a["J"]).max(0)[ok] / sJ[ok]
+    errH = np.abs(b["H"] - a["H"]).max(0)[ok] / sH[ok]
+    assert errJ.max() <= E_TOL32 and errH.max() <= E_TOL32, (errJ.max(), errH.max())
+    assert st["amips_tets"] == T.shape[1]
+    if sigma == 0.1:
+        assert st["amips_fp64"] < 0.2 * st["amips_tets"]
+    else:
+        assert a["flip"].sum() > 0
+
+
+def test_certified_amips_edge_cases(ctx):
+    t = syn.REGULAR_TET.reshape(12)
+    cases = [t, t.reshape(4, 3)[[1, 0, 2, 3]].reshape(12), np.zeros(12), np.r_[t[:9], t[:3]],
+             np.r_[t[:9], 0.5, 0.2, 0.0], t * 1e-100, t * 1e100, t * 1e-12 + 0.5,
+             t * 1e6, np.r_[t[:11], np.nan], np.r_[t[:11], np.inf]]
+    T = np.ascontiguousarray(np.asarray(cases).T)
+    a, b, _ = _both_modes(ctx, lambda: ctx.amips(T, tw.TW_ENERGY_QUALITY))
+    assert np.array_equal(a["flip"], b["flip"])
+    fa = np.isfinite(a["E"]) & (a["E"] < 1e50)
+    assert np.array_equal(fa, np.isfinite(b["E"]) & (b["E"] < 1e50))
+    assert np.all(np.abs(b["E"][fa] - a["E"][fa]) <= E_TOL32 * a["E"][fa])
+    assert np.array_equal(a["E"][~fa], b["E"][~fa])

@@ -53,6 +53,90 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
     }
 }
 
+// TW_PRECISION_FP32_CERTIFIED: the coordinate differences are formed in FP64
+// and rounded once; orientation and E/J/H are evaluated in binary32 with the
+// certified bounds of tw_device.cuh; a tet whose orientation the binary32
+// filter cannot certify takes the FP64 filter (then the exact path), and a tet
+// whose certified energy error exceeds 1e-5 relative is recomputed entirely
+// in FP64 (amips_egh).  Outputs are FP64 like k_amips_soa.
+constexpr float kAmipsTol32 = 1e-5f;
+
+template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
+__global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict__ T, int64_t n,
+                                                        double* __restrict__ E,
+                                                        double* __restrict__ J,
+                                                        double* __restrict__ H,
+                                                        uint8_t* __restrict__ flip,
+                                                        unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    uint32_t ntet = 0, nfp64 = 0, nexact = 0;
+    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane;
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + lane;
+        if (i >= n) continue;
+        double t[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
+        float d1[3], d2[3], d3[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            d1[k] = __double2float_rn(t[3 + k] - t[k]);
+            d2[k] = __double2float_rn(t[6 + k] - t[k]);
+            d3[k] = __double2float_rn(t[9 + k] - t[k]);
+        }
+        int ori = 1;
+        if (WF || QUAL) {
+            ori = orient32_filter(d1, d2, d3);
+            if (ori == 2) {
+                int ex = 0;
+                ori = orient3d(t, t + 3, t + 6, t + 9, &ex);
+                nexact += ex;
+            }
+        }
+        ++ntet;
+        Amips32 R = amips_egh32<WJ, WH>(d1, d2, d3, kAmipsTol32);
+        double e, jv[3], hv[9];
+        if (R.ok) {
+            e = (double)R.E;
+            if (WJ)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) jv[c] = (double)R.J[c];
+            if (WH)
+#pragma unroll
+                for (int c = 0; c < 9; ++c) hv[c] = (double)R.H[c];
+        } else {
+            ++nfp64;
+            if (WJ || WH)
+                e = amips_egh(t, WJ ? jv : nullptr, WH ? hv : nullptr);
+            else
+                e = amips_energy(t);
+        }
+        if (WE) E[i] = QUAL ? quality_from(ori, e) : e;
+        if (WF) flip[i] = (uint8_t)(ori != 1);
+        if (WJ) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+        }
+        if (WH) {
+#pragma unroll
+            for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+        }
+    }
+    unsigned long long a = ntet, f = nfp64, x = nexact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        f += __shfl_xor_sync(0xffffffffu, f, o);
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+    }
+    if (lane == 0) {
+        if (a) atomicAdd(counters + kCntAmipsTets, a);
+        if (f) atomicAdd(counters + kCntAmipsFp64, f);
+        if (x) atomicAdd(counters + kCntExactOrient, x);
+    }
+}
+
 int grid_for(int64_t n, int block, int blocks_per_sm) {
     static int sms = 0;
     if (sms == 0) {
@@ -91,6 +175,29 @@ void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J
     const int block = 256;
     int grid = grid_for(n, block, 8);
     k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, exact_count);
+}
+
+template <int BITS>
+static AmipsKernel pick_amips_cert() {
+    return k_amips_soa_cert<(BITS & 1) != 0, (BITS & 2) != 0, (BITS & 4) != 0, (BITS & 8) != 0,
+                            (BITS & 16) != 0>;
+}
+
+template <int... B>
+static AmipsKernel amips_cert_table(int bits, std::integer_sequence<int, B...>) {
+    static const AmipsKernel table[] = {pick_amips_cert<B>()...};
+    return table[bits];
+}
+
+void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
+                           uint8_t* flip, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0) return;
+    int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
+               ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
+    AmipsKernel k = amips_cert_table(bits, std::make_integer_sequence<int, 32>{});
+    const int block = 256;
+    int grid = grid_for(n, block, 8);
+    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, counters);
 }
 
 __global__ void __launch_bounds__(256) k_tet_quality_idx(

@@ -306,7 +306,10 @@ int tw_amips_soa_device(tw_ctx* c, const double* T, int64_t n, int mode, double*
     if (mode != TW_ENERGY_RAW && mode != TW_ENERGY_QUALITY)
         return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
     Guard g(c->device);
-    launch_amips_soa(T, n, mode, E, J, H, flip, c->counters, c->stream);
+    if (c->precision == TW_PRECISION_FP32_CERTIFIED)
+        launch_amips_soa_cert(T, n, mode, E, J, H, flip, c->counters, c->stream);
+    else
+        launch_amips_soa(T, n, mode, E, J, H, flip, c->counters + kCntExactOrient, c->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_amips_soa_device");
     return TW_OK;
@@ -343,7 +346,11 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
         for (int comp = 0; comp < 12; ++comp)
             cudaMemcpyAsync(dT[k] + comp * len, T + comp * n + i0, 8 * (size_t)len,
                             cudaMemcpyHostToDevice, s);
-        launch_amips_soa(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s);
+        if (c->precision == TW_PRECISION_FP32_CERTIFIED)
+            launch_amips_soa_cert(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s);
+        else
+            launch_amips_soa(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k],
+                             c->counters + kCntExactOrient, s);
         if (E) cudaMemcpyAsync(E + i0, dE[k], 8 * (size_t)len, cudaMemcpyDeviceToHost, s);
         if (J)
             for (int comp = 0; comp < 3; ++comp)

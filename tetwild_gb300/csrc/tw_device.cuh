@@ -311,6 +311,131 @@ __device__ __forceinline__ int orient3d(const double* p, const double* q, const 
     return orient3d_exact(p, q, r, s);
 }
 
+// ---------------------------------------------------------------------------
+// Certified binary32 AMIPS (TW_PRECISION_FP32_CERTIFIED).
+// ---------------------------------------------------------------------------
+constexpr float kU32 = 5.9604644775390625e-08f;  // 2^-24
+
+// x^(-1/3) for a normal positive binary32 x: exponent reduction to [1,8) and
+// four Newton-Raphson steps from a linear seed; relative error below 4 u.
+__device__ __forceinline__ float icbrt32(float x) {
+    unsigned u = __float_as_uint(x);
+    int e = (int)((u >> 23) & 0xffu) - 127;
+    int q = (e >= 0) ? e / 3 : -((-e + 2) / 3);
+    int rem = e - 3 * q;
+    float m = __uint_as_float((u & 0x7fffffu) | ((unsigned)(127 + rem) << 23));
+    float y = fmaf(-0.06015f, m, 0.9318f);
+    const float third = 0.333333343f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float y3 = (y * y) * y;
+        y = fmaf(y * fmaf(-m, y3, 1.0f), third, y);
+    }
+    return y * __uint_as_float((unsigned)(127 - q) << 23);
+}
+
+// Result of the binary32 evaluation: ok = false when the certified relative
+// error bound of E exceeds tol (or a magnitude leaves the safe binary32 range);
+// the caller then recomputes the tet in FP64.
+struct Amips32 {
+    bool ok;
+    float E;
+    float J[3];
+    float H[9];
+};
+
+// d1 = p1 - p0, d2 = p2 - p0, d3 = p3 - p0, each rounded once from FP64.
+// Frame (same map as amips_frame): a = -d3, b = (d3 - 2 d1)/sqrt3,
+// c = (d1 + d3 - 3 d2)/sqrt6.  Error bound (u = 2^-24, first order):
+// the components of a, b, c carry errors <= u A_k, 4u B_k, 5u C_k with
+// A = |d3|, B = (|d3| + 2|d1|)/sqrt3, C = (|d1| + |d3| + 3|d2|)/sqrt6 (input
+// rounding, fma, constant and product roundings), so with perm(A,B,C) the
+// permanent of the rows A, B, C:  |dD| <= 16u perm(A,B,C) (10u from the
+// inputs, 5u from the triple product), |dN| <= 10u sum(A^2+B^2+C^2) + 4u N,
+// and rel(E) <= rel(N) + 2/3 rel(D) + 6u (icbrt <= 4u, D^2 and N r).
+template <bool WJ, bool WH>
+__device__ __forceinline__ Amips32 amips_egh32(const float* d1, const float* d2, const float* d3,
+                                               float tol) {
+    const float isq3 = 0.577350269f, isq6 = 0.408248290f;
+    float a[3], b[3], c[3], A[3], B[3], C[3], NB = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = -d3[k];
+        b[k] = fmaf(-2.0f, d1[k], d3[k]) * isq3;
+        c[k] = fmaf(-3.0f, d2[k], d1[k] + d3[k]) * isq6;
+        A[k] = fabsf(d3[k]);
+        B[k] = fmaf(2.0f, fabsf(d1[k]), fabsf(d3[k])) * isq3;
+        C[k] = fmaf(3.0f, fabsf(d2[k]), fabsf(d1[k]) + fabsf(d3[k])) * isq6;
+        NB = fmaf(A[k], A[k], fmaf(B[k], B[k], fmaf(C[k], C[k], NB)));
+    }
+    float PD = A[0] * fmaf(B[1], C[2], B[2] * C[1]) + A[1] * fmaf(B[2], C[0], B[0] * C[2]) +
+               A[2] * fmaf(B[0], C[1], B[1] * C[0]);
+    float N = fmaf(a[2], a[2], fmaf(a[1], a[1], a[0] * a[0])) +
+              fmaf(b[2], b[2], fmaf(b[1], b[1], b[0] * b[0])) +
+              fmaf(c[2], c[2], fmaf(c[1], c[1], c[0] * c[0]));
+    float bc[3] = {fmaf(b[1], c[2], -b[2] * c[1]), fmaf(b[2], c[0], -b[0] * c[2]),
+                   fmaf(b[0], c[1], -b[1] * c[0])};
+    float D = fmaf(a[2], bc[2], fmaf(a[1], bc[1], a[0] * bc[0]));
+    float aD = fabsf(D);
+    Amips32 R;
+    float bound = 1.01f * (14.0f * kU32 * NB / N + 10.6667f * kU32 * PD / aD + 6.0f * kU32);
+    R.ok = (aD > 1e-18f) && (aD < 1e18f) && (N > 1e-30f) && (N < 1e30f) && (bound <= tol);
+    if (!R.ok) return R;
+    float r = icbrt32(D * D);
+    R.E = N * r;
+    if (WJ || WH) {
+        float ca[3] = {fmaf(c[1], a[2], -c[2] * a[1]), fmaf(c[2], a[0], -c[0] * a[2]),
+                       fmaf(c[0], a[1], -c[1] * a[0])};
+        float ab[3] = {fmaf(a[1], b[2], -a[2] * b[1]), fmaf(a[2], b[0], -a[0] * b[2]),
+                       fmaf(a[0], b[1], -a[1] * b[0])};
+        float g[3], gN[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g[k] = fmaf(isq6, ab[k], fmaf(isq3, ca[k], bc[k]));
+            gN[k] = 2.0f * fmaf(isq6, c[k], fmaf(isq3, b[k], a[k]));
+        }
+        float invD = 1.0f / D;
+        if (WJ) {
+            float t = (0.666666687f * N) * invD;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) R.J[k] = r * fmaf(-t, g[k], gN[k]);
+        }
+        if (WH) {
+            float s1 = (0.666666687f * r) * invD;
+            float s2 = ((1.11111116f * N * r) * invD) * invD;
+            float r3 = 3.0f * r;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = i; j < 3; ++j) {
+                    float base = (i == j) ? r3 : 0.0f;
+                    float h = fmaf(s2, g[i] * g[j], fmaf(-s1, fmaf(gN[i], g[j], g[i] * gN[j]), base));
+                    R.H[i * 3 + j] = h;
+                    R.H[j * 3 + i] = h;
+                }
+        }
+    }
+    return R;
+}
+
+// Orientation sign of det[d1, d2, d3] when binary32 can certify it, else 2.
+// The bound adds the rounding of the FP64 differences (3.01 u per term of the
+// permanent) to the stage-A bound (7 + 56 u) u of the binary32 evaluation.
+__device__ __forceinline__ int orient32_filter(const float* d1, const float* d2, const float* d3) {
+    float vywz = d2[1] * d3[2], vzwy = d2[2] * d3[1];
+    float vzwx = d2[2] * d3[0], vxwz = d2[0] * d3[2];
+    float vxwy = d2[0] * d3[1], vywx = d2[1] * d3[0];
+    float det = (d1[0] * (vywz - vzwy) + d1[1] * (vzwx - vxwz)) + d1[2] * (vxwy - vywx);
+    float perm = (fabsf(d1[0]) * (fabsf(vywz) + fabsf(vzwy)) +
+                  fabsf(d1[1]) * (fabsf(vzwx) + fabsf(vxwz))) +
+                 fabsf(d1[2]) * (fabsf(vxwy) + fabsf(vywx));
+    if (!(perm > 1e-30f) || !(perm < 1e30f)) return 2;
+    float bound = 11.0f * kU32 * perm;
+    if (det > bound) return 1;
+    if (-det > bound) return -1;
+    return 2;
+}
+
 // calTetQuality_AMIPS (LocalOperations.cpp:862-884) sentinel rule.
 __device__ __forceinline__ double quality_from(int ori, double e) {
     if (ori != 1) return kMaxEnergy;

@@ -130,6 +130,9 @@ int grid_for(int64_t n, int block, int blocks_per_sm);
 // ---- launchers (tw_amips.cu) ----
 void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
                       uint8_t* flip, unsigned long long* exact_count, cudaStream_t s);
+// certified binary32 variant; counters is the context's counter array
+void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
+                           uint8_t* flip, unsigned long long* counters, cudaStream_t s);
 void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                             const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
                             uint8_t* needs_host, unsigned long long* counters, cudaStream_t s);
