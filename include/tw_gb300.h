@@ -191,6 +191,14 @@ TW_API int tw_newton_stars(tw_ctx* ctx, const int32_t* star_off, const int32_t* 
 TW_API int tw_host_alloc(size_t bytes, void** out);
 TW_API int tw_host_free(void* p);
 
+/* ---- device self-test -----------------------------------------------------------
+ * No counterpart in the reference.  Checks, on `samples` pseudo-random bit
+ * patterns, the integer-arithmetic binary64 <-> binary32 conversions that the
+ * certified mode relies on against the hardware conversions; failures[0]
+ * counts round-to-nearest double->float mismatches, failures[1] exact
+ * float->double mismatches.  Both must be 0.                               */
+TW_API int tw_self_test(tw_ctx* ctx, uint64_t samples, uint64_t* failures);
+
 /* ---- measured pipe peaks (roofline denominators) ------------------------------
  * Times a dependent-FMA loop over the whole GPU and returns FP64 and FP32
  * FMA throughput in TFLOP/s (2 flops per FMA).                              */

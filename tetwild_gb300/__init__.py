@@ -96,6 +96,7 @@ _SIGS = {
     "tw_host_alloc": [_SZ, ctypes.POINTER(_P)],
     "tw_host_free": [_P],
     "tw_probe_peaks": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D)],
+    "tw_self_test": [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
 }
 EXPORTED_SYMBOLS = tuple(_SIGS)
 
@@ -299,6 +300,12 @@ class Context:
         return out, moved
 
     # -- misc ---------------------------------------------------------------------------
+    def self_test(self, samples: int = 1 << 26):
+        """(d2f_rn mismatches, f2d_exact mismatches) against the hardware conversions."""
+        f = (ctypes.c_uint64 * 2)()
+        self._check(self.lib.tw_self_test(self.h, samples, f))
+        return int(f[0]), int(f[1])
+
     def probe_peaks(self):
         a, b = _D(), _D()
         self._check(self.lib.tw_probe_peaks(self.h, ctypes.byref(a), ctypes.byref(b)))

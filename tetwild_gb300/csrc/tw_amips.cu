@@ -81,9 +81,9 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
         float d1[3], d2[3], d3[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            d1[k] = __double2float_rn(t[3 + k] - t[k]);
-            d2[k] = __double2float_rn(t[6 + k] - t[k]);
-            d3[k] = __double2float_rn(t[9 + k] - t[k]);
+            d1[k] = d2f_rn(t[3 + k] - t[k]);
+            d2[k] = d2f_rn(t[6 + k] - t[k]);
+            d3[k] = d2f_rn(t[9 + k] - t[k]);
         }
         int ori = 1;
         if (WF || QUAL) {
@@ -98,13 +98,13 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
         Amips32 R = amips_egh32<WJ, WH>(d1, d2, d3, kAmipsTol32);
         double e, jv[3], hv[9];
         if (R.ok) {
-            e = (double)R.E;
+            e = f2d_exact(R.E);
             if (WJ)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) jv[c] = (double)R.J[c];
+                for (int c = 0; c < 3; ++c) jv[c] = f2d_exact(R.J[c]);
             if (WH)
 #pragma unroll
-                for (int c = 0; c < 9; ++c) hv[c] = (double)R.H[c];
+                for (int c = 0; c < 9; ++c) hv[c] = f2d_exact(R.H[c]);
         } else {
             ++nfp64;
             if (WJ || WH)
@@ -112,7 +112,14 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
             else
                 e = amips_energy(t);
         }
-        if (WE) E[i] = QUAL ? quality_from(ori, e) : e;
+        if (WE) {
+            // a certified binary32 energy is finite and positive: only the
+            // orientation part of the sentinel rule can apply
+            if (R.ok)
+                E[i] = (QUAL && ori != 1) ? kMaxEnergy : e;
+            else
+                E[i] = QUAL ? quality_from(ori, e) : e;
+        }
         if (WF) flip[i] = (uint8_t)(ori != 1);
         if (WJ) {
 #pragma unroll

@@ -91,6 +91,50 @@ void launch_fp32_probe(float* out, int iters, int blocks, cudaStream_t s) {
     k_fp32_probe<<<blocks, 256, 0, s>>>(out, iters);
 }
 
+// Self-test of the integer-arithmetic conversions against the hardware
+// conversions on pseudo-random bit patterns (all classes: normal, subnormal,
+// zero, inf, NaN, out of binary32 range) and on doubles near binary32
+// rounding ties.  fail[0]: d2f_rn, fail[1]: f2d_exact.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+__global__ void k_selftest_conv(unsigned long long n, unsigned long long* fail) {
+    unsigned long long f0 = 0, f1 = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        unsigned long long r = mix64(i);
+        double x;
+        switch (i & 3ULL) {
+        case 0:  // any pattern
+            x = __longlong_as_double((long long)r);
+            break;
+        case 1: {  // exponent within binary32 range
+            unsigned long long e = 1023ULL - 130ULL + ((r >> 52) % 262ULL);
+            x = __longlong_as_double((long long)((r & 0x800fffffffffffffULL) | (e << 52)));
+            break;
+        }
+        default: {  // near ties: low 29 mantissa bits around the half-way point
+            unsigned long long e = 1023ULL - 60ULL + ((r >> 52) % 120ULL);
+            unsigned long long m = (r & 0x000fffffe0000000ULL) | (0x10000000ULL + ((r >> 7) & 3ULL) - 1ULL);
+            x = __longlong_as_double((long long)((r & 0x8000000000000000ULL) | (e << 52) | m));
+            break;
+        }
+        }
+        float a = d2f_rn(x), b = __double2float_rn(x);
+        bool same = (a != a && b != b) || (__float_as_uint(a) == __float_as_uint(b));
+        f0 += same ? 0 : 1;
+        float g = __uint_as_float((unsigned)(r >> 17));
+        double c = f2d_exact(g), d = (double)g;
+        bool same2 = (c != c && d != d) || (__double_as_longlong(c) == __double_as_longlong(d));
+        f1 += same2 ? 0 : 1;
+    }
+    if (f0) atomicAdd(fail, f0);
+    if (f1) atomicAdd(fail + 1, f1);
+}
+
 __global__ void k_aos_to_soa(const double* __restrict__ xyz, int32_t n, double* __restrict__ x,
                              double* __restrict__ y, double* __restrict__ z) {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -665,6 +709,19 @@ int tw_host_alloc(size_t bytes, void** out) {
 int tw_host_free(void* p) {
     if (!p) return TW_OK;
     return cudaFreeHost(p) == cudaSuccess ? TW_OK : TW_ERR_CUDA;
+}
+
+int tw_self_test(tw_ctx* c, uint64_t samples, uint64_t* failures) {
+    if (!c || !failures) return TW_ERR_ARG;
+    Guard g(c->device);
+    void* p;
+    int st = ensure(c, 6, 64, &p);
+    if (st != TW_OK) return st;
+    cudaMemsetAsync(p, 0, 16, c->stream);
+    k_selftest_conv<<<1024, 256, 0, c->stream>>>((unsigned long long)samples,
+                                                 (unsigned long long*)p);
+    cudaMemcpyAsync(failures, p, 16, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_self_test");
 }
 
 int tw_probe_peaks(tw_ctx* c, double* fp64_tflops, double* fp32_tflops) {

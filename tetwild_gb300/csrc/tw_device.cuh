@@ -312,6 +312,36 @@ __device__ __forceinline__ int orient3d(const double* p, const double* q, const 
 }
 
 // ---------------------------------------------------------------------------
+// binary32 <-> binary64 conversions in integer arithmetic.  On this GPU the
+// hardware conversions issue to the (slow) FP64 pipe; these use the integer
+// ALU for normal numbers and take the hardware path only for zeros,
+// subnormals, infinities, NaNs and out-of-range exponents.
+// ---------------------------------------------------------------------------
+// Exact: every binary32 value is a binary64 value.
+__device__ __forceinline__ double f2d_exact(float f) {
+    uint32_t b = __float_as_uint(f);
+    uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    uint32_t hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3);
+    uint32_t lo = b << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+// Round to nearest, ties to even (the IEEE default), like __double2float_rn.
+__device__ __forceinline__ float d2f_rn(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(x);
+    uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
+    uint32_t rest = lo & 0x1fffffffu;                  // the 29 dropped bits
+    uint32_t r = ((uint32_t)e << 23) | m;
+    // a carry out of the mantissa increments the exponent (and rounds to inf
+    // at the top of the range), as round-to-nearest requires
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float((hi & 0x80000000u) | r);
+}
+
+// ---------------------------------------------------------------------------
 // Certified binary32 AMIPS (TW_PRECISION_FP32_CERTIFIED).
 // ---------------------------------------------------------------------------
 constexpr float kU32 = 5.9604644775390625e-08f;  // 2^-24

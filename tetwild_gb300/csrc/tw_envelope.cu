@@ -44,155 +44,7 @@ __device__ __forceinline__ double leaf_sqdist(const double* __restrict__ tri, in
 
 constexpr int32_t kTraversalError = -2;
 
-// ---------------------------------------------------------------------------
-// Certified binary32 culling (TW_PRECISION_FP32_CERTIFIED).
-//
-// Boxes: binary32 copies rounded outward; the point is rounded to binary32
-// (error <= 2^-24 M per coordinate, M = max |coordinate|); a child is
-// skipped only when its computed squared distance exceeds
-// (eps (1 + 2^-20) + tau32)^2, tau32 = 2^-21 M + 2^-20 eps, which covers the
-// point rounding (sqrt3 2^-24 M) and the rounding of the distance (3 u eps).
-//
-// Facets: d(p, f)^2 >= h^2 + max(0, max_e s_e)^2, with h the distance of p to
-// the facet's plane and s_e the signed distance of p to the in-plane
-// half-plane of edge e (the facet lies in the plane and inside every edge's
-// half-plane, and the plane and a half-plane boundary are orthogonal).  h and
-// s_e are evaluated in binary32 from r = p - a (rounded from FP64) with the
-// stored unit normals; their error is below 8 u |r|_1 (+ 8 u |c_e|), u = 2^-24
-// (rounding of r: u|r|_1, of the normal: u|r|_1, of the 3-term dot: 3.01 u|r|_1,
-// of the offset and the subtraction: 2u(|r|_1 + |c_e|)).  The facet is
-// skipped only when the lower bound computed from (|h| - delta)+ and
-// (s_e - delta_e)+ exceeds eps^2 (1 + 2^-18), rounded up: then the exact
-// distance exceeds eps by far more than the error of the FP64 evaluation, so
-// the FP64 test would also have found d^2 > eps^2.  Every other facet is
-// evaluated in FP64 exactly as in TW_PRECISION_FP64.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float round_up_f(double x) { return __double2float_ru(x); }
-
-__device__ __forceinline__ float box_thr32(const V3& p, double eps2, double scale) {
-    double m = scale;
-    m = fmax(m, fabs(p.x));
-    m = fmax(m, fabs(p.y));
-    m = fmax(m, fabs(p.z));
-    double eps = sqrt(eps2);
-    double tau = 4.76837158203125e-07 * m + 9.5367431640625e-07 * eps;
-    double e = eps * (1.0 + 9.5367431640625e-07) + tau;
-    return round_up_f(e * e);
-}
-
-__device__ __forceinline__ float point_box_sqdist32(float px, float py, float pz, const float* lo,
-                                                    const float* hi) {
-    float r = 0.0f;
-    if (px < lo[0]) { float d = lo[0] - px; r = d * d; }
-    else if (px > hi[0]) { float d = px - hi[0]; r = d * d; }
-    if (py < lo[1]) { float d = lo[1] - py; r = r + d * d; }
-    else if (py > hi[1]) { float d = py - hi[1]; r = r + d * d; }
-    if (pz < lo[2]) { float d = lo[2] - pz; r = r + d * d; }
-    else if (pz > hi[2]) { float d = pz - hi[2]; r = r + d * d; }
-    return r;
-}
-
-// True when facet f is certainly farther than eps from p (see above).
-__device__ __forceinline__ bool facet_certainly_out(const FacetCull* __restrict__ cull, int32_t f,
-                                                    const V3& p, float eps2hi) {
-    const float4* q = reinterpret_cast<const float4*>(cull + f);
-    const double2* qd = reinterpret_cast<const double2*>(cull + f);
-    double2 a01 = __ldg(qd);
-    float4 w1 = __ldg(q + 1);  // a.z (as two floats), n.x, n.y
-    float4 w2 = __ldg(q + 2);  // n.z, ne0.xyz
-    float4 w3 = __ldg(q + 3);  // ne1.xyz, ne2.x
-    float4 w4 = __ldg(q + 4);  // ne2.yz, c0, c1
-    float4 w5 = __ldg(q + 5);  // c2, ok, pad
-    if (__float_as_uint(w5.y) == 0u) return false;
-    double az = __ldg(reinterpret_cast<const double*>(cull + f) + 2);
-    float rx = __double2float_rn(p.x - a01.x);
-    float ry = __double2float_rn(p.y - a01.y);
-    float rz = __double2float_rn(p.z - az);
-    float R1 = fabsf(rx) + fabsf(ry) + fabsf(rz);
-    const float k8u = 4.76837158203125e-07f;  // 8 * 2^-24
-    float h = fmaf(w2.x, rz, fmaf(w1.w, ry, w1.z * rx));
-    float hl = fmaxf(fabsf(h) - k8u * R1, 0.0f);
-    float s0 = fmaf(w2.w, rz, fmaf(w2.z, ry, w2.y * rx)) - w4.z;
-    float s1 = fmaf(w3.z, rz, fmaf(w3.y, ry, w3.x * rx)) - w4.w;
-    float s2 = fmaf(w4.y, rz, fmaf(w4.x, ry, w3.w * rx)) - w5.x;
-    s0 -= k8u * (R1 + fabsf(w4.z));
-    s1 -= k8u * (R1 + fabsf(w4.w));
-    s2 -= k8u * (R1 + fabsf(w5.x));
-    float sl = fmaxf(fmaxf(s0, s1), fmaxf(s2, 0.0f));
-    float L2 = fmaf(sl, sl, hl * hl);
-    return L2 > eps2hi;
-}
-
-struct TravStats {
-    uint32_t facets = 0;  // facets reached
-    uint32_t fp64 = 0;    // facets evaluated in FP64
-};
-
-// FP32-culled traversal; decisions identical to find_facet_within (FP64).
-__device__ __forceinline__ int32_t find_facet_within32(const BvhNode32* __restrict__ nodes,
-                                                       const FacetCull* __restrict__ cull,
-                                                       const double* __restrict__ tri, int32_t nf,
-                                                       const V3& p, double eps2, float thr32,
-                                                       float eps2hi, TravStats& st) {
-    if (nf == 1) {
-        ++st.facets;
-        if (facet_certainly_out(cull, 0, p, eps2hi)) return -1;
-        ++st.fp64;
-        return leaf_sqdist(tri, 0, p) <= eps2 ? 0 : -1;
-    }
-    const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
-                pz = __double2float_rn(p.z);
-    int32_t stack[kStack];
-    int sp = 0;
-    int32_t cur = 0;
-    for (int32_t iter = 0; iter < nf; ++iter) {
-        if ((uint32_t)cur >= (uint32_t)(nf - 1)) return kTraversalError;
-        const float4* nd = reinterpret_cast<const float4*>(nodes + cur);
-        float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
-        int4 q3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
-        float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
-        float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
-        int2 ch = make_int2(q3.x, q3.y);
-        float d0 = point_box_sqdist32(px, py, pz, lo0, hi0);
-        float d1 = point_box_sqdist32(px, py, pz, lo1, hi1);
-        bool h0 = d0 <= thr32, h1 = d1 <= thr32;
-        if (h0 && ch.x < 0) {
-            int32_t lf = ~ch.x;
-            if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
-            ++st.facets;
-            if (!facet_certainly_out(cull, lf, p, eps2hi)) {
-                ++st.fp64;
-                if (leaf_sqdist(tri, lf, p) <= eps2) return lf;
-            }
-            h0 = false;
-        }
-        if (h1 && ch.y < 0) {
-            int32_t lf = ~ch.y;
-            if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
-            ++st.facets;
-            if (!facet_certainly_out(cull, lf, p, eps2hi)) {
-                ++st.fp64;
-                if (leaf_sqdist(tri, lf, p) <= eps2) return lf;
-            }
-            h1 = false;
-        }
-        if (h0 && h1) {
-            if (sp >= kStack) return kTraversalError;
-            int32_t nearc = (d0 <= d1) ? ch.x : ch.y;
-            int32_t farc = (d0 <= d1) ? ch.y : ch.x;
-            stack[sp++] = farc;
-            cur = nearc;
-        } else if (h0) {
-            cur = ch.x;
-        } else if (h1) {
-            cur = ch.y;
-        } else {
-            if (sp == 0) return -1;
-            cur = stack[--sp];
-        }
-    }
-    return kTraversalError;
-}
+#include "tw_envcert.cuh"
 
 // One atomic per warp for the traversal statistics.
 __device__ __forceinline__ void flush_stats(const TravStats& st, unsigned long long* counters,
@@ -280,29 +132,44 @@ struct EnvTree {
     const double* tri;
     int32_t nf;
     double scale;
+    float scale_hi;  // scale rounded up to binary32
 };
 
 template <bool FP32>
-__device__ __forceinline__ int32_t query_point(const EnvTree& T, const V3& p, double eps2,
-                                               float eps2hi, TravStats& st) {
+__device__ __forceinline__ int32_t query_point(const EnvTree& T, const V3& p, const EpsParams& E,
+                                               TravStats& st) {
     if (FP32)
-        return find_facet_within32(T.nodes32, T.cull, T.tri, T.nf, p, eps2,
-                                   box_thr32(p, eps2, T.scale), eps2hi, st);
-    return find_facet_within(T.nodes, T.tri, T.nf, p, eps2, prune_threshold(p, eps2, T.scale), st);
+        return find_facet_within32(T.nodes32, T.cull, T.tri, T.nf, p, cert_query(p, E, T.scale_hi),
+                                   E.eps2, st);
+    return find_facet_within(T.nodes, T.tri, T.nf, p, E.eps2, prune_threshold(p, E.eps2, T.scale),
+                             st);
 }
 
-__device__ __forceinline__ float eps2_hi(double eps2) {
-    return round_up_f(eps2 * (1.0 + 3.814697265625e-06));  // eps^2 (1 + 2^-18)
+// eps = sqrt(eps2) rounded up and down to binary32, and the scale rounded up.
+static EpsParams eps_params(double eps2) {
+    EpsParams E;
+    E.eps2 = eps2;
+    double eps = std::sqrt(eps2);
+    float f = (float)eps;
+    E.eps_hi = ((double)f < eps) ? std::nextafter(f, INFINITY) : f;
+    E.eps_lo = ((double)f > eps) ? std::nextafter(f, 0.0f) : f;
+    return E;
+}
+static float round_up_float(double x) {
+    float f = (float)x;
+    return ((double)f < x) ? std::nextafter(f, INFINITY) : f;
+}
+static EnvTree env_tree(const Surface& S) {
+    return EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale)};
 }
 
 template <bool FP32>
 __global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P,
                                                     const int32_t* __restrict__ order, int64_t n,
-                                                    EnvTree T, double eps2,
+                                                    EnvTree T, EpsParams E,
                                                     uint8_t* __restrict__ out,
                                                     unsigned long long* __restrict__ counters) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const float e2hi = eps2_hi(eps2);
     TravStats st;
     uint32_t nq = 0;
     // every lane runs the same number of iterations so the final warp
@@ -314,7 +181,7 @@ __global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P
         if (i < n) {
             const int64_t j = order ? (int64_t)__ldg(order + i) : i;
             V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
-            int32_t f = query_point<FP32>(T, p, eps2, e2hi, st);
+            int32_t f = query_point<FP32>(T, p, E, st);
             if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
             out[j] = (uint8_t)(f == -1);
             ++nq;
@@ -325,18 +192,20 @@ __global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P
 
 // 30-bit Morton code of each query point on the tree's centroid grid
 // (points outside the grid clamp to its faces).
-__global__ void k_point_codes(const double* __restrict__ P, int64_t n, double lx, double ly,
-                              double lz, double sx, double sy, double sz,
+// The order only changes how much work the traversal does, never its
+// results, so it is computed in binary32 (integer-rounded inputs).
+__global__ void k_point_codes(const double* __restrict__ P, int64_t n, float lx, float ly,
+                              float lz, float sx, float sy, float sz,
                               uint32_t* __restrict__ codes, int32_t* __restrict__ idx) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double c[3] = {(__ldg(P + 3 * i) - lx) * sx, (__ldg(P + 3 * i + 1) - ly) * sy,
-                   (__ldg(P + 3 * i + 2) - lz) * sz};
+    float c[3] = {(d2f_rn(__ldg(P + 3 * i)) - lx) * sx, (d2f_rn(__ldg(P + 3 * i + 1)) - ly) * sy,
+                  (d2f_rn(__ldg(P + 3 * i + 2)) - lz) * sz};
     uint32_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double v = c[k] * 1024.0;
-        v = fmin(fmax(v, 0.0), 1023.0);  // NaN -> 0
+        float v = c[k] * 1024.0f;
+        v = fminf(fmaxf(v, 0.0f), 1023.0f);  // NaN -> 0
         q[k] = (uint32_t)v;
     }
     codes[i] = (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
@@ -395,18 +264,20 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
             sc[k] = ext > 0.0 ? 1.0 / ext : 0.0;
         }
         k_point_codes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-            P, n, S.lo[0], S.lo[1], S.lo[2], sc[0], sc[1], sc[2], L.codes, L.idx);
+            P, n, (float)S.lo[0], (float)S.lo[1], (float)S.lo[2], (float)sc[0], (float)sc[1],
+            (float)sc[2], L.codes, L.idx);
         size_t tb = L.temp_bytes;
         cub::DeviceRadixSort::SortPairs(L.temp, tb, L.codes, L.codes2, L.idx, L.idx2, (int)n, 0, 30,
                                         s);
         order = L.idx2;
     }
-    EnvTree T{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale};
+    const EnvTree T = env_tree(S);
+    const EpsParams E = eps_params(eps2);
     if (precision == TW_PRECISION_FP32_CERTIFIED)
-        k_env_points<true><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, eps2, out,
+        k_env_points<true><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                     counters);
     else
-        k_env_points<false><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, eps2, out,
+        k_env_points<false><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                      counters);
 }
 
@@ -543,8 +414,7 @@ __device__ __noinline__ bool tri_collinear(const double* t) {
 
 struct FaceCtx {
     EnvTree T;
-    double eps2;
-    float eps2hi;
+    EpsParams E;
     unsigned long long* counters;
 };
 
@@ -568,13 +438,19 @@ __device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_
                                            TravStats& st) {
     if (hint >= 0) {
         ++st.facets;
-        bool skip = FP32 && facet_certainly_out(F.T.cull, hint, p, F.eps2hi);
-        if (!skip) {
+        if (FP32) {
+            int cls = facet_classify(F.T.cull, hint, cert_query(p, F.E, F.T.scale_hi));
+            if (cls == kFacetIn) return false;
+            if (cls == kFacetBand) {
+                ++st.fp64;
+                if (leaf_sqdist(F.T.tri, hint, p) <= F.E.eps2) return false;
+            }
+        } else {
             ++st.fp64;
-            if (leaf_sqdist(F.T.tri, hint, p) <= F.eps2) return false;
+            if (leaf_sqdist(F.T.tri, hint, p) <= F.E.eps2) return false;
         }
     }
-    int32_t f = query_point<FP32>(F.T, p, F.eps2, F.eps2hi, st);
+    int32_t f = query_point<FP32>(F.T, p, F.E, st);
     if (f == kTraversalError) {
         atomicOr(F.counters + kCntError, 1ULL);
         return false;
@@ -693,11 +569,8 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
     const int block = 128;
     int64_t warps_needed = n;
     int grid = grid_for(warps_needed * 32, block, 16);
-    FaceCtx F{EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale}, eps2, 0.0f, counters};
+    FaceCtx F{env_tree(S), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED) {
-        F.eps2hi = (float)(eps2 * (1.0 + 3.814697265625e-06));
-        if ((double)F.eps2hi < eps2 * (1.0 + 3.814697265625e-06))
-            F.eps2hi = nextafterf(F.eps2hi, INFINITY);
         k_env_faces<true><<<grid, block, 0, s>>>(tris, n, F, sd, out);
     } else {
         k_env_faces<false><<<grid, block, 0, s>>>(tris, n, F, sd, out);

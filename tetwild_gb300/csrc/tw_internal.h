@@ -34,20 +34,26 @@ struct alignas(16) BvhNode32 {
 };
 static_assert(sizeof(BvhNode32) == 64, "BvhNode32 must be 64 bytes");
 
-// Per-facet data for a certified FP32 lower bound of the point-facet
-// distance: vertex a (FP64), unit normal n and the three in-plane outward
-// edge normals ne[e] with offsets c[e] = ne[e] . (v_e - a), all rounded to
-// binary32 from FP64.  ok = 0 for facets whose normal is not accurate to far
-// better than binary32 (degenerate or sliver facets): they are never culled.
+// Per-facet data for certified binary32 bounds of the point-facet distance,
+// all computed in FP64 and rounded to binary32: vertex a as a two-float pair
+// (ah = nearest binary32, al = a - ah rounded), unit normal n, the in-plane
+// outward unit edge normals ne[e] with offsets c[e] = ne[e] . (v_e - a), the
+// offsets o[e] = t_e . (v_e - a) along the unit edge directions
+// t_e = n x ne[e], and the edge lengths.  ok = 0 for facets whose normal is
+// not accurate to far better than binary32 (degenerate or sliver facets):
+// they always take the FP64 test.
 struct alignas(16) FacetCull {
-    double a[3];
+    float ah[3];
+    float al[3];
     float n[3];
     float ne[3][3];
     float c[3];
+    float o[3];
+    float len[3];
     uint32_t ok;
-    float pad[2];
+    float pad[4];
 };
-static_assert(sizeof(FacetCull) == 96, "FacetCull must be 96 bytes");
+static_assert(sizeof(FacetCull) == 128, "FacetCull must be 128 bytes");
 
 struct Surface {
     int32_t nf = 0;

@@ -233,10 +233,12 @@ __global__ void k_facet_cull(const double* __restrict__ tri, int32_t nf,
     double ln = sqrt(dot3(n, n));
     double lab = sqrt(dot3(ab, ab)), lac = sqrt(dot3(ac, ac));
     FacetCull C;
-    C.a[0] = v[0].x;
-    C.a[1] = v[0].y;
-    C.a[2] = v[0].z;
-    C.pad[0] = C.pad[1] = 0.0f;
+    double a[3] = {v[0].x, v[0].y, v[0].z};
+    for (int k = 0; k < 3; ++k) {
+        C.ah[k] = __double2float_rn(a[k]);
+        C.al[k] = __double2float_rn(a[k] - (double)C.ah[k]);
+    }
+    C.pad[0] = C.pad[1] = C.pad[2] = C.pad[3] = 0.0f;
     bool ok = ln > 9.5367431640625e-07 * lab * lac && isfinite(ln) && ln > 0.0;
     V3 un{0.0, 0.0, 0.0};
     if (ok) un = V3{n.x / ln, n.y / ln, n.z / ln};
@@ -247,16 +249,19 @@ __global__ void k_facet_cull(const double* __restrict__ tri, int32_t nf,
         const V3& p0 = v[e];
         const V3& p1 = v[(e + 1) % 3];
         V3 te{p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
+        double le = sqrt(dot3(te, te));
         V3 ne = cross3(te, un);  // outward for a counter-clockwise facet about n
         double l = sqrt(dot3(ne, ne));
-        if (!(l > 0.0)) ok = false;
+        if (!(l > 0.0) || !(le > 0.0)) ok = false;
         if (ok) ne = V3{ne.x / l, ne.y / l, ne.z / l};
+        V3 tu = cross3(un, ne);  // unit edge direction (n and ne orthonormal)
         V3 d{p0.x - v[0].x, p0.y - v[0].y, p0.z - v[0].z};
-        double c = ok ? dot3(ne, d) : 0.0;
         C.ne[e][0] = (float)ne.x;
         C.ne[e][1] = (float)ne.y;
         C.ne[e][2] = (float)ne.z;
-        C.c[e] = (float)c;
+        C.c[e] = ok ? (float)dot3(ne, d) : 0.0f;
+        C.o[e] = ok ? (float)dot3(tu, d) : 0.0f;
+        C.len[e] = (float)le;
     }
     C.ok = ok ? 1u : 0u;
     out[f] = C;
