@@ -116,9 +116,16 @@ __global__ void k_selftest_conv(unsigned long long n, unsigned long long* fail) 
             x = __longlong_as_double((long long)((r & 0x800fffffffffffffULL) | (e << 52)));
             break;
         }
-        default: {  // near ties: low 29 mantissa bits around the half-way point
+        case 2: {  // near ties: low 29 mantissa bits around the half-way point
             unsigned long long e = 1023ULL - 60ULL + ((r >> 52) % 120ULL);
             unsigned long long m = (r & 0x000fffffe0000000ULL) | (0x10000000ULL + ((r >> 7) & 3ULL) - 1ULL);
+            x = __longlong_as_double((long long)((r & 0x8000000000000000ULL) | (e << 52) | m));
+            break;
+        }
+        default: {  // binary32 subnormal range, underflow to zero, and its ties
+            unsigned long long e = 1023ULL - 185ULL + ((r >> 52) % 62ULL);
+            unsigned long long m = r & 0x000fffffffffffffULL;
+            if ((r >> 9) & 1ULL) m &= ~((1ULL << ((r >> 10) % 50ULL)) - 1ULL);
             x = __longlong_as_double((long long)((r & 0x8000000000000000ULL) | (e << 52) | m));
             break;
         }

@@ -313,32 +313,65 @@ __device__ __forceinline__ int orient3d(const double* p, const double* q, const 
 
 // ---------------------------------------------------------------------------
 // binary32 <-> binary64 conversions in integer arithmetic.  On this GPU the
-// hardware conversions issue to the (slow) FP64 pipe; these use the integer
-// ALU for normal numbers and take the hardware path only for zeros,
-// subnormals, infinities, NaNs and out-of-range exponents.
+// hardware conversions issue to the (slow) FP64 pipe; these use only the
+// integer ALU, for every class of input (normal, subnormal, zero, infinity,
+// NaN), and agree with the hardware bit for bit (tw_self_test checks it).
 // ---------------------------------------------------------------------------
 // Exact: every binary32 value is a binary64 value.
 __device__ __forceinline__ double f2d_exact(float f) {
     uint32_t b = __float_as_uint(f);
+    uint32_t s = b & 0x80000000u;
     uint32_t e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)f;
-    uint32_t hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((b & 0x7fffffu) >> 3);
-    uint32_t lo = b << 29;
+    uint32_t m = b & 0x7fffffu;
+    uint32_t hi, lo;
+    if (e == 0xffu) {            // inf / NaN: payload kept
+        hi = s | 0x7ff00000u | (m >> 3);
+        lo = m << 29;
+    } else if (e != 0u) {        // normal
+        hi = s | ((e + (1023u - 127u)) << 20) | (m >> 3);
+        lo = m << 29;
+    } else if (m == 0u) {        // signed zero
+        hi = s;
+        lo = 0u;
+    } else {                     // subnormal: m * 2^-149, top bit at position p
+        uint32_t p = 31u - (uint32_t)__clz(m);
+        unsigned long long mant = ((unsigned long long)m << (52u - p)) & 0x000fffffffffffffULL;
+        hi = s | ((p + 1023u - 149u) << 20) | (uint32_t)(mant >> 32);
+        lo = (uint32_t)mant;
+    }
     return __hiloint2double((int)hi, (int)lo);
 }
 // Round to nearest, ties to even (the IEEE default), like __double2float_rn.
 __device__ __forceinline__ float d2f_rn(double x) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
     uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
-    int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    if (e <= 0 || e >= 255) return __double2float_rn(x);
-    uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
-    uint32_t rest = lo & 0x1fffffffu;                  // the 29 dropped bits
-    uint32_t r = ((uint32_t)e << 23) | m;
-    // a carry out of the mantissa increments the exponent (and rounds to inf
-    // at the top of the range), as round-to-nearest requires
-    r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
-    return __uint_as_float((hi & 0x80000000u) | r);
+    uint32_t s = hi & 0x80000000u;
+    uint32_t e11 = (hi >> 20) & 0x7ffu;
+    if (e11 == 0x7ffu) {                               // inf / NaN (NaN made quiet)
+        bool nan = ((hi & 0xfffffu) | lo) != 0u;
+        return __uint_as_float(s | 0x7f800000u | (nan ? 0x00400000u | ((hi & 0xfffffu) << 3) | (lo >> 29) : 0u));
+    }
+    int e = (int)e11 - 1023 + 127;
+    if (e >= 255) return __uint_as_float(s | 0x7f800000u);   // overflow: inf
+    if (e >= 1) {                                       // normal result
+        uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
+        uint32_t rest = lo & 0x1fffffffu;                  // the 29 dropped bits
+        uint32_t r = ((uint32_t)e << 23) | m;
+        // a carry out of the mantissa increments the exponent (and rounds to
+        // inf at the top of the range), as round-to-nearest requires
+        r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+        return __uint_as_float(s | r);
+    }
+    // subnormal or zero result: value = M53 * 2^(e11 - 1075) = k * 2^-149
+    if (e11 == 0u) return __uint_as_float(s);          // double zero or subnormal
+    unsigned long long M = (b & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    uint32_t sh = 926u - e11;                           // >= 30 here
+    if (sh > 54u) return __uint_as_float(s);            // below half the smallest subnormal
+    unsigned long long k = M >> sh;
+    unsigned long long rest = M & ((1ULL << sh) - 1ULL);
+    unsigned long long half = 1ULL << (sh - 1u);
+    k += (rest > half || (rest == half && (k & 1ULL))) ? 1ULL : 0ULL;
+    return __uint_as_float(s | (uint32_t)k);            // k = 2^23 is the smallest normal
 }
 
 // ---------------------------------------------------------------------------

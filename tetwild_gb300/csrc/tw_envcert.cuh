@@ -165,6 +165,19 @@ __device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull
     return kFacetBand;
 }
 
+// The certified test of one leaf: FP32 classification, FP64 in the band.
+__device__ __forceinline__ bool cert_leaf_within(const FacetCull* __restrict__ cull,
+                                                 const double* __restrict__ tri, int32_t lf,
+                                                 const V3& p, const CertQuery& q, double eps2,
+                                                 TravStats& st) {
+    ++st.facets;
+    int cls = facet_classify(cull, lf, q);
+    if (cls == kFacetIn) return true;
+    if (cls == kFacetOut) return false;
+    ++st.fp64;
+    return leaf_sqdist(tri, lf, p) <= eps2;
+}
+
 // FP32-culled traversal; decisions identical to find_facet_within (FP64).
 __device__ __forceinline__ int32_t find_facet_within32(const BvhNode32* __restrict__ nodes,
                                                        const FacetCull* __restrict__ cull,
