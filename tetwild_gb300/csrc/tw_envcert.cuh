@@ -130,6 +130,10 @@ __device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull
         maybe[e] = s[e] + ds[e] >= 0.0f;
         sure[e] = s[e] - ds[e] > 0.0f;
     }
+    // the generic lower bound first: it excludes most facets near the query
+    // without the edge-segment terms
+    const float sm = fmaxf(fmaxf(s[0] - ds[0], s[1] - ds[1]), fmaxf(s[2] - ds[2], 0.0f));
+    if (fmaf(hlo, hlo, sm * sm) > q.e2hi) return kFacetOut;
     float L2, U2;
     if (!maybe[0] && !maybe[1] && !maybe[2]) {
         L2 = hlo * hlo;
@@ -153,12 +157,10 @@ __device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull
             Lx = fminf(Lx, fmaf(hlo, hlo, fmaf(slo, slo, xlo * xlo)));
         }
         U2 = Ux;
-        if (maybe[0] == sure[0] && maybe[1] == sure[1] && maybe[2] == sure[2]) {
+        if (maybe[0] == sure[0] && maybe[1] == sure[1] && maybe[2] == sure[2])
             L2 = Lx;
-        } else {
-            const float sm = fmaxf(fmaxf(s[0] - ds[0], s[1] - ds[1]), fmaxf(s[2] - ds[2], 0.0f));
+        else
             L2 = fmaf(hlo, hlo, sm * sm);
-        }
     }
     if (L2 > q.e2hi) return kFacetOut;
     if (U2 < q.e2lo) return kFacetIn;
@@ -208,17 +210,17 @@ __device__ __forceinline__ int32_t find_facet_within32(const BvhNode32* __restri
         float d0 = point_box_sqdist32(px, py, pz, lo0, hi0);
         float d1 = point_box_sqdist32(px, py, pz, lo1, hi1);
         bool h0 = d0 <= q.thr, h1 = d1 <= q.thr;
-        if (h0 && ch.x < 0) {
-            int32_t lf = ~ch.x;
+        // leaf children: the nearer box first, so a contained point stops sooner
+        const bool second_first = d1 < d0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const bool right = (k == 0) == second_first;
+            const int32_t c = right ? ch.y : ch.x;
+            if (!(right ? h1 : h0) || c >= 0) continue;
+            const int32_t lf = ~c;
             if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
             if (test_leaf(lf)) return lf;
-            h0 = false;
-        }
-        if (h1 && ch.y < 0) {
-            int32_t lf = ~ch.y;
-            if ((uint32_t)lf >= (uint32_t)nf) return kTraversalError;
-            if (test_leaf(lf)) return lf;
-            h1 = false;
+            if (right) h1 = false; else h0 = false;
         }
         if (h0 && h1) {
             if (sp >= kStack) return kTraversalError;

@@ -163,8 +163,8 @@ static EnvTree env_tree(const Surface& S) {
     return EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale)};
 }
 
-template <bool FP32>
-__global__ void __launch_bounds__(128) k_env_points(const double* __restrict__ P,
+template <bool FP32, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_env_points(const double* __restrict__ P,
                                                     const int32_t* __restrict__ order, int64_t n,
                                                     EnvTree T, EpsParams E,
                                                     uint8_t* __restrict__ out,
@@ -273,9 +273,11 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     }
     const EnvTree T = env_tree(S);
     const EpsParams E = eps_params(eps2);
+    // at least 6 blocks of 128 threads per SM (85 registers): measured best of
+    // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (precision == TW_PRECISION_FP32_CERTIFIED)
-        k_env_points<true><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
-                                                                    counters);
+        k_env_points<true, 6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
+                                                                       counters);
     else
         k_env_points<false><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                      counters);
