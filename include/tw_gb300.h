@@ -187,6 +187,32 @@ TW_API int tw_sample_triangle(tw_ctx* ctx, const double* tri9, double sampling_d
 TW_API int tw_newton_stars(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
                     const int32_t* centers, int32_t nstars, double* out, uint8_t* moved);
 
+/* Device-pointer variant (asynchronous on the context stream): star_off,
+ * tets, centers, out and moved are device pointers; ids are not checked.  */
+TW_API int tw_newton_stars_device(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                                  const int32_t* centers, int32_t nstars, double* out,
+                                  uint8_t* moved);
+/* Launch shape of the Newton step: lanes per star (1, 8, 16, 32) and block
+ * size (64, 128, 256), TW_NEWTON_SHAPES in all; every shape gives
+ * bit-identical results.  tw_newton_autotune_device times every shape on
+ * the given batch (device pointers, results written to out/moved), keeps the
+ * fastest in the context, and reports it and, if ms_per_shape is non-NULL,
+ * each shape's time.  No counterpart in the reference.                     */
+#define TW_NEWTON_SHAPES 10
+TW_API int tw_set_newton_shape(tw_ctx* ctx, int shape);
+TW_API int tw_newton_autotune_device(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                                     const int32_t* centers, int32_t nstars, double* out,
+                                     uint8_t* moved, int* best_shape, float* ms_per_shape);
+
+/* ---- CUDA graphs of the context stream -------------------------------------------
+ * Capture the _device calls issued between begin and end into an executable
+ * graph and replay it with one launch (the inputs are re-read from the same
+ * device pointers at every replay).  No counterpart in the reference.      */
+TW_API int tw_capture_begin(tw_ctx* ctx);
+TW_API int tw_capture_end(tw_ctx* ctx, void** graph_exec);
+TW_API int tw_graph_launch(tw_ctx* ctx, void* graph_exec);
+TW_API int tw_graph_destroy(void* graph_exec);
+
 /* ---- pinned host memory for fast copies --------------------------------------- */
 TW_API int tw_host_alloc(size_t bytes, void** out);
 TW_API int tw_host_free(void* p);

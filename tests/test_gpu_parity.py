@@ -247,3 +247,71 @@ def test_newton_stars_capped_backtracking(ctx, oracle):
     out, moved = ctx.newton_stars(off, tets, cen)
     want, wmoved = oracle.newton_stars(xyz, off, tets, cen, 1, 8, nthreads=8)
     assert np.array_equal(moved, wmoved) and np.array_equal(out, want)
+
+
+@pytest.mark.parametrize("mean_tets", [6.0, 24.0, 60.0])
+def test_newton_every_launch_shape_bitwise(ctx, oracle, mean_tets):
+    """Every launch shape (thread per star; 8, 16 or 32 lanes per star with the
+    per-tet terms added in tet order) reproduces the oracle bit for bit, on
+    stars smaller than, close to and larger than one lane group."""
+    xyz, off, tets, cen = syn.star_batch(1200, seed=12 + int(mean_tets), mean_tets=mean_tets,
+                                         lo=4, hi=96, jitter_rel=0.2)
+    ctx.set_params(1e-6, 1e-3, 15, 20)
+    ctx.mesh_upload(xyz)
+    want, wmoved = oracle.newton_stars(xyz, off, tets, cen, 15, 20, nthreads=8)
+    try:
+        for shape in range(ctx.NEWTON_SHAPES):
+            ctx.set_newton_shape(shape)
+            out, moved = ctx.newton_stars(off, tets, cen)
+            assert np.array_equal(moved, wmoved), shape
+            assert np.array_equal(out, want), shape
+    finally:
+        ctx.set_newton_shape(5)
+
+
+def test_newton_shape_rejects_unknown(ctx):
+    with pytest.raises(tw.TetWildGpuError):
+        ctx.set_newton_shape(ctx.NEWTON_SHAPES)
+    with pytest.raises(tw.TetWildGpuError):
+        ctx.set_newton_shape(-1)
+
+
+def test_newton_device_autotune_and_graph_replay(ctx, oracle):
+    """Device-pointer Newton step: autotuned shape, then captured in a CUDA
+    graph and replayed; each replay rewrites the same outputs identically."""
+    import torch
+
+    xyz, off, tets, cen = syn.star_batch(2000, seed=21, mean_tets=24.0)
+    ctx.set_params(1e-6, 1e-3, 1, 8)
+    ctx.mesh_upload(xyz)
+    want, wmoved = oracle.newton_stars(xyz, off, tets, cen, 1, 8, nthreads=8)
+    dev = torch.device("cuda", 0)
+    d_off = torch.from_numpy(off.astype(np.int32)).to(dev)
+    d_tets = torch.from_numpy(tets.astype(np.int32).reshape(-1)).to(dev)
+    d_cen = torch.from_numpy(cen.astype(np.int32)).to(dev)
+    ns = int(cen.size)
+    d_out = torch.empty(3 * ns, dtype=torch.float64, device=dev)
+    d_mov = torch.empty(ns, dtype=torch.uint8, device=dev)
+    args = (d_off.data_ptr(), d_tets.data_ptr(), d_cen.data_ptr(), ns, d_out.data_ptr(),
+            d_mov.data_ptr())
+    try:
+        torch.cuda.synchronize()
+        best, ms = ctx.newton_autotune_device(*args)
+        assert 0 <= best < ctx.NEWTON_SHAPES and all(t > 0 for t in ms)
+        assert np.array_equal(d_out.cpu().numpy().reshape(-1, 3), want)
+        d_out.fill_(0.0)
+        d_mov.fill_(7)
+        torch.cuda.synchronize()
+        ctx.capture_begin()
+        ctx.newton_stars_device(*args)
+        g = ctx.capture_end()
+        for _ in range(2):
+            g.launch()
+            ctx.synchronize()
+            assert np.array_equal(d_mov.cpu().numpy(), wmoved)
+            assert np.array_equal(d_out.cpu().numpy().reshape(-1, 3), want)
+            d_out.fill_(0.0)
+            torch.cuda.synchronize()
+        g.close()
+    finally:
+        ctx.set_newton_shape(5)

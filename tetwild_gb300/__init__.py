@@ -93,6 +93,14 @@ _SIGS = {
     "tw_envelope_faces_device": [_P, _P, _I64, _P],
     "tw_sample_triangle": [_P, _P, _D, _P, _I64, ctypes.POINTER(_I64)],
     "tw_newton_stars": [_P, _P, _P, _P, _I32, _P, _P],
+    "tw_newton_stars_device": [_P, _P, _P, _P, _I32, _P, _P],
+    "tw_set_newton_shape": [_P, _I],
+    "tw_newton_autotune_device": [_P, _P, _P, _P, _I32, _P, _P, ctypes.POINTER(_I),
+                                  ctypes.POINTER(ctypes.c_float)],
+    "tw_capture_begin": [_P],
+    "tw_capture_end": [_P, ctypes.POINTER(_P)],
+    "tw_graph_launch": [_P, _P],
+    "tw_graph_destroy": [_P],
     "tw_host_alloc": [_SZ, ctypes.POINTER(_P)],
     "tw_host_free": [_P],
     "tw_probe_peaks": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D)],
@@ -299,6 +307,36 @@ class Context:
                                              _ptr(moved)))
         return out, moved
 
+    def newton_stars_device(self, off_ptr: int, tets_ptr: int, centers_ptr: int, nstars: int,
+                            out_ptr: int, moved_ptr: int):
+        """Device-pointer variant; asynchronous on the context stream."""
+        self._check(self.lib.tw_newton_stars_device(self.h, off_ptr, tets_ptr, centers_ptr, nstars,
+                                                    out_ptr, moved_ptr))
+
+    NEWTON_SHAPES = 10
+
+    def set_newton_shape(self, shape: int):
+        self._check(self.lib.tw_set_newton_shape(self.h, shape))
+
+    def newton_autotune_device(self, off_ptr: int, tets_ptr: int, centers_ptr: int, nstars: int,
+                               out_ptr: int, moved_ptr: int):
+        """Times every launch shape on this batch; returns (best shape, ms per shape)."""
+        best = _I()
+        ms = (ctypes.c_float * self.NEWTON_SHAPES)()
+        self._check(self.lib.tw_newton_autotune_device(self.h, off_ptr, tets_ptr, centers_ptr,
+                                                       nstars, out_ptr, moved_ptr,
+                                                       ctypes.byref(best), ms))
+        return int(best.value), [float(x) for x in ms]
+
+    # -- CUDA graphs of the context stream ---------------------------------------------
+    def capture_begin(self):
+        self._check(self.lib.tw_capture_begin(self.h))
+
+    def capture_end(self) -> "Graph":
+        g = _P()
+        self._check(self.lib.tw_capture_end(self.h, ctypes.byref(g)))
+        return Graph(self, g.value)
+
     # -- misc ---------------------------------------------------------------------------
     def self_test(self, samples: int = 1 << 26):
         """(d2f_rn mismatches, f2d_exact mismatches) against the hardware conversions."""
@@ -389,6 +427,28 @@ class LocalOperations:
 
     def isFaceOutEnvelop(self, tri) -> bool:
         return bool(self.ctx.envelope_faces(np.asarray(tri).reshape(1, 9))[0])
+
+
+class Graph:
+    """An executable CUDA graph captured from the context stream."""
+
+    def __init__(self, ctx: Context, handle: int):
+        self.ctx = ctx
+        self.handle = handle
+
+    def launch(self):
+        self.ctx._check(self.ctx.lib.tw_graph_launch(self.ctx.h, self.handle))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.tw_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class VertexSmoother(LocalOperations):

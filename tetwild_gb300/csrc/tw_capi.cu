@@ -694,14 +694,105 @@ int tw_newton_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets, con
     st = sync_status(c, "tw_newton_stars");
     if (st != TW_OK) return st;
     if (hbad) return fail(c, TW_ERR_ARG, "star vertex id out of range");
-    launch_newton_stars(c->vx, c->vy, c->vz, doff, dt, dc, nstars, c->newton_max_step,
-                        c->newton_max_it, dout, dm, c->stream);
+    launch_newton_stars_shape(c->newton_shape, c->vx, c->vy, c->vz, doff, dt, dc, nstars,
+                              c->newton_max_step, c->newton_max_it, dout, dm, c->stream);
     cudaMemcpyAsync(out, dout, 24 * (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(moved, dm, (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
     return sync_status(c, "tw_newton_stars");
 }
 
 // ---- misc ---------------------------------------------------------------------------
+int tw_newton_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                           const int32_t* centers, int32_t nstars, double* out, uint8_t* moved) {
+    if (!c || nstars < 0 || (nstars > 0 && (!star_off || !tets || !centers || !out || !moved)))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    launch_newton_stars_shape(c->newton_shape, c->vx, c->vy, c->vz, star_off, tets, centers,
+                              nstars, c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_newton_stars_device");
+    return TW_OK;
+}
+
+int tw_set_newton_shape(tw_ctx* c, int shape) {
+    if (!c) return TW_ERR_ARG;
+    if (shape < 0 || shape >= newton_num_shapes())
+        return fail(c, TW_ERR_ARG, "tw_set_newton_shape: unknown shape");
+    c->newton_shape = shape;
+    return TW_OK;
+}
+
+int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                              const int32_t* centers, int32_t nstars, double* out, uint8_t* moved,
+                              int* best_shape, float* ms_per_shape) {
+    if (!c || !best_shape || nstars <= 0 || !star_off || !tets || !centers || !out || !moved)
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    int best = c->newton_shape;
+    float best_ms = 0.0f;
+    for (int sh = 0; sh < newton_num_shapes(); ++sh) {
+        float ms = 0.0f;
+        // one untimed launch, then the best of two timed launches
+        for (int rep = 0; rep < 3; ++rep) {
+            cudaEventRecord(c->ev[3], c->stream);
+            launch_newton_stars_shape(sh, c->vx, c->vy, c->vz, star_off, tets, centers, nstars,
+                                      c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+            cudaEventRecord(c->ev[4], c->stream);
+            cudaError_t e = cudaEventSynchronize(c->ev[4]);
+            if (e != cudaSuccess) return cuda_fail(c, e, "tw_newton_autotune_device");
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, c->ev[3], c->ev[4]);
+            if (rep == 1 || (rep == 2 && t < ms)) ms = t;
+        }
+        if (ms_per_shape) ms_per_shape[sh] = ms;
+        if (sh == 0 || ms < best_ms) {
+            best_ms = ms;
+            best = sh;
+        }
+    }
+    c->newton_shape = best;
+    *best_shape = best;
+    return sync_status(c, "tw_newton_autotune_device");
+}
+
+// ---- CUDA graphs of the context stream ---------------------------------------------
+int tw_capture_begin(tw_ctx* c) {
+    if (!c) return TW_ERR_ARG;
+    Guard g(c->device);
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_capture_begin");
+    return TW_OK;
+}
+
+int tw_capture_end(tw_ctx* c, void** graph_exec) {
+    if (!c || !graph_exec) return TW_ERR_ARG;
+    Guard g(c->device);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_capture_end");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_capture_end (instantiate)");
+    *graph_exec = (void*)exec;
+    return TW_OK;
+}
+
+int tw_graph_launch(tw_ctx* c, void* graph_exec) {
+    if (!c || !graph_exec) return TW_ERR_ARG;
+    Guard g(c->device);
+    cudaError_t e = cudaGraphLaunch((cudaGraphExec_t)graph_exec, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_graph_launch");
+    return TW_OK;
+}
+
+int tw_graph_destroy(void* graph_exec) {
+    if (!graph_exec) return TW_OK;
+    return cudaGraphExecDestroy((cudaGraphExec_t)graph_exec) == cudaSuccess ? TW_OK : TW_ERR_CUDA;
+}
+
 int tw_host_alloc(size_t bytes, void** out) {
     if (!out) return TW_ERR_ARG;
     cudaError_t e = cudaMallocHost(out, bytes ? bytes : 16);

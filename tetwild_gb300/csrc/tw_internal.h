@@ -102,6 +102,7 @@ struct tw_ctx {
     int32_t nv = 0;
     size_t mesh_bytes = 0;
     int precision = TW_PRECISION_FP64;
+    int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
     tw::Buffer scratch[8];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
@@ -168,6 +169,14 @@ void launch_newton_stars(const double* vx, const double* vy, const double* vz,
                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                          int32_t nstars, int max_step, int max_it, double* out, uint8_t* moved,
                          cudaStream_t s);
+// shape in [0, newton_num_shapes()): lanes per star and block size (see
+// kNewtonShapes); every shape gives bit-identical results.
+int newton_num_shapes();
+void newton_shape_info(int shape, int* group, int* block);
+void launch_newton_stars_shape(int shape, const double* vx, const double* vy, const double* vz,
+                               const int32_t* star_off, const int32_t* tets,
+                               const int32_t* centers, int32_t nstars, int max_step, int max_it,
+                               double* out, uint8_t* moved, cudaStream_t s);
 
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);

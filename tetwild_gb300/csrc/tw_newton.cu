@@ -228,15 +228,194 @@ __global__ void __launch_bounds__(128) k_newton_stars(const double* __restrict__
     moved[sid] = (uint8_t)is_moved;
 }
 
+// ---------------------------------------------------------------------------
+// Fused Newton step with G lanes per star (G = 8, 16 or 32).
+//
+// The lanes of a group evaluate the star's tets G at a time; the per-tet
+// terms are then added in tet order by broadcasting lane 0's value first,
+// lane 1's next, ...: every lane accumulates the same sequence, so every lane
+// holds the sum rounded exactly as the sequential loops of the reference
+// (VertexSmoother.cpp:654-672 for E/J/H, :606-614 for the trial energy).
+// The QR solve, the step logic and the acceptance tests are evaluated
+// redundantly by all lanes of the group (uniform within the group); a trial
+// position is rejected if any lane finds an inverted tet.
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+    return (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_newton_group(const double* __restrict__ vx,
+                                                      const double* __restrict__ vy,
+                                                      const double* __restrict__ vz,
+                                                      const int32_t* __restrict__ star_off,
+                                                      const int4* __restrict__ tets,
+                                                      const int32_t* __restrict__ centers,
+                                                      int32_t nstars, int max_step, int max_it,
+                                                      double* __restrict__ out,
+                                                      uint8_t* __restrict__ moved) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const unsigned gm = group_mask<G>(lane);
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t sid = gid; sid < nstars; sid += ngroups) {
+        const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        double pos[3] = {vx[S.v], vy[S.v], vz[S.v]};
+        int is_moved = 0;
+        double old_energy = 0.0, new_energy = 0.0, J[3], H[9];
+        for (int step = 0; step < max_step; ++step) {
+            // NewtonsUpdate: E, J, H summed over the tets in caller order
+            double e = 0.0;
+            for (int k = 0; k < 3; ++k) J[k] = 0.0;
+            for (int k = 0; k < 9; ++k) H[k] = 0.0;
+            for (int c0 = 0; c0 < nt; c0 += G) {
+                const int cnt = min(G, nt - c0);
+                double te = 0.0, tJ[3] = {0.0, 0.0, 0.0}, tH[9];
+                for (int k = 0; k < 9; ++k) tH[k] = 0.0;
+                if (gl < cnt) {
+                    int4 tv = __ldg(S.tets + c0 + gl);
+                    int start = (tv.x == S.v) ? 0 : (tv.y == S.v) ? 1 : (tv.z == S.v) ? 2
+                              : (tv.w == S.v) ? 3 : 0;
+                    double T[12];
+                    gather_tet(S, tv, start, pos, T);
+                    te = amips_energy(T);
+                    amips_egh(T, tJ, tH);
+                }
+                for (int t = 0; t < cnt; ++t) {
+                    e += __shfl_sync(gm, te, t, G);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) J[k] += __shfl_sync(gm, tJ[k], t, G);
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) H[k] += __shfl_sync(gm, tH[k], t, G);
+                }
+            }
+            if (isinf(e)) e = kMaxEnergy;
+            old_energy = e;
+            bool ok = !isnan(e) && !(e <= 0.0);
+            for (int k = 0; k < 3; ++k) ok = ok && isfinite(J[k]);
+            for (int k = 0; k < 9; ++k) ok = ok && isfinite(H[k]);
+            if (!ok) break;
+            double old_pf[3] = {pos[0], pos[1], pos[2]};
+            double X0[3] = {pos[0], pos[1], pos[2]};
+            double a = 1.0;
+            bool step_taken = false;
+            for (int it = 0; it < max_it; ++it) {
+                double rhs[3], X[3];
+                for (int i = 0; i < 3; ++i)
+                    rhs[i] = ((H[3 * i] * X0[0] + H[3 * i + 1] * X0[1]) + H[3 * i + 2] * X0[2]) -
+                             a * J[i];
+                qr_solve3(H, rhs, X);
+                if (!isfinite(X[0]) || !isfinite(X[1]) || !isfinite(X[2])) {
+                    a /= 2.0;
+                    continue;
+                }
+                pos[0] = X[0];
+                pos[1] = X[1];
+                pos[2] = X[2];
+                bool flip = false;
+                for (int c0 = gl; c0 < nt; c0 += G) {
+                    double T[12];
+                    gather_tet(S, __ldg(S.tets + c0), 0, pos, T);
+                    flip = flip || (orient3d(T, T + 3, T + 6, T + 9) != 1);
+                }
+                if (__any_sync(gm, flip)) {
+                    pos[0] = old_pf[0];
+                    pos[1] = old_pf[1];
+                    pos[2] = old_pf[2];
+                    a /= 2.0;
+                    continue;
+                }
+                double s = 0.0;
+                for (int c0 = 0; c0 < nt; c0 += G) {
+                    const int cnt = min(G, nt - c0);
+                    double te = 0.0;
+                    if (gl < cnt) {
+                        double T[12];
+                        gather_tet(S, __ldg(S.tets + c0 + gl), 0, pos, T);
+                        te = amips_energy(T);
+                    }
+                    for (int t = 0; t < cnt; ++t) s += __shfl_sync(gm, te, t, G);
+                }
+                if (isinf(s) || isnan(s) || s <= 0.0 || s > kMaxEnergy) s = kMaxEnergy;
+                new_energy = s;
+                if (new_energy >= old_energy || isinf(new_energy) || isnan(new_energy)) {
+                    pos[0] = old_pf[0];
+                    pos[1] = old_pf[1];
+                    pos[2] = old_pf[2];
+                    a /= 2.0;
+                    continue;
+                }
+                step_taken = true;
+                break;
+            }
+            if (fabs(new_energy - old_energy) < 1e-5) step_taken = false;
+            if (!step_taken) {
+                is_moved = (step != 0);
+                break;
+            }
+            is_moved = 1;
+        }
+        if (gl == 0) {
+            out[3 * sid] = pos[0];
+            out[3 * sid + 1] = pos[1];
+            out[3 * sid + 2] = pos[2];
+            moved[sid] = (uint8_t)is_moved;
+        }
+    }
+}
+
+// Launch shape of the fused step: lanes per star (8, 16, 32) and threads per
+// block (64, 128, 256); variant 0 is the one-thread-per-star kernel.
+struct NewtonShape {
+    int group;
+    int block;
+};
+static const NewtonShape kNewtonShapes[] = {{1, 128},  {8, 64},   {8, 128},  {8, 256},
+                                            {16, 64},  {16, 128}, {16, 256}, {32, 64},
+                                            {32, 128}, {32, 256}};
+int newton_num_shapes() { return (int)(sizeof(kNewtonShapes) / sizeof(kNewtonShapes[0])); }
+void newton_shape_info(int shape, int* group, int* block) {
+    if (shape < 0 || shape >= newton_num_shapes()) shape = 5;
+    *group = kNewtonShapes[shape].group;
+    *block = kNewtonShapes[shape].block;
+}
+
+void launch_newton_stars_shape(int shape, const double* vx, const double* vy, const double* vz,
+                               const int32_t* star_off, const int32_t* tets,
+                               const int32_t* centers, int32_t nstars, int max_step, int max_it,
+                               double* out, uint8_t* moved, cudaStream_t s) {
+    if (nstars <= 0) return;
+    if (shape < 0 || shape >= newton_num_shapes()) shape = 5;
+    const NewtonShape sh = kNewtonShapes[shape];
+    const int4* t4 = reinterpret_cast<const int4*>(tets);
+    if (sh.group == 1) {
+        int grid = (nstars + sh.block - 1) / sh.block;
+        k_newton_stars<<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
+                                                 max_step, max_it, out, moved);
+        return;
+    }
+    const int64_t threads = (int64_t)nstars * sh.group;
+    const int grid = grid_for(threads, sh.block, 2048 / sh.block);
+    if (sh.group == 8)
+        k_newton_group<8><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
+                                                    max_step, max_it, out, moved);
+    else if (sh.group == 16)
+        k_newton_group<16><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
+                                                     max_step, max_it, out, moved);
+    else
+        k_newton_group<32><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
+                                                     max_step, max_it, out, moved);
+}
+
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,
                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                          int32_t nstars, int max_step, int max_it, double* out, uint8_t* moved,
                          cudaStream_t s) {
-    if (nstars <= 0) return;
-    const int block = 128;
-    int grid = (nstars + block - 1) / block;
-    k_newton_stars<<<grid, block, 0, s>>>(vx, vy, vz, star_off, reinterpret_cast<const int4*>(tets),
-                                          centers, nstars, max_step, max_it, out, moved);
+    launch_newton_stars_shape(5, vx, vy, vz, star_off, tets, centers, nstars, max_step, max_it, out,
+                              moved, s);
 }
 
 }  // namespace tw
