@@ -177,6 +177,17 @@ TW_API int tw_envelope_faces_device(tw_ctx* ctx, const double* tris, int64_t n, 
 TW_API int tw_sample_triangle(tw_ctx* ctx, const double* tri9, double sampling_dist, double* out,
                        int64_t cap, int64_t* count);
 
+/* Replaces: MeshFacetsAABBWithEps::nearest_facet (mesh_AABB.h:130-141,
+ * mesh_AABB.cpp:381-480) for a batch of points.  P: [n][3].  Q: [n][3]
+ * closest points, D: [n] squared distances, F: [n] input facet indices (any
+ * output may be NULL).  Equal distances go to the smallest facet index
+ * (geogram keeps the first facet its traversal meets; the distance is the
+ * same).                                                                    */
+TW_API int tw_nearest_points(tw_ctx* ctx, const double* P, int64_t n, int which, double* Q,
+                             double* D, int32_t* F);
+TW_API int tw_nearest_points_device(tw_ctx* ctx, const double* P, int64_t n, int which, double* Q,
+                                    double* D, int32_t* F);
+
 /* ---- Newton smoothing ---------------------------------------------------------
  * Replaces: VertexSmoother::NewtonsMethod (VertexSmoother.cpp:465, decl
  * VertexSmoother.h:28) with NewtonsUpdate (:627) and getNewEnergy (:544),
@@ -203,6 +214,57 @@ TW_API int tw_set_newton_shape(tw_ctx* ctx, int shape);
 TW_API int tw_newton_autotune_device(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
                                      const int32_t* centers, int32_t nstars, double* out,
                                      uint8_t* moved, int* best_shape, float* ms_per_shape);
+
+/* ---- one smoothing pass over independent stars ---------------------------------
+ * Replaces: the per-vertex bodies of VertexSmoother::smoothSingle
+ * (VertexSmoother.cpp:114-210, interior vertices) and smoothSurface
+ * (:244-450, surface vertices; decl VertexSmoother.h:24-25), for a batch of
+ * stars whose centres are not in one another's stars, with every vertex
+ * rounded and the stored tet qualities equal to calTetQuality at the current
+ * positions.  Per star: all tets POSITIVE (else TW_SMOOTH_INVALID);
+ * NewtonsMethod with the context's max_step / max_it (not moved:
+ * TW_SMOOTH_NOT_MOVED); interior stars are then TW_SMOOTH_MOVED.  Surface
+ * stars project the Newton position on the nearest facet of the input
+ * surface (TW_STAR_BOUNDARY: of the boundary surface), then reject on an
+ * inverted tet (TW_SMOOTH_REJECT_FLIP), on max energy not decreasing
+ * (TW_SMOOTH_REJECT_QUALITY), or on a one-ring surface face outside the
+ * envelope of the input surface (TW_SMOOTH_REJECT_ENVELOPE, eps_2 and
+ * sampling_dist of tw_set_params).
+ * face_flags: [ntets], bit j set when the face of the tet opposite its j-th
+ * vertex is a surface face (is_surface_fs != NOT_SURFACE); may be NULL when
+ * every star is interior.  kinds: [nstars] TW_STAR_* (NULL: all interior).
+ * out: [nstars][3] the new position (the old one unless TW_SMOOTH_MOVED);
+ * status: [nstars] TW_SMOOTH_*.  The envelope decisions follow the
+ * context's precision mode (identical decisions in both).                  */
+#define TW_STAR_INTERIOR 0
+#define TW_STAR_SURFACE 1
+#define TW_STAR_BOUNDARY 2
+#define TW_SMOOTH_INVALID 0
+#define TW_SMOOTH_NOT_MOVED 1
+#define TW_SMOOTH_MOVED 2
+#define TW_SMOOTH_REJECT_FLIP 3
+#define TW_SMOOTH_REJECT_QUALITY 4
+#define TW_SMOOTH_REJECT_ENVELOPE 5
+TW_API int tw_smooth_stars(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                           const uint8_t* face_flags, const int32_t* centers, const uint8_t* kinds,
+                           int32_t nstars, double* out, uint8_t* status);
+/* Device-pointer variant (asynchronous on the context stream; ids and kinds
+ * are not checked, a kind other than 1 or 2 is interior).  ntets must equal
+ * star_off[nstars].  Its scratch grows on first use: a CUDA-graph capture
+ * must follow one uncaptured call of at least the same sizes.              */
+/* Times the whole pass for every Newton launch shape on this batch (device
+ * pointers; results written to out/status), keeps the fastest shape in the
+ * context and reports it and, if ms_per_shape is non-NULL, each shape's
+ * time.  No counterpart in the reference.                                  */
+TW_API int tw_smooth_autotune_device(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                                     const uint8_t* face_flags, const int32_t* centers,
+                                     const uint8_t* kinds, int32_t nstars, int64_t ntets,
+                                     double* out, uint8_t* status, int* best_shape,
+                                     float* ms_per_shape);
+TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const int32_t* tets,
+                                  const uint8_t* face_flags, const int32_t* centers,
+                                  const uint8_t* kinds, int32_t nstars, int64_t ntets, double* out,
+                                  uint8_t* status);
 
 /* ---- CUDA graphs of the context stream -------------------------------------------
  * Capture the _device calls issued between begin and end into an executable

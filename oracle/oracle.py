@@ -82,6 +82,12 @@ class Oracle:
             "two_points_out_batch": ([_P, _P, _I64, _D, _P, _I], None),
             "two_faces_out_batch": ([_P, _P, _I64, _D, _D, _P, _I], None),
             "two_newton_stars_batch": ([_P, _P, _P, _P, _I64, _I, _I, _P, _P, _I], None),
+            "two_nearest_facet": ([_P, _P, _P, _P], _I32),
+            "two_nearest_facet_brute": ([_P, _P, _P, _P], _I32),
+            "two_nearest_batch": ([_P, _P, _I64, _P, _P, _P, _I], None),
+            "two_smooth_star": ([_P, _P, _P, _I32, _I32, _I, _P, _P, _D, _D, _I, _I, _P], _I),
+            "two_smooth_stars_batch": ([_P, _P, _P, _P, _P, _P, _I64, _P, _P, _D, _D, _I, _I, _P,
+                                        _P, _I], None),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -152,6 +158,27 @@ class Oracle:
         return out, moved
 
 
+    def smooth_stars(self, xyz, star_off, tets, centers, face_flags=None, kinds=None,
+                     surface=None, boundary=None, eps2=0.0, sd=0.0, max_step=15, max_it=20,
+                     nthreads=1):
+        """One smoothing pass over independent stars (two_smooth_star): returns
+        (positions [ns,3], status [ns] int8)."""
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        C = _c(centers, np.int32)
+        FF = None if face_flags is None else _c(face_flags, np.uint8)
+        K = None if kinds is None else _c(kinds, np.uint8)
+        ns = C.size
+        out = np.empty((ns, 3))
+        st = np.empty(ns, np.int8)
+        self.L.two_smooth_stars_batch(_p(X), _p(O), _p(T), _p(FF), _p(C), _p(K), ns,
+                                      surface.h if surface is not None else None,
+                                      boundary.h if boundary is not None else None,
+                                      eps2, sd, max_step, max_it, _p(out), _p(st), nthreads)
+        return out, st
+
+
 class OracleSurface:
     def __init__(self, o: Oracle, V, F):
         self.o = o
@@ -181,6 +208,23 @@ class OracleSurface:
         self.o.L.two_faces_out_batch(self.h, _p(X), X.shape[0], eps2, sd, _p(out), nthreads)
         return out
 
+    def nearest(self, P, nthreads=1):
+        """(closest points [n,3], squared distances [n], input facet ids [n])."""
+        X = _c(P, np.float64).reshape(-1, 3)
+        n = X.shape[0]
+        Q = np.empty((n, 3))
+        D = np.empty(n)
+        F = np.empty(n, np.int32)
+        self.o.L.two_nearest_batch(self.h, _p(X), n, _p(Q), _p(D), _p(F), nthreads)
+        return Q, D, F
+
+    def nearest_brute(self, p):
+        x = _c(p, np.float64)
+        q = np.empty(3)
+        d = ctypes.c_double()
+        f = self.o.L.two_nearest_facet_brute(self.h, _p(x), _p(q), ctypes.byref(d))
+        return q, d.value, int(f)
+
 
 class RefLib:
     """The reference's own code (oracle/_ref/libtwref.so)."""
@@ -197,6 +241,7 @@ class RefLib:
             "twref_surface_free": ([_P], None),
             "twref_points_out": ([_P, _P, _I64, _D, _P, _I], None),
             "twref_faces_out": ([_P, _P, _I64, _D, _D, _P, _I], None),
+            "twref_nearest": ([_P, _P, _I64, _P, _P, _I], None),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -253,3 +298,12 @@ class RefSurface:
         out = np.empty(X.shape[0], np.uint8)
         self.r.L.twref_faces_out(self.h, _p(X), X.shape[0], eps2, sd, _p(out), nthreads)
         return out
+
+    def nearest(self, P, nthreads=1):
+        """(closest points [n,3], squared distances [n]) from the reference's tree."""
+        X = _c(P, np.float64).reshape(-1, 3)
+        n = X.shape[0]
+        Q = np.empty((n, 3))
+        D = np.empty(n)
+        self.r.L.twref_nearest(self.h, _p(X), n, _p(Q), _p(D), nthreads)
+        return Q, D

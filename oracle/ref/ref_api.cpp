@@ -208,4 +208,23 @@ void twref_faces_out(void* h, const double* tris, int64_t n, double eps2, double
     });
 }
 
+// MeshFacetsAABBWithEps::nearest_facet (mesh_AABB.h:130-141): closest point
+// and squared distance (the facet index refers to the tree's reordered facets
+// and is not returned).
+void twref_nearest(void* h, const double* P, int64_t n, double* Q, double* D, int nthreads) {
+    RefSurface* s = static_cast<RefSurface*>(h);
+    parallel_for(n, nthreads, [=](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            GEO::vec3 p(P[3 * i], P[3 * i + 1], P[3 * i + 2]);
+            GEO::vec3 q;
+            double d = 0.0;
+            s->tree->nearest_facet(p, q, d);
+            Q[3 * i] = q.x;
+            Q[3 * i + 1] = q.y;
+            Q[3 * i + 2] = q.z;
+            D[i] = d;
+        }
+    });
+}
+
 }  // extern "C"

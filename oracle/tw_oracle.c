@@ -628,6 +628,7 @@ int64_t two_sample_count(const double v[9], double sd)
 struct two_surface {
     int32_t nf;
     double* tri;      /* 9 doubles per facet, tree order */
+    int32_t* fid;     /* input facet index of each tree position */
     double* box;      /* 6 doubles per node (lo, hi), implicit indexing */
     int32_t nbox;
     double scale;     /* max |coordinate| of the surface */
@@ -713,6 +714,8 @@ two_surface* two_surface_build(const double* V, int32_t nV, const int32_t* F, in
     }
     tw_median_order(cen, ids, nF, 0, scratch);
     s->tri = (double*)malloc(sizeof(double) * 9 * (size_t)nF);
+    s->fid = (int32_t*)malloc(sizeof(int32_t) * (size_t)nF);
+    for (int32_t i = 0; i < nF; ++i) s->fid[i] = ids[i];
     for (int32_t i = 0; i < nF; ++i)
         for (int v = 0; v < 3; ++v)
             for (int k = 0; k < 3; ++k) s->tri[9 * i + 3 * v + k] = V[3 * F[3 * ids[i] + v] + k];
@@ -730,6 +733,7 @@ void two_surface_free(two_surface* s)
 {
     if (!s) return;
     free(s->tri);
+    free(s->fid);
     free(s->box);
     free(s);
 }
@@ -783,6 +787,99 @@ int two_point_out_brute(const two_surface* s, const double p[3], double eps2)
         if (two_point_triangle_sqdist(p, t, t + 3, t + 6, NULL) <= eps2) return 0;
     }
     return 1;
+}
+
+/* =========================================================================
+ * Nearest facet (MeshFacetsAABBWithEps::nearest_facet, mesh_AABB.h:130-141,
+ * mesh_AABB.cpp:381-480): the facet with the smallest point-facet squared
+ * distance (the closest-point routine above) and its closest point.  Among
+ * facets at exactly the same computed distance, the smallest input facet
+ * index wins.  (geogram keeps the first one its traversal meets, and that
+ * order follows its own facet reordering, which is not part of the
+ * reference sources; the distance is the same either way.)  A child box is
+ * skipped only when its squared distance exceeds (b + tau)^2, b = sqrt of
+ * the best distance so far, tau = 64 * 2^-53 * max|coord| + 16 * 2^-53 * b:
+ * a facet whose computed distance could tie or beat the best is never
+ * skipped, so the result is the exact minimum over all facets, whatever the
+ * tree.
+ * ========================================================================= */
+typedef struct {
+    double d;
+    int32_t id;
+    double q[3];
+} tw_nearest_t;
+
+static double tw_nearest_threshold(const two_surface* s, const double p[3], double best)
+{
+    if (!(best < INFINITY)) return INFINITY;
+    double m = s->scale;
+    for (int k = 0; k < 3; ++k)
+        if (fabs(p[k]) > m) m = fabs(p[k]);
+    double b = sqrt(best);
+    double tau = 64.0 * TW_EPS * m + 16.0 * TW_EPS * b;
+    return (b + tau) * (b + tau);
+}
+
+static void tw_nearest_recursive(const two_surface* s, const double p[3], tw_nearest_t* best,
+                                 int32_t node, int32_t b, int32_t e)
+{
+    if (b + 1 == e) {
+        const double* t = s->tri + 9 * b;
+        double q[3];
+        double d = two_point_triangle_sqdist(p, t, t + 3, t + 6, q);
+        int32_t id = s->fid[b];
+        if (d < best->d || (d == best->d && id < best->id)) {
+            best->d = d;
+            best->id = id;
+            best->q[0] = q[0]; best->q[1] = q[1]; best->q[2] = q[2];
+        }
+        return;
+    }
+    int32_t m = b + (e - b) / 2;
+    const double* L = s->box + 12 * node;
+    const double* R = L + 6;
+    double dl = two_point_box_sqdist(p, L, L + 3);
+    double dr = two_point_box_sqdist(p, R, R + 3);
+    if (dl <= dr) {
+        if (dl <= tw_nearest_threshold(s, p, best->d)) tw_nearest_recursive(s, p, best, 2 * node, b, m);
+        if (dr <= tw_nearest_threshold(s, p, best->d)) tw_nearest_recursive(s, p, best, 2 * node + 1, m, e);
+    } else {
+        if (dr <= tw_nearest_threshold(s, p, best->d)) tw_nearest_recursive(s, p, best, 2 * node + 1, m, e);
+        if (dl <= tw_nearest_threshold(s, p, best->d)) tw_nearest_recursive(s, p, best, 2 * node, b, m);
+    }
+}
+
+int32_t two_nearest_facet(const two_surface* s, const double p[3], double q[3], double* sqd)
+{
+    tw_nearest_t best;
+    best.d = INFINITY;
+    best.id = INT32_MAX;
+    best.q[0] = best.q[1] = best.q[2] = 0.0;
+    if (s) tw_nearest_recursive(s, p, &best, 1, 0, s->nf);
+    if (q) { q[0] = best.q[0]; q[1] = best.q[1]; q[2] = best.q[2]; }
+    if (sqd) *sqd = best.d;
+    return s ? best.id : -1;
+}
+
+int32_t two_nearest_facet_brute(const two_surface* s, const double p[3], double q[3], double* sqd)
+{
+    tw_nearest_t best;
+    best.d = INFINITY;
+    best.id = INT32_MAX;
+    best.q[0] = best.q[1] = best.q[2] = 0.0;
+    for (int32_t f = 0; s && f < s->nf; ++f) {
+        const double* t = s->tri + 9 * f;
+        double qq[3];
+        double d = two_point_triangle_sqdist(p, t, t + 3, t + 6, qq);
+        if (d < best.d || (d == best.d && s->fid[f] < best.id)) {
+            best.d = d;
+            best.id = s->fid[f];
+            best.q[0] = qq[0]; best.q[1] = qq[1]; best.q[2] = qq[2];
+        }
+    }
+    if (q) { q[0] = best.q[0]; q[1] = best.q[1]; q[2] = best.q[2]; }
+    if (sqd) *sqd = best.d;
+    return s ? best.id : -1;
 }
 
 /* isFaceOutEnvelop_sampling, LocalOperations.cpp:1046-1109: a degenerate
@@ -997,6 +1094,108 @@ int two_newton_star(const double* xyz, const int32_t* tets, int32_t nt, int32_t 
 }
 
 /* =========================================================================
+ * One vertex of a smoothing pass (VertexSmoother.cpp).  Interior vertex:
+ * the body of smoothSingle (:114-210); surface vertex: the body of
+ * smoothSurface (:244-450) with the defaults use_onering_projection = false
+ * and use_energy_max = true (State.h:53,60), isBoundarySlide returning false
+ * (LocalOperations.cpp:1123-1124), every vertex already rounded (posf ==
+ * pos), and the stored tet qualities equal to calTetQuality at the current
+ * positions.
+ *   1. every tet of the star must be POSITIVE at the current positions
+ *      (:161-170, :289-297), else TWO_SMOOTH_INVALID;
+ *   2. NewtonsMethod (:465-542); not moved -> TWO_SMOOTH_NOT_MOVED;
+ *   interior: the final isFlip (:189-194) cannot fire (every accepted trial
+ *      passed the same exact test) and is kept as a check; -> MOVED;
+ *   surface: 3. the Newton position is projected on the nearest facet of the
+ *      input surface (boundary vertices: of the boundary surface) (:353-363);
+ *   4. isFlip at the projected position -> REJECT_FLIP (:374-378);
+ *   5. max calTetQuality after < max before, else REJECT_QUALITY (:379-386);
+ *   6. each one-ring surface face (faces through the vertex that the caller
+ *      flags as surface faces, as sorted vertex triples without repeats),
+ *      written from the vertex onward in the cyclic order of its sorted
+ *      triple, must pass isFaceOutEnvelop on the input surface (:417-440),
+ *      else REJECT_ENVELOPE.
+ * fflags[i] bit j: the face of tet i opposite its j-th vertex is a surface
+ * face (is_surface_fs != NOT_SURFACE).  out = the new position when MOVED,
+ * else the old one.
+ * ========================================================================= */
+static int tw_tri_key_cmp(const int32_t* a, const int32_t* b)
+{
+    for (int k = 0; k < 3; ++k) {
+        if (a[k] < b[k]) return -1;
+        if (a[k] > b[k]) return 1;
+    }
+    return 0;
+}
+
+int two_smooth_star(const double* xyz, const int32_t* tets, const uint8_t* fflags, int32_t nt,
+                    int32_t v, int kind, const two_surface* s_in, const two_surface* s_b,
+                    double eps2, double sd, int max_step, int max_it, double out[3])
+{
+    const double* p0 = xyz + 3 * (size_t)v;
+    double T[12];
+    out[0] = p0[0]; out[1] = p0[1]; out[2] = p0[2];
+    for (int32_t i = 0; i < nt; ++i) {
+        tw_gather(xyz, tets + 4 * i, v, p0, 0, T);
+        if (two_orient3d(T, T + 3, T + 6, T + 9) != 1) return TWO_SMOOTH_INVALID;
+    }
+    double pf[3];
+    if (!two_newton_star(xyz, tets, nt, v, max_step, max_it, pf)) return TWO_SMOOTH_NOT_MOVED;
+    if (kind == TWO_STAR_INTERIOR) {
+        if (tw_star_flip(xyz, tets, nt, v, pf)) return TWO_SMOOTH_REJECT_FLIP;
+        out[0] = pf[0]; out[1] = pf[1]; out[2] = pf[2];
+        return TWO_SMOOTH_MOVED;
+    }
+    const two_surface* tree = (kind == TWO_STAR_BOUNDARY) ? s_b : s_in;
+    if (!tree || !s_in) return -1;
+    double p[3];
+    two_nearest_facet(tree, pf, p, NULL);
+    if (tw_star_flip(xyz, tets, nt, v, p)) return TWO_SMOOTH_REJECT_FLIP;
+    double old_max = 0.0, new_max = 0.0;
+    for (int32_t i = 0; i < nt; ++i) {
+        tw_gather(xyz, tets + 4 * i, v, p0, 0, T);
+        double e = two_tet_quality(T);
+        if (e > old_max) old_max = e;
+        tw_gather(xyz, tets + 4 * i, v, p, 0, T);
+        e = two_tet_quality(T);
+        if (e > new_max) new_max = e;
+    }
+    if (!(new_max < old_max)) return TWO_SMOOTH_REJECT_QUALITY;
+    for (int32_t i = 0; i < nt; ++i) {
+        const int32_t* t = tets + 4 * i;
+        for (int j = 0; j < 4; ++j) {
+            if (t[j] == v || !((fflags[i] >> j) & 1)) continue;
+            int32_t key[3] = {t[(j + 1) % 4], t[(j + 2) % 4], t[(j + 3) % 4]};
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2 - a; ++b)
+                    if (key[b] > key[b + 1]) { int32_t x = key[b]; key[b] = key[b + 1]; key[b + 1] = x; }
+            /* repeated triple: only its first occurrence is tested */
+            int seen = 0;
+            for (int32_t i2 = 0; i2 <= i && !seen; ++i2) {
+                const int32_t* t2 = tets + 4 * i2;
+                for (int j2 = 0; j2 < 4 && !seen; ++j2) {
+                    if (i2 == i && j2 >= j) break;
+                    if (t2[j2] == v || !((fflags[i2] >> j2) & 1)) continue;
+                    int32_t k2[3] = {t2[(j2 + 1) % 4], t2[(j2 + 2) % 4], t2[(j2 + 3) % 4]};
+                    for (int a = 0; a < 2; ++a)
+                        for (int b = 0; b < 2 - a; ++b)
+                            if (k2[b] > k2[b + 1]) { int32_t x = k2[b]; k2[b] = k2[b + 1]; k2[b + 1] = x; }
+                    seen = (tw_tri_key_cmp(key, k2) == 0);
+                }
+            }
+            if (seen) continue;
+            int k = (key[0] == v) ? 0 : (key[1] == v) ? 1 : 2;
+            const double* b1 = xyz + 3 * (size_t)key[(k + 1) % 3];
+            const double* b2 = xyz + 3 * (size_t)key[(k + 2) % 3];
+            double tri[9] = {p[0], p[1], p[2], b1[0], b1[1], b1[2], b2[0], b2[1], b2[2]};
+            if (two_face_out(s_in, tri, eps2, sd)) return TWO_SMOOTH_REJECT_ENVELOPE;
+        }
+    }
+    out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
+    return TWO_SMOOTH_MOVED;
+}
+
+/* =========================================================================
  * Threaded batch drivers.
  * ========================================================================= */
 typedef struct {
@@ -1006,6 +1205,10 @@ typedef struct {
     const void* a1;
     const void* a2;
     const void* a3;
+    const void* a4;
+    const void* a5;
+    const void* a6;
+    const void* a7;
     double d0, d1;
     int i0, i1, i2;
     void* o0;
@@ -1071,6 +1274,39 @@ static void tw_run_stars(tw_job* j)
         moved[i] = (uint8_t)mv;
     }
 }
+static void tw_run_smooth(tw_job* j)
+{
+    const double* xyz = (const double*)j->a0;
+    const int32_t* off = (const int32_t*)j->a1;
+    const int32_t* tets = (const int32_t*)j->a2;
+    const int32_t* cen = (const int32_t*)j->a3;
+    const uint8_t* ff = (const uint8_t*)j->a4;
+    const uint8_t* kinds = (const uint8_t*)j->a5;
+    double* out = (double*)j->o0;
+    int8_t* status = (int8_t*)j->o1;
+    for (int64_t i = j->lo; i < j->hi; ++i) {
+        int32_t b = off[i], e = off[i + 1];
+        status[i] = (int8_t)two_smooth_star(xyz, tets + 4 * (size_t)b, ff ? ff + b : NULL, e - b,
+                                            cen[i], kinds ? kinds[i] : TWO_STAR_INTERIOR,
+                                            (const two_surface*)j->a6, (const two_surface*)j->a7,
+                                            j->d0, j->d1, j->i0, j->i1, out + 3 * i);
+    }
+}
+static void tw_run_nearest(tw_job* j)
+{
+    const two_surface* s = (const two_surface*)j->a0;
+    const double* P = (const double*)j->a1;
+    double* Q = (double*)j->o0;
+    double* D = (double*)j->o1;
+    int32_t* F = (int32_t*)j->o2;
+    for (int64_t i = j->lo; i < j->hi; ++i) {
+        double q[3], d;
+        int32_t f = two_nearest_facet(s, P + 3 * i, q, &d);
+        if (Q) { Q[3 * i] = q[0]; Q[3 * i + 1] = q[1]; Q[3 * i + 2] = q[2]; }
+        if (D) D[i] = d;
+        if (F) F[i] = f;
+    }
+}
 static void* tw_thread_main(void* arg)
 {
     tw_job* j = (tw_job*)arg;
@@ -1079,6 +1315,8 @@ static void* tw_thread_main(void* arg)
     case 1: tw_run_points(j); break;
     case 2: tw_run_faces(j); break;
     case 3: tw_run_stars(j); break;
+    case 4: tw_run_smooth(j); break;
+    case 5: tw_run_nearest(j); break;
     default: break;
     }
     return NULL;
@@ -1160,4 +1398,44 @@ void two_newton_stars_batch(const double* xyz, const int32_t* star_off, const in
     j.o0 = out;
     j.o1 = moved;
     tw_parallel(j, nstars, nthreads);
+}
+
+void two_smooth_stars_batch(const double* xyz, const int32_t* star_off, const int32_t* tets,
+                            const uint8_t* fflags, const int32_t* centers, const uint8_t* kinds,
+                            int64_t nstars, const two_surface* s_in, const two_surface* s_b,
+                            double eps2, double sd, int max_step, int max_it, double* out,
+                            int8_t* status, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 4;
+    j.a0 = xyz;
+    j.a1 = star_off;
+    j.a2 = tets;
+    j.a3 = centers;
+    j.a4 = fflags;
+    j.a5 = kinds;
+    j.a6 = s_in;
+    j.a7 = s_b;
+    j.d0 = eps2;
+    j.d1 = sd;
+    j.i0 = max_step;
+    j.i1 = max_it;
+    j.o0 = out;
+    j.o1 = status;
+    tw_parallel(j, nstars, nthreads);
+}
+
+void two_nearest_batch(const two_surface* s, const double* P, int64_t n, double* Q, double* D,
+                       int32_t* F, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 5;
+    j.a0 = s;
+    j.a1 = P;
+    j.o0 = Q;
+    j.o1 = D;
+    j.o2 = F;
+    tw_parallel(j, n, nthreads);
 }

@@ -80,6 +80,26 @@ int two_qr_solve3(const double H[9], const double b[3], double x[3]);
 int two_newton_star(const double* xyz, const int32_t* tets, int32_t ntets, int32_t v,
                     int max_step, int max_it, double out[3]);
 
+/* ---- nearest facet (MeshFacetsAABBWithEps::nearest_facet, mesh_AABB.h:130) */
+/* Returns the input index of the nearest facet (smallest squared distance,  *
+ * ties to the smallest index), its closest point q and the squared distance.*/
+int32_t two_nearest_facet(const two_surface* s, const double p[3], double q[3], double* sqd);
+int32_t two_nearest_facet_brute(const two_surface* s, const double p[3], double q[3], double* sqd);
+
+/* ---- one vertex of a smoothing pass (VertexSmoother.cpp:114-210, 244-450) - */
+#define TWO_STAR_INTERIOR 0
+#define TWO_STAR_SURFACE 1
+#define TWO_STAR_BOUNDARY 2
+#define TWO_SMOOTH_INVALID 0
+#define TWO_SMOOTH_NOT_MOVED 1
+#define TWO_SMOOTH_MOVED 2
+#define TWO_SMOOTH_REJECT_FLIP 3
+#define TWO_SMOOTH_REJECT_QUALITY 4
+#define TWO_SMOOTH_REJECT_ENVELOPE 5
+int two_smooth_star(const double* xyz, const int32_t* tets, const uint8_t* fflags, int32_t ntets,
+                    int32_t v, int kind, const two_surface* s_in, const two_surface* s_b,
+                    double eps2, double sampling_dist, int max_step, int max_it, double out[3]);
+
 /* ---- batch drivers (pthreads; nthreads <= 0 means 1) --------------------- */
 /* T is SoA [12][n] (the energy_ispc layout).  Any output may be NULL.       *
  * J and H are SoA ([3][n], [9][n]).  flip[i] = two_tet_flip; E[i] is the    *
@@ -93,6 +113,14 @@ void two_faces_out_batch(const two_surface* s, const double* tris, int64_t n, do
 void two_newton_stars_batch(const double* xyz, const int32_t* star_off, const int32_t* tets,
                             const int32_t* centers, int64_t nstars, int max_step, int max_it,
                             double* out, uint8_t* moved, int nthreads);
+
+void two_smooth_stars_batch(const double* xyz, const int32_t* star_off, const int32_t* tets,
+                            const uint8_t* fflags, const int32_t* centers, const uint8_t* kinds,
+                            int64_t nstars, const two_surface* s_in, const two_surface* s_b,
+                            double eps2, double sampling_dist, int max_step, int max_it,
+                            double* out, int8_t* status, int nthreads);
+void two_nearest_batch(const two_surface* s, const double* P, int64_t n, double* Q, double* D,
+                       int32_t* F, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -16,8 +16,13 @@ rational arithmetic (Python fractions) for the orientation signs:
                     (LocalOperations.cpp:1034-1109 over mesh_AABB.cpp)
   orient_exact.npz  adversarial point quadruples and their exact
                     det[q-p, r-p, s-p] signs (CGAL::orientation convention)
+  nearest_ref.npz   a small displaced-sphere surface, query points near and
+                    far from it, and the closest points and squared
+                    distances of the reference's
+                    MeshFacetsAABBWithEps::nearest_facet (mesh_AABB.h:130)
 
-Run: python tests/golden/make_golden.py
+Run: python tests/golden/make_golden.py [fixture names without .npz]
+(all fixtures when no name is given)
 """
 from __future__ import annotations
 
@@ -105,10 +110,24 @@ def orient_cases(rng):
     return quads, signs
 
 
-def main():
+def make_nearest(ref):
+    V, F = syn.displaced_sphere(seed=8, n_lon=40, n_rings=20)
+    rng = np.random.default_rng(77)
+    P = syn.envelope_points(V, F, 3000, 1e-2, seed=9)
+    P = np.vstack([P, P[:1000] + rng.normal(0.0, 0.05, (1000, 3)),
+                   rng.uniform(-2.0, 2.0, (500, 3))])
+    Q, D = ref.surface(V, F).nearest(P)
+    np.savez_compressed(HERE / "nearest_ref.npz", V=V, F=F, P=P, Q=Q, D=D)
+
+
+def main(names=None):
     rng = np.random.default_rng(2024)
     ref = RefLib()
-    out = {}
+    if names:
+        if "nearest_ref" in names:
+            make_nearest(ref)
+        return
+    make_nearest(ref)
 
     T = amips_cases(rng)
     E, J, H = ref.amips_batch_soa(T.T.copy())
@@ -151,4 +170,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -309,3 +309,93 @@ def test_newton_star_decreases_energy(oracle):
         # never inverts a tet
         flips = oracle.amips_batch_soa(np.ascontiguousarray(X[T].reshape(-1, 12).T))[3]
         assert flips.sum() == 0 or not moved[s]
+
+
+# -------------------------------------------------------- nearest facet ----
+def _nearest_vs(Q, D, Qr, Dr):
+    """Distances identical everywhere; closest points identical except where
+    two facets tie at the same distance (the tie goes to a different facet)."""
+    assert np.array_equal(D, Dr)
+    diff = np.any(Q != Qr, axis=1)
+    # ties happen where the closest feature is an edge shared by two facets
+    # (computed once from each side) and are rarer the nearer the points
+    assert diff.mean() < 0.02, diff.mean()
+    if diff.any():
+        # a tie: both points are at the same distance and agree to a few ulps
+        err = np.abs(Q[diff] - Qr[diff]) / np.maximum(1.0, np.abs(Qr[diff]))
+        assert err.max() <= 4.5e-16, err.max()
+    return int(diff.sum())
+
+
+def test_nearest_matches_reference_golden(oracle):
+    g = golden("nearest_ref.npz")
+    Q, D, Fi = oracle.surface(g["V"], g["F"]).nearest(g["P"], nthreads=4)
+    _nearest_vs(Q, D, g["Q"], g["D"])
+    assert (Fi >= 0).all() and (Fi < len(g["F"])).all()
+
+
+def test_nearest_matches_reference_live(oracle, reflib):
+    V, F = syn.displaced_sphere(seed=3, n_lon=100, n_rings=50)
+    P = syn.envelope_points(V, F, 20000, 1e-3, seed=4)
+    P = np.vstack([P, P[:5000] + np.random.default_rng(5).normal(0, 0.02, (5000, 3))])
+    Q, D, _ = oracle.surface(V, F).nearest(P, nthreads=8)
+    Qr, Dr = reflib.surface(V, F).nearest(P, nthreads=8)
+    _nearest_vs(Q, D, Qr, Dr)
+
+
+def test_nearest_tree_equals_brute_force(oracle):
+    V, F = syn.displaced_sphere(seed=6, n_lon=30, n_rings=15)
+    rng = np.random.default_rng(7)
+    P = np.vstack([syn.envelope_points(V, F, 300, 1e-2, seed=8), rng.uniform(-1.5, 1.5, (100, 3))])
+    S = oracle.surface(V, F)
+    Q, D, Fi = S.nearest(P)
+    for i in range(len(P)):
+        q, d, f = S.nearest_brute(P[i])
+        assert d == D[i] and f == Fi[i] and np.array_equal(q, Q[i])
+
+
+# ------------------------------------------------------ smoothing pass ----
+def test_smooth_interior_is_newton(oracle):
+    """Interior stars: the pass equals NewtonsMethod wherever the star is valid."""
+    xyz, off, tets, cen = syn.star_batch(300, seed=15, jitter_rel=0.25)
+    out, st = oracle.smooth_stars(xyz, off, tets, cen, max_step=15, max_it=20, nthreads=4)
+    want, moved = oracle.newton_stars(xyz, off, tets, cen, 15, 20, nthreads=4)
+    valid = st != 0
+    assert valid.mean() > 0.5
+    assert np.array_equal(st[valid] == 2, moved[valid] == 1)
+    m = st == 2
+    assert np.array_equal(out[m], want[m])
+    assert np.array_equal(out[~m], xyz[cen[~m]])
+
+
+def test_smooth_surface_outcomes_are_consistent(oracle):
+    """Surface stars: accepted positions lie on the surface (projection), keep
+    every tet positive, lower the max energy and keep the one-ring surface
+    faces in the envelope; rejected stars keep their old position."""
+    V, F = syn.displaced_sphere(seed=0, n_lon=60, n_rings=30)
+    eps = 1e-3
+    xyz, off, tets, ff, cen = syn.surface_star_batch(V, F, 400, eps, seed=2)
+    S = oracle.surface(V, F)
+    kinds = np.ones(len(cen), np.uint8)
+    out, st = oracle.smooth_stars(xyz, off, tets, cen, ff, kinds, surface=S, boundary=S,
+                                  eps2=eps * eps, sd=eps / 2, max_step=1, max_it=8, nthreads=4)
+    counts = np.bincount(st, minlength=6)
+    assert counts[2] > 50 and counts[4] + counts[5] > 10, counts
+    rej = st != 2
+    assert np.array_equal(out[rej], xyz[cen[rej]])
+    for i in np.nonzero(st == 2)[0][:60]:
+        q, d, _ = S.nearest(out[i:i + 1])
+        assert d[0] <= 1e-24
+        T = tets[off[i]:off[i + 1]]
+        X = xyz.copy()
+        old = X[T].reshape(-1, 12)
+        X[cen[i]] = out[i]
+        new = X[T].reshape(-1, 12)
+        qo = [oracle.L.two_tet_quality(np.ascontiguousarray(t).ctypes.data) for t in old]
+        qn = [oracle.L.two_tet_quality(np.ascontiguousarray(t).ctypes.data) for t in new]
+        assert max(qn) < max(qo) and max(qn) < 1e50
+        tris = []
+        for t in T:
+            tri = X[[t[0], t[1], t[2]]]  # face opposite vertex 3 (the flagged one)
+            tris.append(tri.reshape(9))
+        assert not S.faces_out(np.asarray(tris), eps * eps, eps / 2).any()

@@ -34,6 +34,15 @@ TW_ENERGY_RAW = 0
 TW_ENERGY_QUALITY = 1
 TW_SURFACE_INPUT = 0
 TW_SURFACE_BOUNDARY = 1
+TW_STAR_INTERIOR = 0
+TW_STAR_SURFACE = 1
+TW_STAR_BOUNDARY = 2
+TW_SMOOTH_INVALID = 0
+TW_SMOOTH_NOT_MOVED = 1
+TW_SMOOTH_MOVED = 2
+TW_SMOOTH_REJECT_FLIP = 3
+TW_SMOOTH_REJECT_QUALITY = 4
+TW_SMOOTH_REJECT_ENVELOPE = 5
 MAX_ENERGY = 1e50  # State.h:29
 
 _PKG = Path(__file__).resolve().parent
@@ -95,6 +104,12 @@ _SIGS = {
     "tw_newton_stars": [_P, _P, _P, _P, _I32, _P, _P],
     "tw_newton_stars_device": [_P, _P, _P, _P, _I32, _P, _P],
     "tw_set_newton_shape": [_P, _I],
+    "tw_nearest_points": [_P, _P, _I64, _I, _P, _P, _P],
+    "tw_nearest_points_device": [_P, _P, _I64, _I, _P, _P, _P],
+    "tw_smooth_stars": [_P, _P, _P, _P, _P, _P, _I32, _P, _P],
+    "tw_smooth_stars_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P],
+    "tw_smooth_autotune_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P, ctypes.POINTER(_I),
+                                  ctypes.POINTER(ctypes.c_float)],
     "tw_newton_autotune_device": [_P, _P, _P, _P, _I32, _P, _P, ctypes.POINTER(_I),
                                   ctypes.POINTER(ctypes.c_float)],
     "tw_capture_begin": [_P],
@@ -314,6 +329,55 @@ class Context:
                                                     out_ptr, moved_ptr))
 
     NEWTON_SHAPES = 10
+
+    # -- smoothing pass ------------------------------------------------------------------
+    def smooth_stars(self, star_off, tets, centers, face_flags=None, kinds=None):
+        """One smoothing pass (smoothSingle / smoothSurface bodies) over independent stars.
+        Returns (positions [ns,3], status [ns] TW_SMOOTH_*)."""
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        C = _c(centers, np.int32)
+        FF = None if face_flags is None else _c(face_flags, np.uint8)
+        K = None if kinds is None else _c(kinds, np.uint8)
+        ns = C.size
+        out = np.empty((ns, 3))
+        st = np.empty(ns, np.uint8)
+        self._check(self.lib.tw_smooth_stars(self.h, _ptr(O), _ptr(T), _ptr(FF), _ptr(C), _ptr(K),
+                                             ns, _ptr(out), _ptr(st)))
+        return out, st
+
+    def smooth_stars_device(self, off_ptr: int, tets_ptr: int, ff_ptr, centers_ptr: int, kinds_ptr,
+                            nstars: int, ntets: int, out_ptr: int, status_ptr: int):
+        """Device-pointer variant; asynchronous on the context stream."""
+        self._check(self.lib.tw_smooth_stars_device(self.h, off_ptr, tets_ptr, ff_ptr, centers_ptr,
+                                                    kinds_ptr, nstars, ntets, out_ptr, status_ptr))
+
+    def smooth_autotune_device(self, off_ptr: int, tets_ptr: int, ff_ptr, centers_ptr: int,
+                               kinds_ptr, nstars: int, ntets: int, out_ptr: int, status_ptr: int):
+        """Times the pass for every launch shape on this batch; returns (best, ms per shape)."""
+        best = _I()
+        ms = (ctypes.c_float * self.NEWTON_SHAPES)()
+        self._check(self.lib.tw_smooth_autotune_device(self.h, off_ptr, tets_ptr, ff_ptr,
+                                                       centers_ptr, kinds_ptr, nstars, ntets,
+                                                       out_ptr, status_ptr, ctypes.byref(best), ms))
+        return int(best.value), [float(x) for x in ms]
+
+    # -- nearest facet -----------------------------------------------------------------
+    def nearest_points(self, P, which=TW_SURFACE_INPUT):
+        """(closest points [n,3], squared distances [n], input facet ids [n])."""
+        X = _c(P, np.float64).reshape(-1, 3)
+        n = X.shape[0]
+        Q = np.empty((n, 3))
+        D = np.empty(n)
+        F = np.empty(n, np.int32)
+        self._check(self.lib.tw_nearest_points(self.h, _ptr(X), n, which, _ptr(Q), _ptr(D),
+                                               _ptr(F)))
+        return Q, D, F
+
+    def nearest_points_device(self, P_ptr: int, n: int, Q_ptr, D_ptr, F_ptr,
+                              which=TW_SURFACE_INPUT):
+        self._check(self.lib.tw_nearest_points_device(self.h, P_ptr, n, which, Q_ptr, D_ptr,
+                                                      F_ptr))
 
     def set_newton_shape(self, shape: int):
         self._check(self.lib.tw_set_newton_shape(self.h, shape))

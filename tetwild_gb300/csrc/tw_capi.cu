@@ -205,6 +205,8 @@ int sync_status(tw_ctx* c, const char* where) {
         std::string m = std::string(where) + ": ";
         if (err & 1ULL) m += "surface traversal exceeded its bounds (corrupt tree); ";
         if (err & 2ULL) m += "a face exceeds the per-row sample bound (4e6 samples); ";
+        if (err & 4ULL) m += "a boundary star without a boundary surface; ";
+        if (err & 8ULL) m += "smoothing face list exceeded its capacity; ";
         return fail(c, TW_ERR_ARG, m);
     }
     return TW_OK;
@@ -701,6 +703,187 @@ int tw_newton_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets, con
     return sync_status(c, "tw_newton_stars");
 }
 
+// ---- nearest facet -------------------------------------------------------------------
+int tw_nearest_points_device(tw_ctx* c, const double* P, int64_t n, int which, double* Q,
+                             double* D, int32_t* F) {
+    if (!c || n < 0 || (n > 0 && !P)) return TW_ERR_ARG;
+    if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
+    if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    Guard g(c->device);
+    launch_nearest_points(c->surf[which], P, n, Q, D, F, c->counters, c->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_nearest_points_device");
+    return TW_OK;
+}
+
+int tw_nearest_points(tw_ctx* c, const double* P, int64_t n, int which, double* Q, double* D,
+                      int32_t* F) {
+    if (!c || n < 0 || (n > 0 && !P)) return TW_ERR_ARG;
+    if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
+    if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
+    if (n == 0) return TW_OK;
+    Guard g(c->device);
+    void* p;
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t bytes = align(24 * (size_t)n) * 2 + align(8 * (size_t)n) + align(4 * (size_t)n);
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    double* dP = (double*)q; q += align(24 * (size_t)n);
+    double* dQ = (double*)q; q += align(24 * (size_t)n);
+    double* dD = (double*)q; q += align(8 * (size_t)n);
+    int32_t* dF = (int32_t*)q;
+    cudaMemcpyAsync(dP, P, 24 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    launch_nearest_points(c->surf[which], dP, n, Q ? dQ : nullptr, D ? dD : nullptr,
+                          F ? dF : nullptr, c->counters, c->stream);
+    if (Q) cudaMemcpyAsync(Q, dQ, 24 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (D) cudaMemcpyAsync(D, dD, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (F) cudaMemcpyAsync(F, dF, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_nearest_points");
+}
+
+// ---- smoothing pass ----------------------------------------------------------------
+namespace {
+// Scratch of a smoothing pass (slot 8): per star the Newton / projected
+// position, face range and state; per possible face (3 per tet) its nine
+// coordinates and decision; the face counter.
+struct SmoothScratch {
+    double* pnew;
+    int32_t* face_base;
+    int32_t* face_cnt;
+    double* faces;
+    uint8_t* face_out;
+    unsigned long long* face_count;
+    int64_t face_cap;
+};
+
+int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S) {
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const int64_t cap = 3 * ntets;
+    if (cap > (int64_t)INT32_MAX) return fail(c, TW_ERR_TOO_LARGE, "smoothing batch too large");
+    const size_t ns = (size_t)nstars, nc = (size_t)cap;
+    const size_t bytes = align(24 * ns) + 2 * align(4 * ns) + align(72 * nc) + align(nc) + 256;
+    void* p;
+    int st = ensure(c, 8, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    S.pnew = (double*)q; q += align(24 * ns);
+    S.face_base = (int32_t*)q; q += align(4 * ns);
+    S.face_cnt = (int32_t*)q; q += align(4 * ns);
+    S.faces = (double*)q; q += align(72 * nc);
+    S.face_out = (uint8_t*)q; q += align(nc);
+    S.face_count = (unsigned long long*)q;
+    S.face_cap = cap;
+    return TW_OK;
+}
+
+// The pass on device arrays; asynchronous on the context stream.
+void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uint8_t* ff,
+                   const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
+                   double* out, uint8_t* status, const SmoothScratch& S) {
+    launch_smooth_stage1(c->newton_shape, c->vx, c->vy, c->vz, off, tets, cen, kinds, nstars,
+                         c->newton_max_step, c->newton_max_it, out, S.pnew, status, c->stream);
+    if (!any_surface) return;
+    cudaMemsetAsync(S.face_count, 0, sizeof(unsigned long long), c->stream);
+    launch_smooth_project(c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], kinds, nstars,
+                          status, S.pnew, c->counters, c->stream);
+    launch_smooth_stage2(c->newton_shape, c->vx, c->vy, c->vz, off, tets, ff, cen, nstars, S.pnew,
+                         status, S.faces, S.face_count, S.face_cap, S.face_base, S.face_cnt,
+                         c->counters, c->stream);
+    launch_env_faces_dev(c->surf[TW_SURFACE_INPUT], S.faces, S.face_count, S.face_cap, c->eps2,
+                         c->sampling_dist, S.face_out, c->precision, c->counters, c->stream);
+    launch_smooth_finalize(nstars, S.face_base, S.face_cnt, S.face_out, S.pnew, out, status,
+                           c->stream);
+}
+}  // namespace
+
+int tw_smooth_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                           const uint8_t* face_flags, const int32_t* centers, const uint8_t* kinds,
+                           int32_t nstars, int64_t ntets, double* out, uint8_t* status) {
+    if (!c || nstars < 0 || ntets < 0 ||
+        (nstars > 0 && (!star_off || !centers || !out || !status || (ntets > 0 && !tets))))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (nstars == 0) return TW_OK;
+    const bool any_surface = kinds != nullptr;
+    if (any_surface && !face_flags) return fail(c, TW_ERR_ARG, "surface stars need face_flags");
+    if (any_surface && c->surf[TW_SURFACE_INPUT].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no input surface uploaded");
+    Guard g(c->device);
+    SmoothScratch S;
+    int st = smooth_scratch(c, nstars, ntets, S);
+    if (st != TW_OK) return st;
+    smooth_launch(c, star_off, tets, face_flags, centers, kinds, nstars, any_surface, out, status, S);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "tw_smooth_stars_device");
+    return TW_OK;
+}
+
+int tw_smooth_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                    const uint8_t* face_flags, const int32_t* centers, const uint8_t* kinds,
+                    int32_t nstars, double* out, uint8_t* status) {
+    if (!c || nstars < 0 || (nstars > 0 && (!star_off || !tets || !centers || !out || !status)))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (nstars == 0) return TW_OK;
+    if (star_off[0] != 0) return fail(c, TW_ERR_ARG, "star offsets must start at 0");
+    for (int32_t i = 0; i < nstars; ++i)
+        if (star_off[i + 1] < star_off[i]) return fail(c, TW_ERR_ARG, "star offsets decrease");
+    bool any_surface = false, any_boundary = false;
+    if (kinds) {
+        for (int32_t i = 0; i < nstars; ++i) {
+            if (kinds[i] > TW_STAR_BOUNDARY) return fail(c, TW_ERR_ARG, "unknown star kind");
+            any_surface = any_surface || kinds[i] != TW_STAR_INTERIOR;
+            any_boundary = any_boundary || kinds[i] == TW_STAR_BOUNDARY;
+        }
+    }
+    if (any_surface && !face_flags) return fail(c, TW_ERR_ARG, "surface stars need face_flags");
+    if (any_surface && c->surf[TW_SURFACE_INPUT].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no input surface uploaded");
+    if (any_boundary && c->surf[TW_SURFACE_BOUNDARY].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no boundary surface uploaded");
+    const int64_t nt = star_off[nstars];
+    Guard g(c->device);
+    SmoothScratch S;
+    int st = smooth_scratch(c, nstars, nt, S);
+    if (st != TW_OK) return st;
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t ns = (size_t)nstars;
+    const size_t bytes = align(4 * (ns + 1)) + align(16 * (size_t)nt) + align((size_t)nt) +
+                         align(4 * ns) + align(ns) + align(24 * ns) + align(ns) + 256;
+    void* p;
+    st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* doff = (int32_t*)q; q += align(4 * (ns + 1));
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)nt);
+    uint8_t* dff = (uint8_t*)q; q += align((size_t)nt);
+    int32_t* dc = (int32_t*)q; q += align(4 * ns);
+    uint8_t* dk = (uint8_t*)q; q += align(ns);
+    double* dout = (double*)q; q += align(24 * ns);
+    uint8_t* dst = (uint8_t*)q; q += align(ns);
+    int* bad = (int*)q;
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemcpyAsync(doff, star_off, 4 * (ns + 1), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    if (any_surface) cudaMemcpyAsync(dff, face_flags, (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dc, centers, 4 * ns, cudaMemcpyHostToDevice, c->stream);
+    if (kinds) cudaMemcpyAsync(dk, kinds, ns, cudaMemcpyHostToDevice, c->stream);
+    if (nt > 0)
+        k_check_ids<<<(unsigned)((4 * nt + 255) / 256), 256, 0, c->stream>>>(dt, 4 * nt, c->nv, bad);
+    k_check_ids<<<(unsigned)((ns + 255) / 256), 256, 0, c->stream>>>(dc, nstars, c->nv, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_smooth_stars");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "star vertex id out of range");
+    smooth_launch(c, doff, dt, any_surface ? dff : nullptr, dc, kinds ? dk : nullptr, nstars,
+                  any_surface, dout, dst, S);
+    cudaMemcpyAsync(out, dout, 24 * ns, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(status, dst, ns, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_smooth_stars");
+}
+
 // ---- misc ---------------------------------------------------------------------------
 int tw_newton_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
                            const int32_t* centers, int32_t nstars, double* out, uint8_t* moved) {
@@ -723,25 +906,22 @@ int tw_set_newton_shape(tw_ctx* c, int shape) {
     return TW_OK;
 }
 
-int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
-                              const int32_t* centers, int32_t nstars, double* out, uint8_t* moved,
-                              int* best_shape, float* ms_per_shape) {
-    if (!c || !best_shape || nstars <= 0 || !star_off || !tets || !centers || !out || !moved)
-        return TW_ERR_ARG;
-    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
-    Guard g(c->device);
+namespace {
+// Times run(shape) for every launch shape (one untimed launch, then the best
+// of two timed ones, CUDA events on the context stream), keeps the fastest
+// shape in the context.
+template <class Run>
+int autotune_shapes(tw_ctx* c, const char* where, int* best_shape, float* ms_per_shape, Run run) {
     int best = c->newton_shape;
     float best_ms = 0.0f;
     for (int sh = 0; sh < newton_num_shapes(); ++sh) {
         float ms = 0.0f;
-        // one untimed launch, then the best of two timed launches
         for (int rep = 0; rep < 3; ++rep) {
             cudaEventRecord(c->ev[3], c->stream);
-            launch_newton_stars_shape(sh, c->vx, c->vy, c->vz, star_off, tets, centers, nstars,
-                                      c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+            run(sh);
             cudaEventRecord(c->ev[4], c->stream);
             cudaError_t e = cudaEventSynchronize(c->ev[4]);
-            if (e != cudaSuccess) return cuda_fail(c, e, "tw_newton_autotune_device");
+            if (e != cudaSuccess) return cuda_fail(c, e, where);
             float t = 0.0f;
             cudaEventElapsedTime(&t, c->ev[3], c->ev[4]);
             if (rep == 1 || (rep == 2 && t < ms)) ms = t;
@@ -754,7 +934,47 @@ int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t*
     }
     c->newton_shape = best;
     *best_shape = best;
-    return sync_status(c, "tw_newton_autotune_device");
+    return sync_status(c, where);
+}
+}  // namespace
+
+int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                              const int32_t* centers, int32_t nstars, double* out, uint8_t* moved,
+                              int* best_shape, float* ms_per_shape) {
+    if (!c || !best_shape || nstars <= 0 || !star_off || !tets || !centers || !out || !moved)
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    return autotune_shapes(c, "tw_newton_autotune_device", best_shape, ms_per_shape, [&](int sh) {
+        launch_newton_stars_shape(sh, c->vx, c->vy, c->vz, star_off, tets, centers, nstars,
+                                  c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+    });
+}
+
+int tw_smooth_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
+                              const uint8_t* face_flags, const int32_t* centers,
+                              const uint8_t* kinds, int32_t nstars, int64_t ntets, double* out,
+                              uint8_t* status, int* best_shape, float* ms_per_shape) {
+    if (!c || !best_shape || nstars <= 0 || ntets < 0 || !star_off || !tets || !centers || !out ||
+        !status)
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    const bool any_surface = kinds != nullptr;
+    if (any_surface && !face_flags) return fail(c, TW_ERR_ARG, "surface stars need face_flags");
+    if (any_surface && c->surf[TW_SURFACE_INPUT].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no input surface uploaded");
+    Guard g(c->device);
+    SmoothScratch S;
+    int st = smooth_scratch(c, nstars, ntets, S);
+    if (st != TW_OK) return st;
+    const int keep = c->newton_shape;
+    st = autotune_shapes(c, "tw_smooth_autotune_device", best_shape, ms_per_shape, [&](int sh) {
+        c->newton_shape = sh;
+        smooth_launch(c, star_off, tets, face_flags, centers, kinds, nstars, any_surface, out,
+                      status, S);
+    });
+    if (st != TW_OK) c->newton_shape = keep;
+    return st;
 }
 
 // ---- CUDA graphs of the context stream ---------------------------------------------

@@ -511,11 +511,10 @@ __device__ __forceinline__ double quality_from(int ori, double e) {
 // (Real-Time Collision Detection, 2005, sec. 5.1.5); degenerate face region
 // falls back to the three edges.  Same operation order as the oracle.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double seg_sqdist(const V3& p, const V3& a, const V3& b) {
+__device__ __forceinline__ double seg_nearest(const V3& p, const V3& a, const V3& b, V3& q) {
     V3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
     V3 ap{p.x - a.x, p.y - a.y, p.z - a.z};
     double t = dot3(ap, ab), l = dot3(ab, ab);
-    V3 q;
     if (t <= 0.0 || l <= 0.0) {
         q = a;
     } else if (t >= l) {
@@ -528,12 +527,15 @@ __device__ __forceinline__ double seg_sqdist(const V3& p, const V3& a, const V3&
     return dot3(d, d);
 }
 
-__device__ __forceinline__ double point_tri_sqdist(const V3& p, const V3& a, const V3& b,
-                                                   const V3& c) {
+// Closest point q of triangle (a, b, c) to p and the squared distance
+// |p - q|^2 (Voronoi regions, Ericson 2005 sec. 5.1.5); a triangle whose face
+// region is degenerate falls back to the nearest of its edges ab, bc, ca
+// (first one on ties).
+__device__ __forceinline__ double point_tri_nearest(const V3& p, const V3& a, const V3& b,
+                                                    const V3& c, V3& q) {
     V3 ab{b.x - a.x, b.y - a.y, b.z - a.z};
     V3 ac{c.x - a.x, c.y - a.y, c.z - a.z};
     V3 ap{p.x - a.x, p.y - a.y, p.z - a.z};
-    V3 q;
     double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
     if (d1 <= 0.0 && d2 <= 0.0) {
         q = a;
@@ -567,11 +569,12 @@ __device__ __forceinline__ double point_tri_sqdist(const V3& p, const V3& a, con
                         } else {
                             double den = (va + vb) + vc;
                             if (!(den > 0.0)) {
-                                double best = seg_sqdist(p, a, b);
-                                double d = seg_sqdist(p, b, c);
-                                if (d < best) best = d;
-                                d = seg_sqdist(p, c, a);
-                                if (d < best) best = d;
+                                V3 qa, qb;
+                                double best = seg_nearest(p, a, b, q);
+                                double d = seg_nearest(p, b, c, qa);
+                                if (d < best) { best = d; q = qa; }
+                                d = seg_nearest(p, c, a, qb);
+                                if (d < best) { best = d; q = qb; }
                                 return best;
                             }
                             double inv = 1.0 / den;
@@ -586,6 +589,12 @@ __device__ __forceinline__ double point_tri_sqdist(const V3& p, const V3& a, con
     }
     V3 d{p.x - q.x, p.y - q.y, p.z - q.z};
     return dot3(d, d);
+}
+
+__device__ __forceinline__ double point_tri_sqdist(const V3& p, const V3& a, const V3& b,
+                                                   const V3& c) {
+    V3 q;
+    return point_tri_nearest(p, a, b, c, q);
 }
 
 // Outside part of point_box_signed_squared_distance (mesh_AABB.cpp:201-220).

@@ -133,6 +133,7 @@ struct EnvTree {
     int32_t nf;
     double scale;
     float scale_hi;  // scale rounded up to binary32
+    const int32_t* facet_id;  // input facet index of each leaf
 };
 
 template <bool FP32>
@@ -160,7 +161,8 @@ static float round_up_float(double x) {
     return ((double)f < x) ? std::nextafter(f, INFINITY) : f;
 }
 static EnvTree env_tree(const Surface& S) {
-    return EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale)};
+    return EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale),
+                   S.facet_id};
 }
 
 template <bool FP32, int MINB = 1>
@@ -463,8 +465,9 @@ __device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_
 }
 
 template <bool FP32>
-__global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tris, int64_t n,
-                                                   FaceCtx F, double sd, uint8_t* __restrict__ out) {
+__device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris, int64_t n,
+                                                 const FaceCtx& F, double sd,
+                                                 uint8_t* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -565,6 +568,12 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
     flush_stats(st, F.counters, nq);
 }
 
+template <bool FP32>
+__global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tris, int64_t n,
+                                                   FaceCtx F, double sd, uint8_t* __restrict__ out) {
+    k_env_faces_body<FP32>(tris, n, F, sd, out);
+}
+
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0) return;
@@ -577,6 +586,215 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
     } else {
         k_env_faces<false><<<grid, block, 0, s>>>(tris, n, F, sd, out);
     }
+}
+
+// Envelope faces whose count is known only on the device (*n_dev, at most
+// cap): the grid is sized for cap and the warps beyond *n_dev exit at once.
+template <bool FP32>
+__global__ void __launch_bounds__(128) k_env_faces_dev(const double* __restrict__ tris,
+                                                       const unsigned long long* __restrict__ n_dev,
+                                                       int64_t cap, FaceCtx F, double sd,
+                                                       uint8_t* __restrict__ out) {
+    const int64_t n = (int64_t)min((unsigned long long)cap, *n_dev);
+    k_env_faces_body<FP32>(tris, n, F, sd, out);
+}
+
+void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned long long* n_dev,
+                          int64_t cap, double eps2, double sd, uint8_t* out, int precision,
+                          unsigned long long* counters, cudaStream_t s) {
+    if (cap <= 0) return;
+    const int block = 128;
+    int grid = grid_for(cap * 32, block, 16);
+    FaceCtx F{env_tree(S), eps_params(eps2), counters};
+    if (precision == TW_PRECISION_FP32_CERTIFIED)
+        k_env_faces_dev<true><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
+    else
+        k_env_faces_dev<false><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
+}
+
+// ---------------------------------------------------------------------------
+// Nearest facet (MeshFacetsAABBWithEps::nearest_facet, mesh_AABB.h:130-141,
+// mesh_AABB.cpp:381-480): the facet with the smallest computed squared
+// distance and its closest point; equal distances go to the smallest input
+// facet index.  A child box is skipped only when its squared distance exceeds
+// (b + tau)^2, b = sqrt(best so far), tau = 64 * 2^-53 * max|coord| +
+// 16 * 2^-53 * b, so no facet that could tie or beat the best is skipped and
+// the result is the exact minimum over all facets, independent of the tree.
+// Returns the input facet index, or kTraversalError.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nearest_threshold(double best, double m) {
+    if (!(best < INFINITY)) return INFINITY;
+    double b = sqrt(best);
+    double tau = 64.0 * kEps * m + 16.0 * kEps * b;
+    return (b + tau) * (b + tau);
+}
+
+__device__ __forceinline__ void nearest_leaf(const EnvTree& T, int32_t leaf, const V3& p,
+                                             double& best, int32_t& best_id, V3& best_q) {
+    const double* t = T.tri + 9 * (int64_t)leaf;
+    V3 a{__ldg(t + 0), __ldg(t + 1), __ldg(t + 2)};
+    V3 b{__ldg(t + 3), __ldg(t + 4), __ldg(t + 5)};
+    V3 c{__ldg(t + 6), __ldg(t + 7), __ldg(t + 8)};
+    V3 q;
+    double d = point_tri_nearest(p, a, b, c, q);
+    int32_t id = __ldg(T.facet_id + leaf);
+    if (d < best || (d == best && id < best_id)) {
+        best = d;
+        best_id = id;
+        best_q = q;
+    }
+}
+
+__device__ int32_t nearest_facet(const EnvTree& T, const V3& p, V3& q, double& sqd) {
+    double m = T.scale;
+    m = fmax(m, fabs(p.x));
+    m = fmax(m, fabs(p.y));
+    m = fmax(m, fabs(p.z));
+    double best = INFINITY;
+    int32_t best_id = 0x7fffffff;
+    V3 best_q{0.0, 0.0, 0.0};
+    const int32_t nf = T.nf;
+    if (nf == 1) {
+        nearest_leaf(T, 0, p, best, best_id, best_q);
+        q = best_q;
+        sqd = best;
+        return best_id;
+    }
+    int32_t stack[kStack];
+    double sdist[kStack];
+    int sp = 0;
+    int32_t cur = 0;
+    for (int32_t iter = 0; iter < 2 * nf; ++iter) {
+        if ((uint32_t)cur >= (uint32_t)(nf - 1)) return kTraversalError;
+        const double2* nd = reinterpret_cast<const double2*>(T.nodes + cur);
+        double2 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+        double2 q3 = __ldg(nd + 3), q4 = __ldg(nd + 4), q5 = __ldg(nd + 5);
+        int2 ch = __ldg(reinterpret_cast<const int2*>(nd + 6));
+        double lo0[3] = {q0.x, q0.y, q1.x}, hi0[3] = {q1.y, q2.x, q2.y};
+        double lo1[3] = {q3.x, q3.y, q4.x}, hi1[3] = {q4.y, q5.x, q5.y};
+        double d0 = point_box_sqdist(p, lo0, hi0);
+        double d1 = point_box_sqdist(p, lo1, hi1);
+        // nearer child first
+        int32_t cn = ch.x, cf = ch.y;
+        double dn = d0, df = d1;
+        if (d1 < d0) {
+            cn = ch.y; cf = ch.x;
+            dn = d1; df = d0;
+        }
+        bool hn = dn <= nearest_threshold(best, m);
+        if (hn && cn < 0) {
+            if ((uint32_t)(~cn) >= (uint32_t)nf) return kTraversalError;
+            nearest_leaf(T, ~cn, p, best, best_id, best_q);
+            hn = false;
+        }
+        bool hf = df <= nearest_threshold(best, m);
+        if (hf && cf < 0) {
+            if ((uint32_t)(~cf) >= (uint32_t)nf) return kTraversalError;
+            nearest_leaf(T, ~cf, p, best, best_id, best_q);
+            hf = false;
+        }
+        if (hn && hf) {
+            if (sp >= kStack) return kTraversalError;
+            stack[sp] = cf;
+            sdist[sp] = df;
+            ++sp;
+            cur = cn;
+        } else if (hn) {
+            cur = cn;
+        } else if (hf) {
+            cur = cf;
+        } else {
+            // pop the next subtree still within reach of the best distance
+            cur = -1;
+            while (sp > 0) {
+                --sp;
+                if (sdist[sp] <= nearest_threshold(best, m)) {
+                    cur = stack[sp];
+                    break;
+                }
+            }
+            if (cur < 0) {
+                q = best_q;
+                sqd = best;
+                return best_id;
+            }
+        }
+    }
+    return kTraversalError;
+}
+
+__global__ void k_nearest_points(EnvTree T, const double* __restrict__ P, int64_t n,
+                                 double* __restrict__ Q, double* __restrict__ D,
+                                 int32_t* __restrict__ Fo, unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
+        V3 q;
+        double d;
+        int32_t f = nearest_facet(T, p, q, d);
+        if (f == kTraversalError) {
+            atomicOr(counters + kCntError, 1ULL);
+            q = p;
+            d = 0.0;
+            f = -1;
+        }
+        if (Q) {
+            Q[3 * i] = q.x;
+            Q[3 * i + 1] = q.y;
+            Q[3 * i + 2] = q.z;
+        }
+        if (D) D[i] = d;
+        if (Fo) Fo[i] = f;
+    }
+}
+
+void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,
+                           int32_t* F, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0 || S.nf <= 0) return;
+    const int block = 128;
+    k_nearest_points<<<grid_for(n, block, 8), block, 0, s>>>(env_tree(S), P, n, Q, D, F, counters);
+}
+
+// Projection step of surface smoothing (VertexSmoother.cpp:353-363): every
+// star whose status is kSmoothPendingProject moves its Newton position to the
+// closest point of the nearest facet of the input surface (kind 1) or of the
+// boundary surface (kind 2).  A boundary star without a boundary surface is
+// an argument error (error bit 4) and is left invalid.
+__global__ void k_smooth_project(EnvTree Tin, EnvTree Tb, const uint8_t* __restrict__ kinds,
+                                 int32_t nstars, uint8_t* __restrict__ status,
+                                 double* __restrict__ pnew,
+                                 unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nstars; i += stride) {
+        if (status[i] != kSmoothPendingProject) continue;
+        const bool bnd = kinds[i] == TW_STAR_BOUNDARY;
+        const EnvTree& T = bnd ? Tb : Tin;
+        if (T.nf <= 0) {
+            atomicOr(counters + kCntError, 4ULL);
+            status[i] = TW_SMOOTH_INVALID;
+            continue;
+        }
+        V3 p{pnew[3 * i], pnew[3 * i + 1], pnew[3 * i + 2]};
+        V3 q;
+        double d;
+        if (nearest_facet(T, p, q, d) == kTraversalError) {
+            atomicOr(counters + kCntError, 1ULL);
+            status[i] = TW_SMOOTH_INVALID;
+            continue;
+        }
+        pnew[3 * i] = q.x;
+        pnew[3 * i + 1] = q.y;
+        pnew[3 * i + 2] = q.z;
+    }
+}
+
+void launch_smooth_project(const Surface& Sin, const Surface& Sb, const uint8_t* kinds,
+                           int32_t nstars, uint8_t* status, double* pnew,
+                           unsigned long long* counters, cudaStream_t s) {
+    if (nstars <= 0) return;
+    const int block = 128;
+    k_smooth_project<<<grid_for(nstars, block, 8), block, 0, s>>>(env_tree(Sin), env_tree(Sb), kinds,
+                                                                 nstars, status, pnew, counters);
 }
 
 // One thread generates the full sample list in the reference order with the

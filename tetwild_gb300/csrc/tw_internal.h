@@ -103,7 +103,7 @@ struct tw_ctx {
     size_t mesh_bytes = 0;
     int precision = TW_PRECISION_FP64;
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
-    tw::Buffer scratch[8];
+    tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
     std::string last_error;
@@ -120,6 +120,9 @@ constexpr int kCntAmipsTets = 5;      // tets evaluated by the AMIPS kernels
 constexpr int kCntAmipsFp64 = 6;      // tets recomputed in FP64 (certified mode)
 constexpr int kCntBad = 7;            // host-visible argument check flag
 constexpr int kCntEnvQueries = 8;     // envelope sample/point queries
+// internal star states of a smoothing pass (the final ones are TW_SMOOTH_*)
+constexpr uint8_t kSmoothPendingProject = 6;   // surface star moved by Newton, not yet projected
+constexpr uint8_t kSmoothPendingEnvelope = 7;  // surface star waiting for its face tests
 }  // namespace tw
 
 namespace tw {
@@ -163,6 +166,15 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
 void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
                             int64_t* count, cudaStream_t s);
+// faces whose count *n_dev (<= cap) is known only on the device
+void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned long long* n_dev,
+                          int64_t cap, double eps2, double sd, uint8_t* out, int precision,
+                          unsigned long long* counters, cudaStream_t s);
+void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,
+                           int32_t* F, unsigned long long* counters, cudaStream_t s);
+void launch_smooth_project(const Surface& Sin, const Surface& Sb, const uint8_t* kinds,
+                           int32_t nstars, uint8_t* status, double* pnew,
+                           unsigned long long* counters, cudaStream_t s);
 
 // ---- launchers (tw_newton.cu) ----
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,
@@ -177,6 +189,26 @@ void launch_newton_stars_shape(int shape, const double* vx, const double* vy, co
                                const int32_t* star_off, const int32_t* tets,
                                const int32_t* centers, int32_t nstars, int max_step, int max_it,
                                double* out, uint8_t* moved, cudaStream_t s);
+
+// Smoothing pass (tw_newton.cu): stage 1 = validity + NewtonsMethod (interior
+// stars finish here, surface stars become kSmoothPendingProject with their
+// Newton position in pnew); stage 2 (after launch_smooth_project) = flip and
+// quality checks at the projected position and the list of one-ring surface
+// faces (appended at face_count; face_base/face_cnt per star); finalize =
+// the face results decide the surface stars.
+void launch_smooth_stage1(int shape, const double* vx, const double* vy, const double* vz,
+                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
+                          const uint8_t* kinds, int32_t nstars, int max_step, int max_it,
+                          double* out, double* pnew, uint8_t* status, cudaStream_t s);
+void launch_smooth_stage2(int shape, const double* vx, const double* vy, const double* vz,
+                          const int32_t* star_off, const int32_t* tets, const uint8_t* face_flags,
+                          const int32_t* centers, int32_t nstars, const double* pnew,
+                          uint8_t* status, double* faces, unsigned long long* face_count,
+                          int64_t face_cap, int32_t* face_base, int32_t* face_cnt,
+                          unsigned long long* counters, cudaStream_t s);
+void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
+                            const uint8_t* face_out, const double* pnew, double* out,
+                            uint8_t* status, cudaStream_t s);
 
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);

@@ -245,6 +245,109 @@ __device__ __forceinline__ unsigned group_mask(int lane) {
     return (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
 }
 
+// NewtonsMethod for the star S with G lanes; every lane returns the same
+// position and is_moved.
+template <int G>
+__device__ __forceinline__ int newton_group_star(const StarView& S, double* pos, int max_step,
+                                                 int max_it, int gl, unsigned gm) {
+    const int32_t nt = S.nt;
+    int is_moved = 0;
+    double old_energy = 0.0, new_energy = 0.0, J[3], H[9];
+    for (int step = 0; step < max_step; ++step) {
+        // NewtonsUpdate: E, J, H summed over the tets in caller order
+        double e = 0.0;
+        for (int k = 0; k < 3; ++k) J[k] = 0.0;
+        for (int k = 0; k < 9; ++k) H[k] = 0.0;
+        for (int c0 = 0; c0 < nt; c0 += G) {
+            const int cnt = min(G, nt - c0);
+            double te = 0.0, tJ[3] = {0.0, 0.0, 0.0}, tH[9];
+            for (int k = 0; k < 9; ++k) tH[k] = 0.0;
+            if (gl < cnt) {
+                int4 tv = __ldg(S.tets + c0 + gl);
+                int start = (tv.x == S.v) ? 0 : (tv.y == S.v) ? 1 : (tv.z == S.v) ? 2
+                          : (tv.w == S.v) ? 3 : 0;
+                double T[12];
+                gather_tet(S, tv, start, pos, T);
+                te = amips_energy(T);
+                amips_egh(T, tJ, tH);
+            }
+            for (int t = 0; t < cnt; ++t) {
+                e += __shfl_sync(gm, te, t, G);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) J[k] += __shfl_sync(gm, tJ[k], t, G);
+#pragma unroll
+                for (int k = 0; k < 9; ++k) H[k] += __shfl_sync(gm, tH[k], t, G);
+            }
+        }
+        if (isinf(e)) e = kMaxEnergy;
+        old_energy = e;
+        bool ok = !isnan(e) && !(e <= 0.0);
+        for (int k = 0; k < 3; ++k) ok = ok && isfinite(J[k]);
+        for (int k = 0; k < 9; ++k) ok = ok && isfinite(H[k]);
+        if (!ok) break;
+        double old_pf[3] = {pos[0], pos[1], pos[2]};
+        double X0[3] = {pos[0], pos[1], pos[2]};
+        double a = 1.0;
+        bool step_taken = false;
+        for (int it = 0; it < max_it; ++it) {
+            double rhs[3], X[3];
+            for (int i = 0; i < 3; ++i)
+                rhs[i] = ((H[3 * i] * X0[0] + H[3 * i + 1] * X0[1]) + H[3 * i + 2] * X0[2]) -
+                         a * J[i];
+            qr_solve3(H, rhs, X);
+            if (!isfinite(X[0]) || !isfinite(X[1]) || !isfinite(X[2])) {
+                a /= 2.0;
+                continue;
+            }
+            pos[0] = X[0];
+            pos[1] = X[1];
+            pos[2] = X[2];
+            bool flip = false;
+            for (int c0 = gl; c0 < nt; c0 += G) {
+                double T[12];
+                gather_tet(S, __ldg(S.tets + c0), 0, pos, T);
+                flip = flip || (orient3d(T, T + 3, T + 6, T + 9) != 1);
+            }
+            if (__any_sync(gm, flip)) {
+                pos[0] = old_pf[0];
+                pos[1] = old_pf[1];
+                pos[2] = old_pf[2];
+                a /= 2.0;
+                continue;
+            }
+            double sum = 0.0;
+            for (int c0 = 0; c0 < nt; c0 += G) {
+                const int cnt = min(G, nt - c0);
+                double te = 0.0;
+                if (gl < cnt) {
+                    double T[12];
+                    gather_tet(S, __ldg(S.tets + c0 + gl), 0, pos, T);
+                    te = amips_energy(T);
+                }
+                for (int t = 0; t < cnt; ++t) sum += __shfl_sync(gm, te, t, G);
+            }
+            if (isinf(sum) || isnan(sum) || sum <= 0.0 || sum > kMaxEnergy) sum = kMaxEnergy;
+            new_energy = sum;
+            if (new_energy >= old_energy || isinf(new_energy) || isnan(new_energy)) {
+                pos[0] = old_pf[0];
+                pos[1] = old_pf[1];
+                pos[2] = old_pf[2];
+                a /= 2.0;
+                continue;
+            }
+            step_taken = true;
+            break;
+        }
+        if (fabs(new_energy - old_energy) < 1e-5) step_taken = false;
+        if (!step_taken) {
+            is_moved = (step != 0);
+            break;
+        }
+        is_moved = 1;
+    }
+    return is_moved;
+}
+
 template <int G>
 __global__ void __launch_bounds__(256) k_newton_group(const double* __restrict__ vx,
                                                       const double* __restrict__ vy,
@@ -264,105 +367,235 @@ __global__ void __launch_bounds__(256) k_newton_group(const double* __restrict__
         const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
         StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
         double pos[3] = {vx[S.v], vy[S.v], vz[S.v]};
-        int is_moved = 0;
-        double old_energy = 0.0, new_energy = 0.0, J[3], H[9];
-        for (int step = 0; step < max_step; ++step) {
-            // NewtonsUpdate: E, J, H summed over the tets in caller order
-            double e = 0.0;
-            for (int k = 0; k < 3; ++k) J[k] = 0.0;
-            for (int k = 0; k < 9; ++k) H[k] = 0.0;
-            for (int c0 = 0; c0 < nt; c0 += G) {
-                const int cnt = min(G, nt - c0);
-                double te = 0.0, tJ[3] = {0.0, 0.0, 0.0}, tH[9];
-                for (int k = 0; k < 9; ++k) tH[k] = 0.0;
-                if (gl < cnt) {
-                    int4 tv = __ldg(S.tets + c0 + gl);
-                    int start = (tv.x == S.v) ? 0 : (tv.y == S.v) ? 1 : (tv.z == S.v) ? 2
-                              : (tv.w == S.v) ? 3 : 0;
-                    double T[12];
-                    gather_tet(S, tv, start, pos, T);
-                    te = amips_energy(T);
-                    amips_egh(T, tJ, tH);
-                }
-                for (int t = 0; t < cnt; ++t) {
-                    e += __shfl_sync(gm, te, t, G);
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) J[k] += __shfl_sync(gm, tJ[k], t, G);
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) H[k] += __shfl_sync(gm, tH[k], t, G);
-                }
-            }
-            if (isinf(e)) e = kMaxEnergy;
-            old_energy = e;
-            bool ok = !isnan(e) && !(e <= 0.0);
-            for (int k = 0; k < 3; ++k) ok = ok && isfinite(J[k]);
-            for (int k = 0; k < 9; ++k) ok = ok && isfinite(H[k]);
-            if (!ok) break;
-            double old_pf[3] = {pos[0], pos[1], pos[2]};
-            double X0[3] = {pos[0], pos[1], pos[2]};
-            double a = 1.0;
-            bool step_taken = false;
-            for (int it = 0; it < max_it; ++it) {
-                double rhs[3], X[3];
-                for (int i = 0; i < 3; ++i)
-                    rhs[i] = ((H[3 * i] * X0[0] + H[3 * i + 1] * X0[1]) + H[3 * i + 2] * X0[2]) -
-                             a * J[i];
-                qr_solve3(H, rhs, X);
-                if (!isfinite(X[0]) || !isfinite(X[1]) || !isfinite(X[2])) {
-                    a /= 2.0;
-                    continue;
-                }
-                pos[0] = X[0];
-                pos[1] = X[1];
-                pos[2] = X[2];
-                bool flip = false;
-                for (int c0 = gl; c0 < nt; c0 += G) {
-                    double T[12];
-                    gather_tet(S, __ldg(S.tets + c0), 0, pos, T);
-                    flip = flip || (orient3d(T, T + 3, T + 6, T + 9) != 1);
-                }
-                if (__any_sync(gm, flip)) {
-                    pos[0] = old_pf[0];
-                    pos[1] = old_pf[1];
-                    pos[2] = old_pf[2];
-                    a /= 2.0;
-                    continue;
-                }
-                double s = 0.0;
-                for (int c0 = 0; c0 < nt; c0 += G) {
-                    const int cnt = min(G, nt - c0);
-                    double te = 0.0;
-                    if (gl < cnt) {
-                        double T[12];
-                        gather_tet(S, __ldg(S.tets + c0 + gl), 0, pos, T);
-                        te = amips_energy(T);
-                    }
-                    for (int t = 0; t < cnt; ++t) s += __shfl_sync(gm, te, t, G);
-                }
-                if (isinf(s) || isnan(s) || s <= 0.0 || s > kMaxEnergy) s = kMaxEnergy;
-                new_energy = s;
-                if (new_energy >= old_energy || isinf(new_energy) || isnan(new_energy)) {
-                    pos[0] = old_pf[0];
-                    pos[1] = old_pf[1];
-                    pos[2] = old_pf[2];
-                    a /= 2.0;
-                    continue;
-                }
-                step_taken = true;
-                break;
-            }
-            if (fabs(new_energy - old_energy) < 1e-5) step_taken = false;
-            if (!step_taken) {
-                is_moved = (step != 0);
-                break;
-            }
-            is_moved = 1;
-        }
+        const int is_moved = newton_group_star<G>(S, pos, max_step, max_it, gl, gm);
         if (gl == 0) {
             out[3 * sid] = pos[0];
             out[3 * sid + 1] = pos[1];
             out[3 * sid + 2] = pos[2];
             moved[sid] = (uint8_t)is_moved;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Smoothing pass (VertexSmoother.cpp:114-210 and :244-450), G lanes per star.
+// ---------------------------------------------------------------------------
+// True when every tet of the star is POSITIVE with the centre at pos.
+template <int G>
+__device__ __forceinline__ bool star_positive(const StarView& S, const double* pos, int gl,
+                                              unsigned gm) {
+    bool bad = false;
+    for (int c0 = gl; c0 < S.nt; c0 += G) {
+        double T[12];
+        gather_tet(S, __ldg(S.tets + c0), 0, pos, T);
+        bad = bad || (orient3d(T, T + 3, T + 6, T + 9) != 1);
+    }
+    return !__any_sync(gm, bad);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_smooth_stage1(
+    const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ vz,
+    const int32_t* __restrict__ star_off, const int4* __restrict__ tets,
+    const int32_t* __restrict__ centers, const uint8_t* __restrict__ kinds, int32_t nstars,
+    int max_step, int max_it, double* __restrict__ out, double* __restrict__ pnew,
+    uint8_t* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const unsigned gm = group_mask<G>(lane);
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t sid = gid; sid < nstars; sid += ngroups) {
+        const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        const double p0[3] = {vx[S.v], vy[S.v], vz[S.v]};
+        double pos[3] = {p0[0], p0[1], p0[2]};
+        const uint8_t kind = kinds ? kinds[sid] : (uint8_t)TW_STAR_INTERIOR;
+        const bool surface = (kind == TW_STAR_SURFACE || kind == TW_STAR_BOUNDARY);
+        uint8_t st;
+        if (!star_positive<G>(S, p0, gl, gm)) {
+            st = TW_SMOOTH_INVALID;
+        } else if (!newton_group_star<G>(S, pos, max_step, max_it, gl, gm)) {
+            st = TW_SMOOTH_NOT_MOVED;
+        } else {
+            st = surface ? kSmoothPendingProject : (uint8_t)TW_SMOOTH_MOVED;
+        }
+        if (gl == 0) {
+            const bool moved = (st == TW_SMOOTH_MOVED);
+            out[3 * sid] = moved ? pos[0] : p0[0];
+            out[3 * sid + 1] = moved ? pos[1] : p0[1];
+            out[3 * sid + 2] = moved ? pos[2] : p0[2];
+            pnew[3 * sid] = pos[0];
+            pnew[3 * sid + 1] = pos[1];
+            pnew[3 * sid + 2] = pos[2];
+            status[sid] = st;
+        }
+    }
+}
+
+__device__ __forceinline__ int4 tet_at(const StarView& S, int32_t i) { return __ldg(S.tets + i); }
+__device__ __forceinline__ int tet_vertex(int4 tv, int j) {
+    return j == 0 ? tv.x : j == 1 ? tv.y : j == 2 ? tv.z : tv.w;
+}
+
+// The surface face of tet tv opposite its j-th vertex, as a sorted triple.
+__device__ __forceinline__ void face_key(int4 tv, int j, int32_t* k) {
+    int32_t id[4] = {tv.x, tv.y, tv.z, tv.w};
+    int32_t a = id[(j + 1) & 3], b = id[(j + 2) & 3], c = id[(j + 3) & 3];
+    int32_t lo = min(a, min(b, c)), hi = max(a, max(b, c));
+    k[0] = lo;
+    k[1] = (int32_t)((int64_t)a + b + c - lo - hi);
+    k[2] = hi;
+}
+
+// calTetQuality_AMIPS for a tet already known to be POSITIVE.
+__device__ __forceinline__ double positive_tet_quality(const double* T) {
+    return quality_from(1, amips_energy(T));
+}
+
+// True when face j of the star's tet c0 is a surface face through the
+// centre whose sorted triple does not occur at an earlier (tet, face) of the
+// star; writes the triple.
+__device__ __forceinline__ bool first_surface_face(const StarView& S, const uint8_t* ff,
+                                                   int32_t c0, int4 tv, uint8_t fl, int j,
+                                                   int32_t* key) {
+    if (tet_vertex(tv, j) == S.v || !((fl >> j) & 1)) return false;
+    face_key(tv, j, key);
+    for (int32_t i2 = 0; i2 <= c0; ++i2) {
+        int4 t2 = tet_at(S, i2);
+        uint8_t f2 = __ldg(ff + i2);
+        for (int j2 = 0; j2 < 4; ++j2) {
+            if (i2 == c0 && j2 >= j) return true;
+            if (tet_vertex(t2, j2) == S.v || !((f2 >> j2) & 1)) continue;
+            int32_t k2[3];
+            face_key(t2, j2, k2);
+            if (k2[0] == key[0] && k2[1] == key[1] && k2[2] == key[2]) return false;
+        }
+    }
+    return true;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_smooth_stage2(
+    const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ vz,
+    const int32_t* __restrict__ star_off, const int4* __restrict__ tets,
+    const uint8_t* __restrict__ face_flags, const int32_t* __restrict__ centers, int32_t nstars,
+    const double* __restrict__ pnew, uint8_t* __restrict__ status, double* __restrict__ faces,
+    unsigned long long* __restrict__ face_count, int64_t face_cap,
+    int32_t* __restrict__ face_base, int32_t* __restrict__ face_cnt,
+    unsigned long long* __restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const unsigned gm = group_mask<G>(lane);
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t sid = gid; sid < nstars; sid += ngroups) {
+        if (status[sid] != kSmoothPendingProject) continue;  // uniform within the group
+        const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        const double p0[3] = {vx[S.v], vy[S.v], vz[S.v]};
+        const double p[3] = {pnew[3 * sid], pnew[3 * sid + 1], pnew[3 * sid + 2]};
+        // isFlip at the projected position (:374-378)
+        if (!star_positive<G>(S, p, gl, gm)) {
+            if (gl == 0) status[sid] = TW_SMOOTH_REJECT_FLIP;
+            continue;
+        }
+        // max calTetQuality before and after (:379-386); max is exact in any order
+        double old_max = 0.0, new_max = 0.0;
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            double T[12];
+            int4 tv = tet_at(S, c0);
+            gather_tet(S, tv, 0, p0, T);
+            old_max = fmax(old_max, positive_tet_quality(T));
+            gather_tet(S, tv, 0, p, T);
+            new_max = fmax(new_max, positive_tet_quality(T));
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            old_max = fmax(old_max, __shfl_xor_sync(gm, old_max, o, G));
+            new_max = fmax(new_max, __shfl_xor_sync(gm, new_max, o, G));
+        }
+        if (!(new_max < old_max)) {
+            if (gl == 0) status[sid] = TW_SMOOTH_REJECT_QUALITY;
+            continue;
+        }
+        // one-ring surface faces (:314-326): the first occurrence of each
+        // sorted triple; counted, then written at one reservation per star
+        const uint8_t* ff = face_flags + b;
+        int nmine = 0;
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            int4 tv = tet_at(S, c0);
+            uint8_t fl = __ldg(ff + c0);
+            int32_t key[3];
+            for (int j = 0; j < 4; ++j) nmine += first_surface_face(S, ff, c0, tv, fl, j, key);
+        }
+        int incl = nmine;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            int v = __shfl_up_sync(gm, incl, o, G);
+            if (gl >= o) incl += v;
+        }
+        const int total = __shfl_sync(gm, incl, G - 1, G);
+        unsigned long long base = 0;
+        if (gl == 0 && total > 0) base = atomicAdd(face_count, (unsigned long long)total);
+        base = __shfl_sync(gm, base, 0, G);
+        if (total > 0 && base + (unsigned long long)total > (unsigned long long)face_cap) {
+            if (gl == 0) {
+                atomicOr(counters + kCntError, 8ULL);
+                status[sid] = TW_SMOOTH_INVALID;
+            }
+            continue;
+        }
+        int64_t w = (int64_t)base + (incl - nmine);
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            int4 tv = tet_at(S, c0);
+            uint8_t fl = __ldg(ff + c0);
+            for (int j = 0; j < 4; ++j) {
+                int32_t key[3];
+                if (!first_surface_face(S, ff, c0, tv, fl, j, key)) continue;
+                // the face from the centre onward in the cyclic order of its
+                // sorted triple (:427-432)
+                const int kv = (key[0] == S.v) ? 0 : (key[1] == S.v) ? 1 : 2;
+                const int32_t v1 = key[(kv + 1) % 3], v2 = key[(kv + 2) % 3];
+                double* f = faces + 9 * w;
+                f[0] = p[0];
+                f[1] = p[1];
+                f[2] = p[2];
+                f[3] = __ldg(vx + v1);
+                f[4] = __ldg(vy + v1);
+                f[5] = __ldg(vz + v1);
+                f[6] = __ldg(vx + v2);
+                f[7] = __ldg(vy + v2);
+                f[8] = __ldg(vz + v2);
+                ++w;
+            }
+        }
+        if (gl == 0) {
+            face_base[sid] = (int32_t)base;
+            face_cnt[sid] = total;
+            status[sid] = kSmoothPendingEnvelope;
+        }
+    }
+}
+
+__global__ void k_smooth_finalize(int32_t nstars, const int32_t* __restrict__ face_base,
+                                  const int32_t* __restrict__ face_cnt,
+                                  const uint8_t* __restrict__ face_out,
+                                  const double* __restrict__ pnew, double* __restrict__ out,
+                                  uint8_t* __restrict__ status) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nstars; i += stride) {
+        if (status[i] != kSmoothPendingEnvelope) continue;
+        bool outside = false;
+        const int32_t b = face_base[i], n = face_cnt[i];
+        for (int32_t k = 0; k < n && !outside; ++k) outside = face_out[b + k] != 0;
+        if (outside) {
+            status[i] = TW_SMOOTH_REJECT_ENVELOPE;
+        } else {
+            out[3 * i] = pnew[3 * i];
+            out[3 * i + 1] = pnew[3 * i + 1];
+            out[3 * i + 2] = pnew[3 * i + 2];
+            status[i] = TW_SMOOTH_MOVED;
         }
     }
 }
@@ -408,6 +641,70 @@ void launch_newton_stars_shape(int shape, const double* vx, const double* vy, co
     else
         k_newton_group<32><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
                                                      max_step, max_it, out, moved);
+}
+
+// Smoothing kernels use the Newton shape's group size; shape 0 (one thread
+// per star) runs them with 8 lanes.
+static int smooth_group(int shape, int* block) {
+    if (shape < 0 || shape >= newton_num_shapes()) shape = 5;
+    NewtonShape sh = kNewtonShapes[shape];
+    if (sh.group == 1) sh = NewtonShape{8, 128};
+    *block = sh.block;
+    return sh.group;
+}
+
+void launch_smooth_stage1(int shape, const double* vx, const double* vy, const double* vz,
+                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
+                          const uint8_t* kinds, int32_t nstars, int max_step, int max_it,
+                          double* out, double* pnew, uint8_t* status, cudaStream_t s) {
+    if (nstars <= 0) return;
+    int block;
+    const int G = smooth_group(shape, &block);
+    const int grid = grid_for((int64_t)nstars * G, block, 2048 / block);
+    const int4* t4 = reinterpret_cast<const int4*>(tets);
+    if (G == 8)
+        k_smooth_stage1<8><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
+                                                  max_step, max_it, out, pnew, status);
+    else if (G == 16)
+        k_smooth_stage1<16><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
+                                                   max_step, max_it, out, pnew, status);
+    else
+        k_smooth_stage1<32><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
+                                                   max_step, max_it, out, pnew, status);
+}
+
+void launch_smooth_stage2(int shape, const double* vx, const double* vy, const double* vz,
+                          const int32_t* star_off, const int32_t* tets, const uint8_t* face_flags,
+                          const int32_t* centers, int32_t nstars, const double* pnew,
+                          uint8_t* status, double* faces, unsigned long long* face_count,
+                          int64_t face_cap, int32_t* face_base, int32_t* face_cnt,
+                          unsigned long long* counters, cudaStream_t s) {
+    if (nstars <= 0) return;
+    int block;
+    const int G = smooth_group(shape, &block);
+    const int grid = grid_for((int64_t)nstars * G, block, 2048 / block);
+    const int4* t4 = reinterpret_cast<const int4*>(tets);
+    if (G == 8)
+        k_smooth_stage2<8><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
+                                                  nstars, pnew, status, faces, face_count, face_cap,
+                                                  face_base, face_cnt, counters);
+    else if (G == 16)
+        k_smooth_stage2<16><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
+                                                   nstars, pnew, status, faces, face_count, face_cap,
+                                                   face_base, face_cnt, counters);
+    else
+        k_smooth_stage2<32><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
+                                                   nstars, pnew, status, faces, face_count, face_cap,
+                                                   face_base, face_cnt, counters);
+}
+
+void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
+                            const uint8_t* face_out, const double* pnew, double* out,
+                            uint8_t* status, cudaStream_t s) {
+    if (nstars <= 0) return;
+    const int block = 256;
+    k_smooth_finalize<<<grid_for(nstars, block, 8), block, 0, s>>>(nstars, face_base, face_cnt,
+                                                                   face_out, pnew, out, status);
 }
 
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,

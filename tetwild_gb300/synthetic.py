@@ -16,6 +16,10 @@ distributions instead:
 * ``star_batch``: independent one-ring stars (a centre vertex and a fan of
   tets to a jittered convex polyhedron around it), tets per star
   Poisson(24) clamped to [4, 96].
+* ``surface_star_batch``: independent stars of surface vertices: a centre
+  near a surface, a ring of points in its tangent plane, and an apex above
+  and below, so every ring triangle through the centre is a surface face of
+  two tets; tets per star Poisson(24) clamped to [6, 96].
 """
 from __future__ import annotations
 
@@ -219,30 +223,139 @@ def star_batch(nstars: int, seed: int = 0, mean_tets: float = 24.0, lo: int = 4,
     ntet = np.clip(ntet, lo, hi)
     if centres is None:
         centres = rng.random((nstars, 3))
-    hull_cache = {}
-    xyz, off, tets, cen = [], [0], [], []
-    nv = 0
-    for s in range(nstars):
-        k = int(ntet[s]) // 2 + 2
-        if k not in hull_cache:
-            d = _fib_dirs(k)
-            hull_cache[k] = (d, ConvexHull(d).simplices.astype(np.int32))
-        d, simp = hull_cache[k]
-        R = random_rotations(rng, 1)[0]
-        ring = centres[s] + radius * (d @ R.T)
-        c = centres[s]
-        pts = np.vstack([c[None], ring])
+    centres = np.asarray(centres, np.float64)
+    k = ntet // 2 + 2
+    nv_star = k + 1
+    voff = np.concatenate([[0], np.cumsum(nv_star)])
+    toff = np.concatenate([[0], np.cumsum(2 * k - 4)]).astype(np.int32)
+    xyz = np.empty((int(voff[-1]), 3))
+    tets = np.empty((int(toff[-1]), 4), np.int32)
+    for kk in np.unique(k):
+        sel = np.nonzero(k == kk)[0]
+        m = len(sel)
+        d = _fib_dirs(int(kk))
+        simp = ConvexHull(d).simplices.astype(np.int32)  # [2kk-4, 3]
+        R = random_rotations(rng, m)
+        ring = centres[sel, None, :] + radius * np.einsum("kj,mij->mki", d, R)
+        c = centres[sel]
+        # orient (centre, a, b, c) POSITIVE on the unjittered geometry
+        pa, pb, pc = ring[:, simp[:, 0]], ring[:, simp[:, 1]], ring[:, simp[:, 2]]
+        det = np.einsum("mfi,mfi->mf", pa - c[:, None], np.cross(pb - c[:, None], pc - c[:, None]))
+        pts = np.concatenate([c[:, None], ring], 1)
         pts = pts + rng.normal(0.0, jitter_rel * radius, pts.shape)
-        ci = nv
-        for f in simp:
-            a, b, cc = (ci + 1 + int(f[0]), ci + 1 + int(f[1]), ci + 1 + int(f[2]))
-            # orient (centre, a, b, cc) POSITIVE on the unjittered geometry
-            p0, pa, pb, pc = c, ring[f[0]], ring[f[1]], ring[f[2]]
-            det = np.dot(pa - p0, np.cross(pb - p0, pc - p0))
-            tets.append((ci, a, b, cc) if det > 0 else (ci, a, cc, b))
-        xyz.append(pts)
-        nv += len(pts)
-        off.append(len(tets))
-        cen.append(ci)
-    return (np.vstack(xyz), np.asarray(off, np.int32), np.asarray(tets, np.int32),
-            np.asarray(cen, np.int32))
+        base = voff[sel]
+        for j in range(kk + 1):
+            xyz[base + j] = pts[:, j]
+        a = base[:, None] + 1 + simp[None, :, 0]
+        b = base[:, None] + 1 + simp[None, :, 1]
+        cc = base[:, None] + 1 + simp[None, :, 2]
+        pos = det > 0
+        t = np.stack([np.broadcast_to(base[:, None], a.shape), a, np.where(pos, b, cc),
+                      np.where(pos, cc, b)], -1)
+        idx = toff[sel][:, None] + np.arange(len(simp))[None, :]
+        tets[idx.reshape(-1)] = t.reshape(-1, 4)
+    return xyz, toff, tets, voff[:-1].astype(np.int32)
+
+
+def surface_star_batch(V: np.ndarray, F: np.ndarray, nstars: int, eps: float, seed: int = 0,
+                       mean_tets: float = 24.0, lo: int = 6, hi: int = 96,
+                       radius: float = 0.01, ring_off: float = 0.8, centre_jitter: float = 0.25):
+    """Independent surface stars on (V, F), sharing no vertices.
+
+    Star i: a point c on a random facet (uniform by area), the facet's unit normal n and a
+    tangent frame; k = tets/2 ring points at angles 2 pi j / k + U(-0.3, 0.3) * 2 pi / k and
+    distance radius * U(0.7, 1.3) in the tangent plane, each offset along n by
+    U(-ring_off, ring_off) * eps; apexes c +- 0.8 radius n.  Tets (c, r_j, r_j+1, top) and
+    (c, r_j+1, r_j, bottom), oriented POSITIVE on the unperturbed geometry; the face opposite the
+    apex (vertex 3) is flagged as a surface face.  Finally the centre moves by
+    N(0, centre_jitter * radius) in the tangent plane and U(-0.5, 0.5) * eps along n.
+    Returns (xyz [nv,3], star_off [ns+1], tets [nt,4], face_flags [nt] uint8, centers [ns]).
+    """
+    rng = np.random.default_rng(seed)
+    ntet = np.clip(rng.poisson(mean_tets, nstars), lo, hi)
+    ntet = np.clip(ntet + ntet % 2, lo, hi)
+    A, B, C = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    nrm = np.cross(B - A, C - A)
+    area = np.linalg.norm(nrm, axis=1)
+    cdf = np.cumsum(area)
+    cdf /= cdf[-1]
+    f = np.minimum(np.searchsorted(cdf, rng.random(nstars)), len(F) - 1)
+    u, v = rng.random(nstars), rng.random(nstars)
+    flip = u + v > 1
+    u[flip], v[flip] = 1 - u[flip], 1 - v[flip]
+    c = A[f] + u[:, None] * (B[f] - A[f]) + v[:, None] * (C[f] - A[f])
+    n = nrm[f] / area[f, None]
+    t1 = np.cross(n, np.where(np.abs(n[:, :1]) < 0.9, [[1.0, 0.0, 0.0]], [[0.0, 1.0, 0.0]]))
+    t1 /= np.linalg.norm(t1, axis=1, keepdims=True)
+    t2 = np.cross(n, t1)
+    k = ntet // 2
+    nv_star = k + 3
+    voff = np.concatenate([[0], np.cumsum(nv_star)])
+    toff = np.concatenate([[0], np.cumsum(2 * k)]).astype(np.int32)
+    xyz = np.empty((int(voff[-1]), 3))
+    tets = np.empty((int(toff[-1]), 4), np.int32)
+    for kk in np.unique(k):
+        sel = np.nonzero(k == kk)[0]
+        m = len(sel)
+        ang = 2 * math.pi * (np.arange(kk)[None, :] + rng.uniform(-0.3, 0.3, (m, kk))) / kk
+        rad = radius * rng.uniform(0.7, 1.3, (m, kk))
+        off = rng.uniform(-ring_off, ring_off, (m, kk)) * eps
+        cs, t1s, t2s, ns = c[sel, None], t1[sel, None], t2[sel, None], n[sel, None]
+        ring = cs + rad[..., None] * (np.cos(ang)[..., None] * t1s + np.sin(ang)[..., None] * t2s)
+        ring = ring + off[..., None] * ns
+        top = c[sel] + 0.8 * radius * n[sel]
+        bot = c[sel] - 0.8 * radius * n[sel]
+        cj = (rng.normal(0.0, centre_jitter * radius, (m, 2))[:, :1] * t1[sel]
+              + rng.normal(0.0, centre_jitter * radius, (m, 1)) * t2[sel]
+              + rng.uniform(-0.5, 0.5, (m, 1)) * eps * n[sel])
+        base = voff[sel]
+        xyz[base] = c[sel] + cj
+        for j in range(kk):
+            xyz[base + 1 + j] = ring[:, j]
+        xyz[base + 1 + kk] = top
+        xyz[base + 2 + kk] = bot
+        ci = base
+        rj = base[:, None] + 1 + np.arange(kk)[None, :]
+        rj1 = base[:, None] + 1 + (np.arange(kk)[None, :] + 1) % kk
+        tp = base + 1 + kk
+        bt = base + 2 + kk
+        tb = toff[sel]
+        for j in range(kk):
+            tets[tb + 2 * j] = np.stack([ci, rj[:, j], rj1[:, j], tp], 1)
+            tets[tb + 2 * j + 1] = np.stack([ci, rj1[:, j], rj[:, j], bt], 1)
+    ff = np.full(len(tets), 8, np.uint8)  # bit 3: the face opposite the apex
+    cen = voff[:-1].astype(np.int32)
+    return xyz, toff, tets, ff, cen
+
+
+def mixed_star_batch(V: np.ndarray, F: np.ndarray, nstars: int, eps: float, seed: int = 0,
+                     surface_fraction: float = 0.5, mean_tets: float = 24.0):
+    """Interior stars (``star_batch``, centres on the surface's bounding box) followed by
+    surface stars (``surface_star_batch``) in one vertex array.  Returns (xyz, star_off, tets,
+    face_flags, centers, kinds) with kinds 0 (interior) / 1 (surface)."""
+    ns_s = int(round(nstars * surface_fraction))
+    ns_i = nstars - ns_s
+    lo, hi = V.min(0), V.max(0)
+    rng = np.random.default_rng(seed + 7)
+    parts = []
+    if ns_i:
+        cen_i = lo + (hi - lo) * rng.random((ns_i, 3))
+        xi, oi, ti, ci = star_batch(ns_i, seed=seed, mean_tets=mean_tets, centres=cen_i)
+        parts.append((xi, oi, ti, np.zeros(len(ti), np.uint8), ci, np.zeros(ns_i, np.uint8)))
+    if ns_s:
+        xs, os_, ts, fs, cs = surface_star_batch(V, F, ns_s, eps, seed=seed + 1, mean_tets=mean_tets)
+        parts.append((xs, os_, ts, fs, cs, np.ones(ns_s, np.uint8)))
+    xyz, off, tets, ff, cen, kinds = [], [0], [], [], [], []
+    nv = 0
+    nt = 0
+    for x, o, t, f_, c_, k_ in parts:
+        xyz.append(x)
+        tets.append(t + nv)
+        ff.append(f_)
+        cen.append(c_ + nv)
+        kinds.append(k_)
+        off.extend((o[1:] + nt).tolist())
+        nv += len(x)
+        nt += len(t)
+    return (np.vstack(xyz), np.asarray(off, np.int32), np.vstack(tets).astype(np.int32),
+            np.concatenate(ff), np.concatenate(cen).astype(np.int32), np.concatenate(kinds))
