@@ -743,6 +743,8 @@ int tw_nearest_points(tw_ctx* c, const double* P, int64_t n, int which, double* 
 }
 
 // ---- smoothing pass ----------------------------------------------------------------
+}  // extern "C"
+
 namespace {
 // Scratch of a smoothing pass (slot 8): per star the Newton / projected
 // position, face range and state; per possible face (3 per tet) its nine
@@ -796,6 +798,8 @@ void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uin
                            c->stream);
 }
 }  // namespace
+
+extern "C" {
 
 int tw_smooth_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
                            const uint8_t* face_flags, const int32_t* centers, const uint8_t* kinds,
@@ -906,6 +910,8 @@ int tw_set_newton_shape(tw_ctx* c, int shape) {
     return TW_OK;
 }
 
+}  // extern "C"
+
 namespace {
 // Times run(shape) for every launch shape (one untimed launch, then the best
 // of two timed ones, CUDA events on the context stream), keeps the fastest
@@ -937,6 +943,8 @@ int autotune_shapes(tw_ctx* c, const char* where, int* best_shape, float* ms_per
     return sync_status(c, where);
 }
 }  // namespace
+
+extern "C" {
 
 int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
                               const int32_t* centers, int32_t nstars, double* out, uint8_t* moved,
