@@ -49,6 +49,7 @@ extern "C" {
 #define TW_ERR_NO_MESH (-5)
 #define TW_ERR_TIMEOUT (-6)
 #define TW_ERR_TOO_LARGE (-7)    /* request exceeds a fixed capacity (tw_amips_soa_noalloc) */
+#define TW_BUSY 2                /* serving: not admitted now (memory budget), retry later  */
 
 /* AMIPS output modes */
 #define TW_ENERGY_RAW 0          /* comformalAMIPSEnergy_new value            */
@@ -278,6 +279,83 @@ TW_API int tw_graph_destroy(void* graph_exec);
 /* ---- pinned host memory for fast copies --------------------------------------- */
 TW_API int tw_host_alloc(size_t bytes, void** out);
 TW_API int tw_host_free(void* p);
+
+/* ---- serving loop ----------------------------------------------------------------
+ * No counterpart in the reference (TetWild runs one job per process).  A
+ * server holds many meshing jobs resident in HBM (their input and boundary
+ * surfaces as LBVHs, their vertex arrays) and serves their query batches as
+ * they arrive: a dispatcher thread takes the waiting requests, joins point
+ * and face requests of any jobs into one launch (a segment per request), and
+ * runs each batch on one of `lanes` CUDA streams, so batches overlap on the
+ * device and a request that arrives while others run joins the next batch
+ * as soon as a lane is free.  Results are identical to the single-job
+ * entry points on the same inputs (alone or in any mix).
+ *
+ * Jobs are admitted against the HBM budget: tw_server_job_open returns
+ * TW_BUSY when the job's estimated footprint does not fit beside the open
+ * jobs and the lanes' scratch; the caller retries after a job closes.
+ * Request buffers are host (or device-accessible) memory that must stay
+ * valid until tw_server_wait returns for the ticket.                        */
+typedef struct tw_server tw_server;
+
+#define TW_REQ_POINTS 0   /* isPointOutEnvelop: in0 = P[n][3], out0 = u8[n]             */
+#define TW_REQ_FACES 1    /* isFaceOutEnvelop: in0 = tris[n][9], out0 = u8[n]           */
+#define TW_REQ_AMIPS 2    /* E/J/H: in0 = T_soa[12][n]; out0 = E, out1 = J, out2 = H,
+                             out3 = flip (any may be NULL); flags TW_REQ_RAW = raw energy  */
+#define TW_REQ_SMOOTH 3   /* smoothing pass over n stars of the job's resident mesh:
+                             in0 = star_off[n+1], in1 = tets, in2 = face_flags, in3 =
+                             centers, in4 = kinds; out0 = out[n][3], out1 = status[n];
+                             flags TW_REQ_APPLY writes accepted positions into the mesh   */
+#define TW_REQ_RAW 1
+#define TW_REQ_APPLY 2
+
+typedef struct tw_request {
+    int32_t kind;
+    int32_t flags;
+    int64_t n;
+    const void* in0;
+    const void* in1;
+    const void* in2;
+    const void* in3;
+    const void* in4;
+    void* out0;
+    void* out1;
+    void* out2;
+    void* out3;
+} tw_request;
+
+typedef struct tw_server_stats {
+    uint64_t jobs_open;
+    uint64_t bytes_used;       /* jobs + lanes */
+    uint64_t budget;
+    uint64_t requests_done;
+    uint64_t batches;
+    uint64_t queries_done;
+    uint64_t max_requests_per_batch;
+} tw_server_stats;
+
+TW_API int tw_server_create(int device, size_t hbm_budget, int lanes, tw_server** out);
+TW_API int tw_server_destroy(tw_server* srv);
+TW_API const char* tw_server_last_error(tw_server* srv);
+/* Precision mode, Newton caps and launch shape for every request.          */
+TW_API int tw_server_set_params(tw_server* srv, int precision, int newton_max_step,
+                                int newton_max_it, int newton_shape);
+TW_API int tw_server_job_open(tw_server* srv, const double* V, int32_t nv, const int32_t* F,
+                              int32_t nf, double eps_2, double sampling_dist, int32_t* job);
+TW_API int tw_server_job_boundary(tw_server* srv, int32_t job, const double* V, int32_t nv,
+                                  const int32_t* F, int32_t nf);
+/* Resident vertex positions for TW_REQ_SMOOTH (waits for the job's requests
+ * in flight, at most timeout_s).                                           */
+TW_API int tw_server_job_mesh(tw_server* srv, int32_t job, const double* xyz, int32_t nv,
+                              double timeout_s);
+TW_API int tw_server_job_read_mesh(tw_server* srv, int32_t job, double* xyz, double timeout_s);
+/* Waits (at most timeout_s) for the job's requests, then frees its memory. */
+TW_API int tw_server_job_close(tw_server* srv, int32_t job, double timeout_s);
+TW_API int tw_server_submit(tw_server* srv, int32_t job, const tw_request* req, uint64_t* ticket);
+/* Waits at most timeout_s for the request; returns its status (TW_ERR_TIMEOUT
+ * if not done yet: wait again).  latency_ms: submit to completion.          */
+TW_API int tw_server_wait(tw_server* srv, uint64_t ticket, double timeout_s, double* latency_ms);
+TW_API int tw_server_get_stats(tw_server* srv, tw_server_stats* out);
 
 /* ---- device self-test -----------------------------------------------------------
  * No counterpart in the reference.  Checks, on `samples` pseudo-random bit

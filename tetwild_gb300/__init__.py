@@ -34,6 +34,13 @@ TW_ENERGY_RAW = 0
 TW_ENERGY_QUALITY = 1
 TW_SURFACE_INPUT = 0
 TW_SURFACE_BOUNDARY = 1
+TW_BUSY = 2
+TW_REQ_POINTS = 0
+TW_REQ_FACES = 1
+TW_REQ_AMIPS = 2
+TW_REQ_SMOOTH = 3
+TW_REQ_RAW = 1
+TW_REQ_APPLY = 2
 TW_STAR_INTERIOR = 0
 TW_STAR_SURFACE = 1
 TW_STAR_BOUNDARY = 2
@@ -77,6 +84,19 @@ class TwStats(ctypes.Structure):
 
 
 # name -> argtypes (restype int unless noted)
+class TwRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("flags", ctypes.c_int32), ("n", ctypes.c_int64),
+                ("in0", ctypes.c_void_p), ("in1", ctypes.c_void_p), ("in2", ctypes.c_void_p),
+                ("in3", ctypes.c_void_p), ("in4", ctypes.c_void_p), ("out0", ctypes.c_void_p),
+                ("out1", ctypes.c_void_p), ("out2", ctypes.c_void_p), ("out3", ctypes.c_void_p)]
+
+
+class TwServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("jobs_open", "bytes_used", "budget", "requests_done",
+                                               "batches", "queries_done",
+                                               "max_requests_per_batch")]
+
+
 _SIGS = {
     "tw_set_precision": [_P, _I],
     "tw_get_stats": [_P, ctypes.POINTER(TwStats)],
@@ -120,6 +140,18 @@ _SIGS = {
     "tw_host_free": [_P],
     "tw_probe_peaks": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D)],
     "tw_self_test": [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "tw_server_create": [_I, _SZ, _I, ctypes.POINTER(_P)],
+    "tw_server_destroy": [_P],
+    "tw_server_last_error": [_P],
+    "tw_server_set_params": [_P, _I, _I, _I, _I],
+    "tw_server_job_open": [_P, _P, _I32, _P, _I32, _D, _D, ctypes.POINTER(_I32)],
+    "tw_server_job_boundary": [_P, _I32, _P, _I32, _P, _I32],
+    "tw_server_job_mesh": [_P, _I32, _P, _I32, _D],
+    "tw_server_job_read_mesh": [_P, _I32, _P, _D],
+    "tw_server_job_close": [_P, _I32, _D],
+    "tw_server_submit": [_P, _I32, ctypes.POINTER(TwRequest), ctypes.POINTER(ctypes.c_uint64)],
+    "tw_server_wait": [_P, ctypes.c_uint64, _D, ctypes.POINTER(_D)],
+    "tw_server_get_stats": [_P, ctypes.POINTER(TwServerStats)],
 }
 EXPORTED_SYMBOLS = tuple(_SIGS)
 
@@ -138,7 +170,7 @@ def load_library() -> ctypes.CDLL:
     for name, args in _SIGS.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name == "tw_last_error" else _I
+        fn.restype = ctypes.c_char_p if name.endswith("last_error") else _I
     _LIB = lib
     return lib
 
@@ -491,6 +523,132 @@ class LocalOperations:
 
     def isFaceOutEnvelop(self, tri) -> bool:
         return bool(self.ctx.envelope_faces(np.asarray(tri).reshape(1, 9))[0])
+
+
+class Server:
+    """The serving loop (tw_server_*): many jobs resident in HBM, their query batches joined
+    across jobs as they arrive and run on ``lanes`` CUDA streams."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, lanes: int = 4):
+        self.lib = load_library()
+        h = _P()
+        st = self.lib.tw_server_create(device, hbm_budget_bytes, lanes, ctypes.byref(h))
+        if st != TW_OK:
+            raise TetWildGpuError(st, "tw_server_create failed")
+        self.h = h
+        self._keep = {}
+
+    def _check(self, st, allow=(TW_OK,)):
+        if st not in allow:
+            msg = self.lib.tw_server_last_error(self.h)
+            raise TetWildGpuError(st, msg.decode() if msg else "")
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tw_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_params(self, precision=TW_PRECISION_FP32_CERTIFIED, newton_max_step=15,
+                   newton_max_it=20, newton_shape=5):
+        self._check(self.lib.tw_server_set_params(self.h, precision, newton_max_step,
+                                                  newton_max_it, newton_shape))
+
+    def job_open(self, V, F, eps_2, sampling_dist):
+        """Returns the job id, or None when the job does not fit in the budget now (TW_BUSY)."""
+        Vv = _c(V, np.float64).reshape(-1, 3)
+        Ff = _c(F, np.int32).reshape(-1, 3)
+        j = _I32()
+        st = self._check(self.lib.tw_server_job_open(self.h, _ptr(Vv), Vv.shape[0], _ptr(Ff),
+                                                     Ff.shape[0], eps_2, sampling_dist,
+                                                     ctypes.byref(j)), allow=(TW_OK, TW_BUSY))
+        return None if st == TW_BUSY else int(j.value)
+
+    def job_boundary(self, job, V, F):
+        Vv = _c(V, np.float64).reshape(-1, 3)
+        Ff = _c(F, np.int32).reshape(-1, 3)
+        self._check(self.lib.tw_server_job_boundary(self.h, job, _ptr(Vv), Vv.shape[0], _ptr(Ff),
+                                                    Ff.shape[0]))
+
+    def job_mesh(self, job, xyz, timeout_s=60.0):
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        self._check(self.lib.tw_server_job_mesh(self.h, job, _ptr(X), X.shape[0], timeout_s))
+
+    def job_read_mesh(self, job, nv, timeout_s=60.0):
+        out = np.empty((nv, 3))
+        self._check(self.lib.tw_server_job_read_mesh(self.h, job, _ptr(out), timeout_s))
+        return out
+
+    def job_close(self, job, timeout_s=60.0):
+        self._check(self.lib.tw_server_job_close(self.h, job, timeout_s))
+
+    def _submit(self, job, req, keep):
+        t = ctypes.c_uint64()
+        self._check(self.lib.tw_server_submit(self.h, job, ctypes.byref(req), ctypes.byref(t)))
+        self._keep[t.value] = keep
+        return t.value
+
+    def submit_points(self, job, P):
+        X = _c(P, np.float64).reshape(-1, 3)
+        out = np.empty(X.shape[0], np.uint8)
+        r = TwRequest(TW_REQ_POINTS, 0, X.shape[0], _ptr(X), None, None, None, None, _ptr(out))
+        return self._submit(job, r, (X, out)), out
+
+    def submit_faces(self, job, tris):
+        X = _c(tris, np.float64).reshape(-1, 9)
+        out = np.empty(X.shape[0], np.uint8)
+        r = TwRequest(TW_REQ_FACES, 0, X.shape[0], _ptr(X), None, None, None, None, _ptr(out))
+        return self._submit(job, r, (X, out)), out
+
+    def submit_amips(self, job, T_soa, raw=False):
+        T = _c(T_soa, np.float64)
+        n = T.shape[1]
+        E, J, H, Fl = np.empty(n), np.empty((3, n)), np.empty((9, n)), np.empty(n, np.uint8)
+        r = TwRequest(TW_REQ_AMIPS, TW_REQ_RAW if raw else 0, n, _ptr(T), None, None, None, None,
+                      _ptr(E), _ptr(J), _ptr(H), _ptr(Fl))
+        return self._submit(job, r, (T, E, J, H, Fl)), (E, J, H, Fl)
+
+    def submit_smooth(self, job, star_off, tets, centers, face_flags=None, kinds=None,
+                      apply=False):
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        C = _c(centers, np.int32)
+        FF = None if face_flags is None else _c(face_flags, np.uint8)
+        K = None if kinds is None else _c(kinds, np.uint8)
+        ns = C.size
+        out = np.empty((ns, 3))
+        st = np.empty(ns, np.uint8)
+        r = TwRequest(TW_REQ_SMOOTH, TW_REQ_APPLY if apply else 0, ns, _ptr(O), _ptr(T), _ptr(FF),
+                      _ptr(C), _ptr(K), _ptr(out), _ptr(st))
+        return self._submit(job, r, (O, T, FF, C, K, out, st)), (out, st)
+
+    def wait(self, ticket, timeout_s=60.0):
+        """Returns the latency in ms (submit to completion); raises on a failed request."""
+        lat = _D()
+        st = self.lib.tw_server_wait(self.h, ticket, timeout_s, ctypes.byref(lat))
+        if st == TW_ERR_TIMEOUT:
+            raise TimeoutError(f"request {ticket} not done after {timeout_s} s")
+        self._keep.pop(ticket, None)
+        self._check(st)
+        return lat.value
+
+    def stats(self):
+        s = TwServerStats()
+        self._check(self.lib.tw_server_get_stats(self.h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in TwServerStats._fields_}
 
 
 class Graph:

@@ -745,20 +745,7 @@ int tw_nearest_points(tw_ctx* c, const double* P, int64_t n, int which, double* 
 // ---- smoothing pass ----------------------------------------------------------------
 }  // extern "C"
 
-namespace {
-// Scratch of a smoothing pass (slot 8): per star the Newton / projected
-// position, face range and state; per possible face (3 per tet) its nine
-// coordinates and decision; the face counter.
-struct SmoothScratch {
-    double* pnew;
-    int32_t* face_base;
-    int32_t* face_cnt;
-    double* faces;
-    uint8_t* face_out;
-    unsigned long long* face_count;
-    int64_t face_cap;
-};
-
+namespace tw {
 int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S) {
     auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
     const int64_t cap = 3 * ntets;
@@ -779,7 +766,6 @@ int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S) {
     return TW_OK;
 }
 
-// The pass on device arrays; asynchronous on the context stream.
 void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uint8_t* ff,
                    const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
                    double* out, uint8_t* status, const SmoothScratch& S) {
@@ -797,7 +783,7 @@ void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uin
     launch_smooth_finalize(nstars, S.face_base, S.face_cnt, S.face_out, S.pnew, out, status,
                            c->stream);
 }
-}  // namespace
+}  // namespace tw
 
 extern "C" {
 

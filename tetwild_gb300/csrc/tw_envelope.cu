@@ -16,6 +16,8 @@
 // and the warp stops at the first sample that is out.
 #include <cub/device/device_radix_sort.cuh>
 
+#include <cstring>
+
 #include "tw_device.cuh"
 #include "tw_internal.h"
 
@@ -464,31 +466,24 @@ __device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_
     return false;
 }
 
+// One face, the whole warp: 1 if some sample is out, 0 otherwise (and for a
+// degenerate face); a face beyond the per-row sample bound sets error bit 2
+// and counts as out.
 template <bool FP32>
-__device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris, int64_t n,
-                                                 const FaceCtx& F, double sd,
-                                                 uint8_t* __restrict__ out) {
+__device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
+                                                 const FaceCtx& F, double sd, TravStats& st,
+                                                 uint32_t& nq) {
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    TravStats st;
-    uint32_t nq = 0;
-    for (int64_t f = warp; f < n; f += nwarps) {
+    {
         double t[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) t[k] = __ldg(tris + 9 * f + k);
-        if (tri_collinear(t)) {
-            if (lane == 0) out[f] = 0;
-            continue;
-        }
+        for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + k);
+        if (tri_collinear(t)) return 0;
         SampleHeader h;
         sample_header(t, sd, h);
         if (header_too_large(h)) {
-            if (lane == 0) {
-                atomicOr(F.counters + kCntError, 2ULL);
-                out[f] = 1;
-            }
-            continue;
+            if (lane == 0) atomicOr(F.counters + kCntError, 2ULL);
+            return 1;
         }
         int32_t hint = -1;
         bool out_found = false;
@@ -498,8 +493,7 @@ __device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris
                 ++nq;
             }
             out_found = __any_sync(0xffffffffu, out_found);
-            if (lane == 0) out[f] = out_found ? 1 : 0;
-            continue;
+            return out_found ? 1 : 0;
         }
         // Row break: first m in [1, M] with distance(v0_m, v1_m) <= sd.
         int mstop = h.M + 1;
@@ -563,7 +557,22 @@ __device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris
             if (__any_sync(0xffffffffu, o)) { out_found = true; break; }
             if (__all_sync(0xffffffffu, !have)) break;
         }
-        if (lane == 0) out[f] = out_found ? 1 : 0;
+        return out_found ? 1 : 0;
+    }
+}
+
+template <bool FP32>
+__device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris, int64_t n,
+                                                 const FaceCtx& F, double sd,
+                                                 uint8_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    TravStats st;
+    uint32_t nq = 0;
+    for (int64_t f = warp; f < n; f += nwarps) {
+        uint8_t o = env_face_warp<FP32>(tris + 9 * f, F, sd, st, nq);
+        if (lane == 0) out[f] = o;
     }
     flush_stats(st, F.counters, nq);
 }
@@ -610,6 +619,107 @@ void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned l
         k_env_faces_dev<true><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
     else
         k_env_faces_dev<false><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
+}
+
+// ---------------------------------------------------------------------------
+// Several jobs in one launch (the serving loop): query i belongs to the last
+// segment whose begin is <= i; each segment names its job's tree and eps.
+// ---------------------------------------------------------------------------
+struct EnvSeg {
+    int64_t begin;
+    EnvTree T;
+    EpsParams E;
+    double sd;
+};
+
+size_t env_seg_bytes() { return sizeof(EnvSeg); }
+
+void fill_env_seg(void* dst, const Surface& S, int64_t begin, double eps2, double sd) {
+    EnvSeg g;
+    g.begin = begin;
+    g.T = env_tree(S);
+    g.E = eps_params(eps2);
+    g.sd = sd;
+    std::memcpy(dst, &g, sizeof g);
+}
+
+__device__ __forceinline__ int find_seg(const EnvSeg* __restrict__ segs, int nsegs, int64_t i) {
+    int lo = 0, hi = nsegs - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&segs[mid].begin) <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(128) k_env_points_segs(const double* __restrict__ P, int64_t n,
+                                                         const EnvSeg* __restrict__ segs, int nsegs,
+                                                         uint8_t* __restrict__ out,
+                                                         unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    TravStats st;
+    uint32_t nq = 0;
+    const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t base0 = first - (threadIdx.x & 31);
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + (threadIdx.x & 31);
+        if (i < n) {
+            const EnvSeg& g = segs[find_seg(segs, nsegs, i)];
+            const EnvTree T = g.T;
+            const EpsParams E = g.E;
+            V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
+            int32_t f = query_point<FP32>(T, p, E, st);
+            if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
+            out[i] = (uint8_t)(f == -1);
+            ++nq;
+        }
+    }
+    flush_stats(st, counters, nq);
+}
+
+template <bool FP32>
+__global__ void __launch_bounds__(128) k_env_faces_segs(const double* __restrict__ tris, int64_t n,
+                                                        const EnvSeg* __restrict__ segs, int nsegs,
+                                                        uint8_t* __restrict__ out,
+                                                        unsigned long long* __restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    TravStats st;
+    uint32_t nq = 0;
+    for (int64_t f = warp; f < n; f += nwarps) {
+        const EnvSeg& g = segs[find_seg(segs, nsegs, f)];
+        FaceCtx F{g.T, g.E, counters};
+        uint8_t o = env_face_warp<FP32>(tris + 9 * f, F, g.sd, st, nq);
+        if (lane == 0) out[f] = o;
+    }
+    flush_stats(st, counters, nq);
+}
+
+void launch_env_points_segs(const double* P, int64_t n, const void* segs, int nsegs, uint8_t* out,
+                            int precision, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0 || nsegs <= 0) return;
+    const int block = 128;
+    const int grid = grid_for(n, block, 6);
+    const EnvSeg* g = static_cast<const EnvSeg*>(segs);
+    if (precision == TW_PRECISION_FP32_CERTIFIED)
+        k_env_points_segs<true><<<grid, block, 0, s>>>(P, n, g, nsegs, out, counters);
+    else
+        k_env_points_segs<false><<<grid, block, 0, s>>>(P, n, g, nsegs, out, counters);
+}
+
+void launch_env_faces_segs(const double* tris, int64_t n, const void* segs, int nsegs, uint8_t* out,
+                           int precision, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0 || nsegs <= 0) return;
+    const int block = 128;
+    const int grid = grid_for(n * 32, block, 16);
+    const EnvSeg* g = static_cast<const EnvSeg*>(segs);
+    if (precision == TW_PRECISION_FP32_CERTIFIED)
+        k_env_faces_segs<true><<<grid, block, 0, s>>>(tris, n, g, nsegs, out, counters);
+    else
+        k_env_faces_segs<false><<<grid, block, 0, s>>>(tris, n, g, nsegs, out, counters);
 }
 
 // ---------------------------------------------------------------------------

@@ -170,6 +170,14 @@ void launch_sample_triangle(const double* tri, double sd, double* out, int64_t c
 void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned long long* n_dev,
                           int64_t cap, double eps2, double sd, uint8_t* out, int precision,
                           unsigned long long* counters, cudaStream_t s);
+// Several jobs per launch: segs is a device array of nsegs env_seg_bytes()
+// records filled by fill_env_seg (ascending begin offsets, the first 0).
+size_t env_seg_bytes();
+void fill_env_seg(void* dst, const Surface& S, int64_t begin, double eps2, double sd);
+void launch_env_points_segs(const double* P, int64_t n, const void* segs, int nsegs, uint8_t* out,
+                            int precision, unsigned long long* counters, cudaStream_t s);
+void launch_env_faces_segs(const double* tris, int64_t n, const void* segs, int nsegs, uint8_t* out,
+                           int precision, unsigned long long* counters, cudaStream_t s);
 void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,
                            int32_t* F, unsigned long long* counters, cudaStream_t s);
 void launch_smooth_project(const Surface& Sin, const Surface& Sb, const uint8_t* kinds,
@@ -209,6 +217,25 @@ void launch_smooth_stage2(int shape, const double* vx, const double* vy, const d
 void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
                             const uint8_t* face_out, const double* pnew, double* out,
                             uint8_t* status, cudaStream_t s);
+
+// Scratch of a smoothing pass (context slot 8): per star the Newton /
+// projected position, face range and state; per possible face (3 per tet)
+// its nine coordinates and decision; the face counter (tw_capi.cu).
+struct SmoothScratch {
+    double* pnew;
+    int32_t* face_base;
+    int32_t* face_cnt;
+    double* faces;
+    uint8_t* face_out;
+    unsigned long long* face_count;
+    int64_t face_cap;
+};
+int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S);
+// The pass over device arrays with the context's mesh, surfaces, parameters
+// and stream; asynchronous.
+void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uint8_t* ff,
+                   const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
+                   double* out, uint8_t* status, const SmoothScratch& S);
 
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);
