@@ -359,6 +359,8 @@ def run_ours(args):
     }
     if not args.no_batching:
         line["batching"] = run_batching(ctx, V, F, args, dev, ws)
+    if not args.no_serving:
+        line["serving"] = run_serving(args, dev)
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle.oracle import default_threads
 
@@ -475,6 +477,220 @@ def run_batching(ctx, V, F, args, dev, ws):
     }
 
 
+N_JOBS = 64
+SERVE_SECONDS = 6.0
+SERVE_LANES = 4
+SERVE_BUDGET = 150 << 30
+SERVE_MIX = (("points", 0.40, 1_000, 500_000), ("amips", 0.30, 1_000, 500_000),
+             ("faces", 0.15, 1_000, 20_000), ("smooth", 0.15, 1_000, 10_000))
+SERVE_SLOTS = 64
+
+
+def _serving_surface(shape, target, seed):
+    from tetwild_gb300 import synthetic as syn
+
+    if shape == 0:
+        subdiv = int(np.clip(round(np.log(target / 20.0) / np.log(4.0)), 2, 6))
+        return syn.icosphere(subdiv, seed=seed)
+    if shape == 1:
+        m = max(8, int(round(np.sqrt(target / 6.0))))
+        return syn.torus(1.0, 0.3, 3 * m, m)
+    r = max(8, int(round(np.sqrt(target / 4.0))))
+    return syn.displaced_sphere(seed=seed, n_lon=2 * r, n_rings=r)
+
+
+def _faces_near(V, F, n, sd, rng):
+    """Small triangles (edges ~3 sampling distances) around surface points, offset along the
+    normal by U(-1.5, 1.5) eps (eps = sd here)."""
+    from tetwild_gb300 import synthetic as syn
+
+    P = syn.envelope_points(V, F, n, 0.0, seed=int(rng.integers(1 << 30)))
+    a = rng.normal(size=(n, 3))
+    b = rng.normal(size=(n, 3))
+    a *= 3 * sd / np.linalg.norm(a, axis=1, keepdims=True)
+    b *= 3 * sd / np.linalg.norm(b, axis=1, keepdims=True)
+    off = rng.uniform(-1.5, 1.5, (n, 1)) * sd * np.array([[0.0, 0.0, 1.0]])
+    return np.hstack([P + off, P + a + off, P + b + off])
+
+
+def run_serving(args, dev):
+    """Serving workload: 64 meshing jobs (icospheres, tori R=1 r=0.3, displaced spheres) of
+    1k-200k triangles (log-uniform) resident in HBM under a 150 GB budget; requests of 1k-500k
+    queries (log-uniform per kind: envelope points, AMIPS E/J/H, envelope faces, smoothing
+    stars) for uniformly chosen jobs.  A burst of 256 requests measures capacity in each
+    precision mode; then requests arrive as a Poisson process at 70% of the certified capacity
+    for SERVE_SECONDS, and the server-side latency of each (submit to results in host memory)
+    gives p50 / p99."""
+    import threading
+
+    import tetwild_gb300 as tw
+    from tetwild_gb300 import synthetic as syn
+
+    rng = np.random.default_rng(2025)
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(2e5), N_JOBS))
+    srv = tw.Server(dev, SERVE_BUDGET, lanes=SERVE_LANES)
+    max_n = {k: hi for k, _, _, hi in SERVE_MIX}
+    pinned = []
+
+    def pin(a):
+        p = tw.PinnedArray(a.shape, a.dtype)
+        p.array[...] = a
+        pinned.append(p)
+        return p.array
+
+    jobs, tris = [], 0
+    t_gen = time.perf_counter()
+    for i in range(N_JOBS):
+        V, F = _serving_surface(i % 3, sizes[i], seed=i)
+        tris += len(F)
+        diag = float(np.linalg.norm(V.max(0) - V.min(0)))
+        eps = 1e-3 * diag
+        sd = eps
+        j = srv.job_open(V, F, eps * eps, sd)
+        if j is None:
+            raise RuntimeError("job not admitted under the 150 GB budget")
+        P = pin(syn.envelope_points(V, F, max_n["points"], eps, seed=1000 + i))
+        Fc = pin(_faces_near(V, F, max_n["faces"], sd, rng))
+        xyz, off, tets, ff, cen = syn.surface_star_batch(V, F, max_n["smooth"], eps, seed=2000 + i,
+                                                         radius=6 * eps)
+        srv.job_mesh(j, xyz)
+        jobs.append({"id": j, "P": P, "F": Fc, "off": pin(off), "tets": pin(tets), "ff": pin(ff),
+                     "cen": pin(cen), "kinds": pin(np.ones(len(cen), np.uint8))})
+    # AMIPS requests take one of 16 log-spaced sizes, each a contiguous pinned SoA batch
+    amips_sizes = np.unique(np.geomspace(1_000, max_n["amips"], 16).astype(np.int64))
+    Tpool = {int(n): pin(syn.energy_batch(int(n), seed=77 + k)) for k, n in enumerate(amips_sizes)}
+    t_gen = time.perf_counter() - t_gen
+
+    # output slots (pinned), reused once the request that held them has completed
+    outs = {"points": pin(np.zeros((SERVE_SLOTS, max_n["points"]), np.uint8)),
+            "faces": pin(np.zeros((SERVE_SLOTS, max_n["faces"]), np.uint8)),
+            "E": pin(np.zeros((SERVE_SLOTS, max_n["amips"]))),
+            "J": pin(np.zeros((SERVE_SLOTS, 3 * max_n["amips"]))),
+            "H": pin(np.zeros((SERVE_SLOTS, 9 * max_n["amips"]))),
+            "flip": pin(np.zeros((SERVE_SLOTS, max_n["amips"]), np.uint8)),
+            "sout": pin(np.zeros((SERVE_SLOTS, 3 * max_n["smooth"]))),
+            "sst": pin(np.zeros((SERVE_SLOTS, max_n["smooth"]), np.uint8))}
+
+    kinds = [k for k, _, _, _ in SERVE_MIX]
+    probs = np.array([p for _, p, _, _ in SERVE_MIX])
+
+    def draw(m):
+        out = []
+        for _ in range(m):
+            k = int(rng.choice(len(kinds), p=probs))
+            _, _, lo, hi = SERVE_MIX[k]
+            n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+            if kinds[k] == "amips":
+                n = int(amips_sizes[np.argmin(np.abs(np.log(amips_sizes / n)))])
+            out.append((kinds[k], int(rng.integers(N_JOBS)), n))
+        return out
+
+    def submit(i, req):
+        kind, ji, n = req
+        J = jobs[ji]
+        slot = i % SERVE_SLOTS
+        if kind == "points":
+            t, _ = srv.submit_points(J["id"], J["P"][:n], out=outs["points"][slot, :n])
+        elif kind == "faces":
+            t, _ = srv.submit_faces(J["id"], J["F"][:n], out=outs["faces"][slot, :n])
+        elif kind == "amips":
+            o = (outs["E"][slot, :n], outs["J"][slot, :3 * n].reshape(3, n),
+                 outs["H"][slot, :9 * n].reshape(9, n), outs["flip"][slot, :n])
+            t, _ = srv.submit_amips(J["id"], Tpool[n], out=o)
+        else:
+            o = (outs["sout"][slot, :3 * n].reshape(n, 3), outs["sst"][slot, :n])
+            t, _ = srv.submit_smooth(J["id"], J["off"][:n + 1], J["tets"][:J["off"][n]],
+                                     J["cen"][:n], J["ff"][:J["off"][n]], J["kinds"][:n], out=o)
+        return t
+
+    def run(reqs, arrivals=None):
+        """Submits reqs (at the given arrival times, else at once) and returns per-request
+        latencies (ms) and the wall time from the first submission to the last completion."""
+        lat = [0.0] * len(reqs)
+        done = [threading.Event() for _ in reqs]
+        tickets = [None] * len(reqs)
+        ready = [threading.Event() for _ in reqs]
+        err = []
+
+        def waiter():
+            try:
+                for i in range(len(reqs)):
+                    ready[i].wait()
+                    lat[i] = srv.wait(tickets[i], 120.0)
+                    done[i].set()
+            except Exception as e:
+                err.append(e)
+                for d in done:
+                    d.set()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            if i >= SERVE_SLOTS:
+                done[i - SERVE_SLOTS].wait()
+            if arrivals is not None:
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+            tickets[i] = submit(i, r)
+            ready[i].set()
+        th.join()
+        wall = time.perf_counter() - t0
+        if err:
+            raise err[0]
+        return lat, wall
+
+    burst = draw(256)
+    q_burst = sum(n for _, _, n in burst)
+    cap = {}
+    for name, prec in (("fp64", tw.TW_PRECISION_FP64),
+                       ("fp32_certified", tw.TW_PRECISION_FP32_CERTIFIED)):
+        srv.set_params(prec, 1, 8)
+        run(burst[:32])                     # warm-up: lane scratch grows to size
+        lat, wall = run(burst)
+        cap[name] = {"queries_per_s": q_burst / wall, "requests_per_s": len(burst) / wall,
+                     "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                     "p99_ms": float(np.percentile(lat, 99))}
+    rate = 0.7 * cap["fp32_certified"]["requests_per_s"]
+    m = max(64, int(rate * SERVE_SECONDS))
+    reqs = draw(m)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, m))
+    st0 = srv.stats()
+    lat, wall = run(reqs, arrivals)
+    st1 = srv.stats()
+    q = sum(n for _, _, n in reqs)
+    by_kind = {}
+    for k in kinds:
+        l = [x for x, r in zip(lat, reqs) if r[0] == k]
+        if l:
+            by_kind[k] = {"requests": len(l), "p50_ms": float(np.percentile(l, 50)),
+                          "p99_ms": float(np.percentile(l, 99))}
+    stats = srv.stats()
+    srv.close()
+    for p_ in pinned:
+        p_.free()
+    return {
+        "workload": f"{N_JOBS} jobs (icosphere / torus R=1 r=0.3 / displaced sphere, "
+                    f"1k-200k tris log-uniform, {tris} tris in all) under a 150 GB budget; "
+                    "requests: points 40% (1k-500k), AMIPS E/J/H 30% (16 log-spaced sizes 1k-500k), faces 15% "
+                    "(1k-20k), smoothing stars 15% (1k-10k), log-uniform sizes, uniform jobs; "
+                    f"{SERVE_LANES} lanes; certified FP32 mode",
+        "arrival_rate_per_s": rate, "offered_load": "70% of the certified burst capacity",
+        "requests": m, "queries": q, "seconds": wall,
+        "queries_per_s": q / wall, "unit": "queries/s",
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "latency_by_kind": by_kind,
+        "burst_capacity": cap,
+        "capacity_speedup_certified_vs_fp64": (cap["fp32_certified"]["queries_per_s"] /
+                                               cap["fp64"]["queries_per_s"]),
+        "batches": st1["batches"] - st0["batches"],
+        "mean_requests_per_batch": m / max(1, st1["batches"] - st0["batches"]),
+        "max_requests_per_batch": stats["max_requests_per_batch"],
+        "hbm_bytes_used": stats["bytes_used"], "setup_s": t_gen,
+    }
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -565,6 +781,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-batching", action="store_true", help="skip the star-batch pass")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving loop")
     ap.add_argument("--modes", default="plain,cert",
                     help="profiling runs may time one mode only (then no benchmark line)")
     ap.add_argument("--tets", type=int, default=N_TETS, help="smaller case for profiling only")

@@ -601,36 +601,39 @@ class Server:
         self._keep[t.value] = keep
         return t.value
 
-    def submit_points(self, job, P):
+    def submit_points(self, job, P, out=None):
         X = _c(P, np.float64).reshape(-1, 3)
-        out = np.empty(X.shape[0], np.uint8)
+        out = np.empty(X.shape[0], np.uint8) if out is None else out
         r = TwRequest(TW_REQ_POINTS, 0, X.shape[0], _ptr(X), None, None, None, None, _ptr(out))
         return self._submit(job, r, (X, out)), out
 
-    def submit_faces(self, job, tris):
+    def submit_faces(self, job, tris, out=None):
         X = _c(tris, np.float64).reshape(-1, 9)
-        out = np.empty(X.shape[0], np.uint8)
+        out = np.empty(X.shape[0], np.uint8) if out is None else out
         r = TwRequest(TW_REQ_FACES, 0, X.shape[0], _ptr(X), None, None, None, None, _ptr(out))
         return self._submit(job, r, (X, out)), out
 
-    def submit_amips(self, job, T_soa, raw=False):
+    def submit_amips(self, job, T_soa, raw=False, out=None, jacobian=True, hessian=True):
+        """out: optional (E, J, H, flip) arrays; J / H may be None (not computed)."""
         T = _c(T_soa, np.float64)
         n = T.shape[1]
-        E, J, H, Fl = np.empty(n), np.empty((3, n)), np.empty((9, n)), np.empty(n, np.uint8)
+        if out is None:
+            out = (np.empty(n), np.empty((3, n)) if jacobian else None,
+                   np.empty((9, n)) if hessian else None, np.empty(n, np.uint8))
+        E, J, H, Fl = out
         r = TwRequest(TW_REQ_AMIPS, TW_REQ_RAW if raw else 0, n, _ptr(T), None, None, None, None,
                       _ptr(E), _ptr(J), _ptr(H), _ptr(Fl))
         return self._submit(job, r, (T, E, J, H, Fl)), (E, J, H, Fl)
 
     def submit_smooth(self, job, star_off, tets, centers, face_flags=None, kinds=None,
-                      apply=False):
+                      apply=False, out=None):
         O = _c(star_off, np.int32)
         T = _c(tets, np.int32).reshape(-1, 4)
         C = _c(centers, np.int32)
         FF = None if face_flags is None else _c(face_flags, np.uint8)
         K = None if kinds is None else _c(kinds, np.uint8)
         ns = C.size
-        out = np.empty((ns, 3))
-        st = np.empty(ns, np.uint8)
+        out, st = (np.empty((ns, 3)), np.empty(ns, np.uint8)) if out is None else out
         r = TwRequest(TW_REQ_SMOOTH, TW_REQ_APPLY if apply else 0, ns, _ptr(O), _ptr(T), _ptr(FF),
                       _ptr(C), _ptr(K), _ptr(out), _ptr(st))
         return self._submit(job, r, (O, T, FF, C, K, out, st)), (out, st)
