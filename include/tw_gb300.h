@@ -97,6 +97,7 @@ typedef struct tw_stats {
     uint64_t env_facet_fp64;       /* of those, evaluated in binary64               */
     uint64_t amips_tets;           /* tets evaluated by the AMIPS kernels           */
     uint64_t amips_fp64;           /* of those, recomputed in binary64 (certified)  */
+    uint64_t env_warp_fallbacks;   /* point warps that walked the tree per point    */
 } tw_stats;
 TW_API int tw_get_stats(tw_ctx* ctx, tw_stats* out);
 TW_API int tw_reset_stats(tw_ctx* ctx);

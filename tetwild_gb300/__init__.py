@@ -76,7 +76,7 @@ TW_PRECISION_FP64 = 0
 TW_PRECISION_FP32_CERTIFIED = 1
 
 _STAT_FIELDS = ("exact_orientations", "env_queries", "env_facet_tests", "env_facet_fp64",
-                "amips_tets", "amips_fp64")
+                "amips_tets", "amips_fp64", "env_warp_fallbacks")
 
 
 class TwStats(ctypes.Structure):

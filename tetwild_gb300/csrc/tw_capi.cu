@@ -338,6 +338,7 @@ int tw_get_stats(tw_ctx* c, tw_stats* out) {
     out->env_facet_fp64 = h[kCntEnvFp64];
     out->amips_tets = h[kCntAmipsTets];
     out->amips_fp64 = h[kCntAmipsFp64];
+    out->env_warp_fallbacks = h[kCntEnvWarpFallback];
     return TW_OK;
 }
 

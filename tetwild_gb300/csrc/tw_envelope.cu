@@ -194,6 +194,170 @@ __global__ void __launch_bounds__(128, MINB) k_env_points(const double* __restri
     flush_stats(st, counters, nq);
 }
 
+// ---------------------------------------------------------------------------
+// Warp-shared candidates (certified mode).  With the points in Morton order
+// the 32 points of a warp lie close together: the warp walks the tree once
+// for the box of its points grown by the largest per-point culling radius
+// (sqrt of CertQuery::thr, rounded up), collecting every leaf whose binary32
+// box meets it, and each lane then tests its own point against that list.
+// Every leaf that the per-point walk could reach (box within sqrt(thr) of the
+// point) meets the grown box, and each leaf test is the same certified test,
+// so every decision equals the per-point walk's, i.e. FP64's.  A warp whose
+// box meets more than 32 leaves falls back to the per-point walk.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool box_meets(const float* lo, const float* hi, const float* qlo,
+                                          const float* qhi) {
+    return lo[0] <= qhi[0] && hi[0] >= qlo[0] && lo[1] <= qhi[1] && hi[1] >= qlo[1] &&
+           lo[2] <= qhi[2] && hi[2] >= qlo[2];
+}
+
+// Lane k receives the k-th leaf in cand; returns the count (the same on every
+// lane), -1 when above 32, kTraversalError on a malformed tree.  Every lane
+// walks the same nodes (uniform control flow, broadcast loads).
+__device__ __forceinline__ int warp_candidates32(const EnvTree& T, const float* qlo,
+                                                 const float* qhi, int lane, int32_t& cand) {
+    const int32_t nf = T.nf;
+    if (nf == 1) {
+        cand = 0;
+        return 1;
+    }
+    int32_t stack[kStack];
+    int sp = 0, cnt = 0;
+    int32_t cur = 0;
+    for (int32_t iter = 0; iter < nf; ++iter) {
+        if ((uint32_t)cur >= (uint32_t)(nf - 1)) return kTraversalError;
+        const float4* nd = reinterpret_cast<const float4*>(T.nodes32 + cur);
+        float4 q0 = __ldg(nd + 0), q1 = __ldg(nd + 1), q2 = __ldg(nd + 2);
+        int4 q3 = __ldg(reinterpret_cast<const int4*>(nd + 3));
+        const float lo0[3] = {q0.x, q0.y, q0.z}, hi0[3] = {q0.w, q1.x, q1.y};
+        const float lo1[3] = {q1.z, q1.w, q2.x}, hi1[3] = {q2.y, q2.z, q2.w};
+        bool h0 = box_meets(lo0, hi0, qlo, qhi), h1 = box_meets(lo1, hi1, qlo, qhi);
+        if (h0 && q3.x < 0) {
+            if ((uint32_t)(~q3.x) >= (uint32_t)nf) return kTraversalError;
+            if (lane == cnt) cand = ~q3.x;
+            if (++cnt > 32) return -1;
+            h0 = false;
+        }
+        if (h1 && q3.y < 0) {
+            if ((uint32_t)(~q3.y) >= (uint32_t)nf) return kTraversalError;
+            if (lane == cnt) cand = ~q3.y;
+            if (++cnt > 32) return -1;
+            h1 = false;
+        }
+        if (h0 && h1) {
+            if (sp >= kStack) return kTraversalError;
+            stack[sp++] = q3.y;
+            cur = q3.x;
+        } else if (h0) {
+            cur = q3.x;
+        } else if (h1) {
+            cur = q3.y;
+        } else {
+            if (sp == 0) return cnt;
+            cur = stack[--sp];
+        }
+    }
+    return kTraversalError;
+}
+
+// Orders the first cnt candidates (one per lane) by the squared distance from
+// (cx, cy, cz) to their facet's centroid (bitonic sort across the warp), so
+// that the facets most likely to hold a point of the warp are tested first.
+// The order changes the work, never a decision.
+__device__ __forceinline__ void sort_candidates(const EnvTree& T, float cx, float cy, float cz,
+                                                int lane, int cnt, int32_t& cand) {
+    float key = __int_as_float(0x7f800000);
+    if (lane < cnt) {
+        const double* t = T.tri + 9 * (int64_t)cand;
+        const float gx = (float)((__ldg(t) + __ldg(t + 3)) + __ldg(t + 6)) * (1.0f / 3.0f);
+        const float gy = (float)((__ldg(t + 1) + __ldg(t + 4)) + __ldg(t + 7)) * (1.0f / 3.0f);
+        const float gz = (float)((__ldg(t + 2) + __ldg(t + 5)) + __ldg(t + 8)) * (1.0f / 3.0f);
+        key = (gx - cx) * (gx - cx) + (gy - cy) * (gy - cy) + (gz - cz) * (gz - cz);
+    }
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const float ok = __shfl_xor_sync(0xffffffffu, key, j);
+            const int32_t ov = __shfl_xor_sync(0xffffffffu, cand, j);
+            const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+            const bool take = (lower == up) ? (ok < key) : (ok > key);
+            if (take) {
+                key = ok;
+                cand = ov;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_env_points_warp(const double* __restrict__ P,
+                                                         const int32_t* __restrict__ order,
+                                                         int64_t n, EnvTree T, EpsParams E,
+                                                         uint8_t* __restrict__ out,
+                                                         unsigned long long* __restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    TravStats st;
+    uint32_t nq = 0, fallback = 0;
+    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane;
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + lane;
+        const bool valid = i < n;
+        const int64_t j = valid ? (order ? (int64_t)__ldg(order + i) : i) : 0;
+        V3 p{0.0, 0.0, 0.0};
+        if (valid) p = V3{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
+        const CertQuery q = cert_query(p, E, T.scale_hi);
+        const float inf = __int_as_float(0x7f800000);
+        const float r = valid ? __fsqrt_ru(q.thr) : 0.0f;
+        const float R = warp_max(r);
+        float qlo[3], qhi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            qlo[k] = __fsub_rd(warp_min(valid ? q.ph[k] : inf), R);
+            qhi[k] = __fadd_ru(warp_max(valid ? q.ph[k] : -inf), R);
+        }
+        int32_t cand = -1;
+        const int cnt = warp_candidates32(T, qlo, qhi, lane, cand);
+        bool in = false;
+        if (cnt > 1)
+            sort_candidates(T, 0.5f * (qlo[0] + qhi[0]), 0.5f * (qlo[1] + qhi[1]),
+                            0.5f * (qlo[2] + qhi[2]), lane, cnt, cand);
+        if (cnt >= 0) {
+            for (int k = 0; k < cnt; ++k) {
+                const int32_t lf = __shfl_sync(0xffffffffu, cand, k);
+                if (valid && !in) in = cert_leaf_within(T.cull, T.tri, lf, p, q, E.eps2, st);
+                if (__all_sync(0xffffffffu, in || !valid)) break;
+            }
+        } else {
+            if (cnt == kTraversalError && lane == 0) atomicOr(counters + kCntError, 1ULL);
+            ++fallback;
+            if (valid) {
+                int32_t f = query_point<true>(T, p, E, st);
+                if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
+                in = f >= 0;
+            }
+        }
+        if (valid) {
+            out[j] = (uint8_t)!in;
+            ++nq;
+        }
+    }
+    flush_stats(st, counters, nq);
+    if (lane == 0 && fallback) atomicAdd(counters + kCntEnvWarpFallback, (unsigned long long)fallback);
+}
+
 // 30-bit Morton code of each query point on the tree's centroid grid
 // (points outside the grid clamp to its faces).
 // The order only changes how much work the traversal does, never its
@@ -279,7 +443,10 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     const EpsParams E = eps_params(eps2);
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
-    if (precision == TW_PRECISION_FP32_CERTIFIED)
+    if (precision == TW_PRECISION_FP32_CERTIFIED && order)
+        k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
+                                                                      counters);
+    else if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_points<true, 6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                        counters);
     else
@@ -466,6 +633,30 @@ __device__ __forceinline__ bool sample_out(const FaceCtx& F, const V3& p, int32_
     return false;
 }
 
+// Binary32 box of the face's vertices grown by the largest culling radius of
+// any sample (CertQuery::thr with M = the surface's and the face's largest
+// coordinate) plus 2^-20 M for the rounding of the sample construction, all
+// rounded outward: every sample's binary32 point and everything within its
+// culling radius lie inside.
+__device__ __forceinline__ void face_query_box(const double* t, const FaceCtx& F, float* qlo,
+                                               float* qhi) {
+    double m = 0.0;
+    for (int k = 0; k < 9; ++k) m = fmax(m, fabs(t[k]));
+    const CertQuery q = cert_query(V3{m, m, m}, F.E, F.T.scale_hi);
+    const float mu = fmaxf(q.ph[0], F.T.scale_hi);
+    const float R = __fadd_ru(__fsqrt_ru(q.thr), __fmul_ru(9.5367431640625e-07f, mu));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double lo = fmin(t[k], fmin(t[3 + k], t[6 + k]));
+        const double hi = fmax(t[k], fmax(t[3 + k], t[6 + k]));
+        float flo = d2f_rn(lo), fhi = d2f_rn(hi);
+        if (f2d_exact(flo) > lo) flo = nextafterf(flo, -__int_as_float(0x7f800000));
+        if (f2d_exact(fhi) < hi) fhi = nextafterf(fhi, __int_as_float(0x7f800000));
+        qlo[k] = __fsub_rd(flo, R);
+        qhi[k] = __fadd_ru(fhi, R);
+    }
+}
+
 // One face, the whole warp: 1 if some sample is out, 0 otherwise (and for a
 // degenerate face); a face beyond the per-row sample bound sets error bit 2
 // and counts as out.
@@ -487,11 +678,48 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
         }
         int32_t hint = -1;
         bool out_found = false;
-        if (h.trivial) {
-            if (lane < 3) {
-                out_found = sample_out<FP32>(F, h.vs[lane], hint, st);
-                ++nq;
+        // certified mode: the leaves within reach of the face, shared by the
+        // warp (see k_env_points_warp); -1 when above 32 (per-sample walks)
+        int32_t cand = -1;
+        int cnt = -1, kh = 0;
+        if (FP32) {
+            float qlo[3], qhi[3];
+            face_query_box(t, F, qlo, qhi);
+            cnt = warp_candidates32(F.T, qlo, qhi, lane, cand);
+            if (cnt == kTraversalError) {
+                if (lane == 0) atomicOr(F.counters + kCntError, 1ULL);
+                cnt = -1;
             }
+            if (cnt > 1)
+                sort_candidates(F.T, (float)((t[0] + t[3]) + t[6]) * (1.0f / 3.0f),
+                                (float)((t[1] + t[4]) + t[7]) * (1.0f / 3.0f),
+                                (float)((t[2] + t[5]) + t[8]) * (1.0f / 3.0f), lane, cnt, cand);
+        }
+        // out iff the lane's sample (have) is out; called by the whole warp
+        auto lane_out = [&](bool have, const V3& p) -> bool {
+            if (cnt < 0) {
+                bool o = false;
+                if (have) o = sample_out<FP32>(F, p, hint, st);
+                return o;
+            }
+            bool in = !have;
+            CertQuery q;
+            if (have) q = cert_query(p, F.E, F.T.scale_hi);
+            for (int k = 0; k < cnt; ++k) {
+                const int kk = (k + kh) % cnt;
+                const int32_t lf = __shfl_sync(0xffffffffu, cand, kk);
+                if (!in && cert_leaf_within(F.T.cull, F.T.tri, lf, p, q, F.E.eps2, st)) {
+                    in = true;
+                    kh = kk;
+                }
+                if (__all_sync(0xffffffffu, in)) break;
+            }
+            return !in;
+        };
+        if (h.trivial) {
+            const bool have = lane < 3;
+            out_found = lane_out(have, have ? h.vs[lane] : h.vs[0]);
+            if (have) ++nq;
             out_found = __any_sync(0xffffffffu, out_found);
             return out_found ? 1 : 0;
         }
@@ -549,11 +777,8 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
                     else { phase = 5; }
                 }
             }
-            bool o = false;
-            if (have) {
-                o = sample_out<FP32>(F, p, hint, st);
-                ++nq;
-            }
+            const bool o = lane_out(have, p);
+            if (have) ++nq;
             if (__any_sync(0xffffffffu, o)) { out_found = true; break; }
             if (__all_sync(0xffffffffu, !have)) break;
         }

@@ -120,6 +120,7 @@ constexpr int kCntAmipsTets = 5;      // tets evaluated by the AMIPS kernels
 constexpr int kCntAmipsFp64 = 6;      // tets recomputed in FP64 (certified mode)
 constexpr int kCntBad = 7;            // host-visible argument check flag
 constexpr int kCntEnvQueries = 8;     // envelope sample/point queries
+constexpr int kCntEnvWarpFallback = 9;  // warps whose shared candidate list overflowed
 // internal star states of a smoothing pass (the final ones are TW_SMOOTH_*)
 constexpr uint8_t kSmoothPendingProject = 6;   // surface star moved by Newton, not yet projected
 constexpr uint8_t kSmoothPendingEnvelope = 7;  // surface star waiting for its face tests

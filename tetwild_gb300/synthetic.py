@@ -359,3 +359,79 @@ def mixed_star_batch(V: np.ndarray, F: np.ndarray, nstars: int, eps: float, seed
         nt += len(t)
     return (np.vstack(xyz), np.asarray(off, np.int32), np.vstack(tets).astype(np.int32),
             np.concatenate(ff), np.concatenate(cen).astype(np.int32), np.concatenate(kinds))
+
+
+def icosphere_stage1_mesh(subdiv: int = 3, jitter: float = 1e-3, seed: int = 0,
+                          edge_rel: float = 0.05, margin_rel: float = 0.05):
+    """A stand-in for TetWild's mesh at the start of refinement on the jittered icosphere.
+
+    The tet mesh is the Delaunay tetrahedralisation (scipy qhull) of the icosphere's vertices,
+    a lattice at spacing L = edge_rel * bbox diagonal (the CLI's default -l 0.05) over the
+    bounding box grown by margin_rel * diagonal, jittered by N(0, 0.02 L), minus lattice points
+    closer than L/2 to the sphere, plus the grown box's corners.  Tets are oriented POSITIVE.  A face is a surface face
+    when its vertex triple is an icosphere triangle.  Returns a dict with V, F (the input
+    surface), xyz, tets, face_flags (bit j: the face opposite vertex j is a surface face),
+    kind (0 interior, 1 surface, 3 locked box corner) and coverage (icosphere triangles found
+    among the Delaunay faces).
+    """
+    from scipy.spatial import Delaunay
+
+    V, F = icosphere(subdiv, jitter=jitter, seed=seed)
+    lo, hi = V.min(0), V.max(0)
+    diag = float(np.linalg.norm(hi - lo))
+    L = edge_rel * diag
+    glo, ghi = lo - margin_rel * diag, hi + margin_rel * diag
+    axes = [np.arange(glo[k] + L / 2, ghi[k], L) for k in range(3)]
+    G = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    # a regular lattice has co-spherical groups whose Delaunay tets are flat
+    G = G + np.random.default_rng(seed + 1).normal(0.0, 0.02 * L, G.shape)
+    r = np.linalg.norm(G, axis=1)
+    G = G[np.abs(r - 1.0) > L / 2]
+    corners = np.array([[glo[0] if i & 1 else ghi[0], glo[1] if i & 2 else ghi[1],
+                         glo[2] if i & 4 else ghi[2]] for i in range(8)])
+    xyz = np.vstack([V, G, corners])
+    kind = np.concatenate([np.ones(len(V), np.uint8), np.zeros(len(G), np.uint8),
+                           np.full(8, 3, np.uint8)])
+    tets = Delaunay(xyz).simplices.astype(np.int32)
+    p = xyz[tets]
+    det = np.einsum("ij,ij->i", p[:, 1] - p[:, 0], np.cross(p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]))
+    neg = det < 0
+    tets[neg] = tets[neg][:, [0, 2, 1, 3]]
+    surf = {tuple(sorted(map(int, f))) for f in F}
+    ff = np.zeros(len(tets), np.uint8)
+    found = set()
+    for j in range(4):
+        tri = np.sort(np.delete(tets, j, axis=1), axis=1)
+        for i in np.nonzero(np.all(tri < len(V), axis=1))[0]:
+            key = tuple(int(x) for x in tri[i])
+            if key in surf:
+                ff[i] |= np.uint8(1 << j)
+                found.add(key)
+    return {"V": V, "F": F, "xyz": xyz, "tets": tets, "face_flags": ff, "kind": kind,
+            "coverage": len(found) / len(F), "diag": diag, "edge": L}
+
+
+def vertex_stars(tets: np.ndarray, nv: int):
+    """conn_tets of every vertex in ascending tet order (CSR: off [nv+1], ids)."""
+    t = tets.reshape(-1)
+    owner = np.repeat(np.arange(len(tets), dtype=np.int64), 4)
+    order = np.lexsort((owner, t))
+    ids = owner[order].astype(np.int32)
+    off = np.zeros(nv + 1, np.int64)
+    np.add.at(off, t + 1, 1)
+    return np.cumsum(off).astype(np.int64), ids
+
+
+def greedy_colouring(tets: np.ndarray, nv: int) -> np.ndarray:
+    """Vertex colours such that no two vertices of a tet share one: each colour class is a set
+    of independent stars (no centre lies in another centre's star)."""
+    off, ids = vertex_stars(tets, nv)
+    colour = np.full(nv, -1, np.int64)
+    for v in range(nv):
+        nb = np.unique(tets[ids[off[v]:off[v + 1]]].reshape(-1))
+        used = set(colour[nb][colour[nb] >= 0].tolist())
+        c = 0
+        while c in used:
+            c += 1
+        colour[v] = c
+    return colour
