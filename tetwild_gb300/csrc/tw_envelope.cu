@@ -260,36 +260,6 @@ __device__ __forceinline__ int warp_candidates32(const EnvTree& T, const float* 
     return kTraversalError;
 }
 
-// Orders the first cnt candidates (one per lane) by the squared distance from
-// (cx, cy, cz) to their facet's centroid (bitonic sort across the warp), so
-// that the facets most likely to hold a point of the warp are tested first.
-// The order changes the work, never a decision.
-__device__ __forceinline__ void sort_candidates(const EnvTree& T, float cx, float cy, float cz,
-                                                int lane, int cnt, int32_t& cand) {
-    float key = __int_as_float(0x7f800000);
-    if (lane < cnt) {
-        const double* t = T.tri + 9 * (int64_t)cand;
-        const float gx = (float)((__ldg(t) + __ldg(t + 3)) + __ldg(t + 6)) * (1.0f / 3.0f);
-        const float gy = (float)((__ldg(t + 1) + __ldg(t + 4)) + __ldg(t + 7)) * (1.0f / 3.0f);
-        const float gz = (float)((__ldg(t + 2) + __ldg(t + 5)) + __ldg(t + 8)) * (1.0f / 3.0f);
-        key = (gx - cx) * (gx - cx) + (gy - cy) * (gy - cy) + (gz - cz) * (gz - cz);
-    }
-#pragma unroll
-    for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const float ok = __shfl_xor_sync(0xffffffffu, key, j);
-            const int32_t ov = __shfl_xor_sync(0xffffffffu, cand, j);
-            const bool up = (lane & k) == 0, lower = (lane & j) == 0;
-            const bool take = (lower == up) ? (ok < key) : (ok > key);
-            if (take) {
-                key = ok;
-                cand = ov;
-            }
-        }
-    }
-}
-
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -331,9 +301,6 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_warp(const double* __r
         int32_t cand = -1;
         const int cnt = warp_candidates32(T, qlo, qhi, lane, cand);
         bool in = false;
-        if (cnt > 1)
-            sort_candidates(T, 0.5f * (qlo[0] + qhi[0]), 0.5f * (qlo[1] + qhi[1]),
-                            0.5f * (qlo[2] + qhi[2]), lane, cnt, cand);
         if (cnt >= 0) {
             for (int k = 0; k < cnt; ++k) {
                 const int32_t lf = __shfl_sync(0xffffffffu, cand, k);
@@ -690,10 +657,7 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
                 if (lane == 0) atomicOr(F.counters + kCntError, 1ULL);
                 cnt = -1;
             }
-            if (cnt > 1)
-                sort_candidates(F.T, (float)((t[0] + t[3]) + t[6]) * (1.0f / 3.0f),
-                                (float)((t[1] + t[4]) + t[7]) * (1.0f / 3.0f),
-                                (float)((t[2] + t[5]) + t[8]) * (1.0f / 3.0f), lane, cnt, cand);
+
         }
         // out iff the lane's sample (have) is out; called by the whole warp
         auto lane_out = [&](bool have, const V3& p) -> bool {
