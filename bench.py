@@ -233,6 +233,17 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
+    if args.only_batching:        # profiling runs of the star-batch pass alone (no line)
+        from tetwild_gb300 import synthetic as syn
+
+        V, F = syn.displaced_sphere(seed=rank)
+        ctx = tw.Context(dev)
+        ctx.set_params(EPS * EPS, EPS)
+        ctx.surface_upload(V, F)
+        r = run_batching(ctx, V, F, args, dev, ws)
+        print(json.dumps({k: r[k] for k in ("stars", "tets", "value", "unit")}), flush=True)
+        ctx.close()
+        return 0
     T, V, F, P = make_inputs(seed=rank)
     ctx = tw.Context(dev)
     ctx.set_params(EPS * EPS, EPS)
@@ -395,7 +406,7 @@ def run_batching(ctx, V, F, args, dev, ws):
     from oracle.oracle import Oracle, default_threads
     from tetwild_gb300 import synthetic as syn
 
-    xyz, off, tets, ff, cen, kinds = syn.mixed_star_batch(V, F, N_STARS, EPS, seed=11,
+    xyz, off, tets, ff, cen, kinds = syn.mixed_star_batch(V, F, args.stars, EPS, seed=11,
                                                           surface_fraction=STAR_SURFACE_FRACTION)
     ns, nt = int(cen.size), int(len(tets))
     sd = EPS / 2
@@ -782,6 +793,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-batching", action="store_true", help="skip the star-batch pass")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving loop")
+    ap.add_argument("--only-batching", action="store_true",
+                    help="profiling: the star-batch pass alone, no benchmark line")
+    ap.add_argument("--stars", type=int, default=N_STARS, help="smaller star batch for profiling only")
     ap.add_argument("--modes", default="plain,cert",
                     help="profiling runs may time one mode only (then no benchmark line)")
     ap.add_argument("--tets", type=int, default=N_TETS, help="smaller case for profiling only")
