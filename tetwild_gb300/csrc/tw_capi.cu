@@ -295,6 +295,11 @@ int tw_set_params(tw_ctx* c, double eps_2, double sampling_dist, int newton_max_
     c->sampling_dist = sampling_dist;
     c->newton_max_step = newton_max_step;
     c->newton_max_it = newton_max_it;
+    Guard g(c->device);
+    for (auto& S : c->surf) {
+        int st = build_env_grid(c, S, eps_2, c->stream);
+        if (st != TW_OK) return st;
+    }
     return TW_OK;
 }
 
@@ -556,6 +561,7 @@ int tw_surface_upload(tw_ctx* c, const double* V, int32_t nv, const int32_t* F, 
     st = build_surface(c, c->surf[which], (const double*)dV, nv, (const int32_t*)dF, nf, c->stream);
     dev_free(c, dV, 24 * (size_t)nv);
     dev_free(c, dF, 12 * (size_t)nf);
+    if (st == TW_OK) st = build_env_grid(c, c->surf[which], c->eps2, c->stream);
     return st;
 }
 

@@ -15,7 +15,10 @@
 // held its previous sample (the reference's prev_facet hint, :1080-1083),
 // and the warp stops at the first sample that is out.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "tw_device.cuh"
@@ -136,6 +139,12 @@ struct EnvTree {
     double scale;
     float scale_hi;  // scale rounded up to binary32
     const int32_t* facet_id;  // input facet index of each leaf
+    // the uniform grid of the certified test (goff == nullptr: none)
+    float glo[3];
+    float ginv;
+    int32_t gn[3];
+    const uint32_t* goff;
+    const int32_t* glist;
 };
 
 template <bool FP32>
@@ -162,9 +171,27 @@ static float round_up_float(double x) {
     float f = (float)x;
     return ((double)f < x) ? std::nextafter(f, INFINITY) : f;
 }
+static EnvTree env_tree(const Surface& S);
+// The tree with its grid when the grid was built for this eps2.
+static EnvTree env_tree_for(const Surface& S, double eps2) {
+    EnvTree T = env_tree(S);
+    if (S.grid.eps2 != eps2) {
+        T.goff = nullptr;
+        T.glist = nullptr;
+    }
+    return T;
+}
 static EnvTree env_tree(const Surface& S) {
-    return EnvTree{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale),
-                   S.facet_id};
+    EnvTree T{S.nodes, S.nodes32, S.cull, S.tri, S.nf, S.scale, round_up_float(S.scale),
+              S.facet_id};
+    for (int k = 0; k < 3; ++k) {
+        T.glo[k] = S.grid.lo[k];
+        T.gn[k] = S.grid.n[k];
+    }
+    T.ginv = S.grid.inv_c;
+    T.goff = S.grid.off;
+    T.glist = S.grid.list;
+    return T;
 }
 
 template <bool FP32, int MINB = 1>
@@ -325,6 +352,125 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_warp(const double* __r
     if (lane == 0 && fallback) atomicAdd(counters + kCntEnvWarpFallback, (unsigned long long)fallback);
 }
 
+// ---------------------------------------------------------------------------
+// Certified test through the uniform grid: the leaves listed in the point's
+// own cell (see EnvGrid) are every leaf within its culling radius, so the
+// point is in iff one of them tests in.  No tree walk; the lanes of a warp
+// loop over their own lists in step.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void grid_cell_range(const EnvTree& T, const CertQuery& q,
+                                                uint32_t& b, uint32_t& e) {
+    int ix[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float t = __fmul_rn(__fsub_rn(q.ph[k], T.glo[k]), T.ginv);
+        int i;
+        if (!(t > 0.0f)) i = 0;
+        else if (t >= (float)T.gn[k]) i = T.gn[k] - 1;
+        else i = min((int)t, T.gn[k] - 1);
+        ix[k] = i;
+    }
+    const int64_t cell = ((int64_t)ix[2] * T.gn[1] + ix[1]) * T.gn[0] + ix[0];
+    b = __ldg(T.goff + cell);
+    e = __ldg(T.goff + cell + 1);
+}
+
+// in iff a leaf of the point's cell tests in; every lane of the warp calls it
+__device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams& E, bool valid,
+                                              const V3& p, const CertQuery& q, TravStats& st) {
+    uint32_t b = 0, e = 0;
+    if (valid) grid_cell_range(T, q, b, e);
+    bool in = false;
+    for (uint32_t k = b; k < e; ++k) {
+        if (cert_leaf_within(T.cull, T.tri, __ldg(T.glist + k), p, q, E.eps2, st)) {
+            in = true;
+            break;
+        }
+    }
+    return in;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __restrict__ P,
+                                                         const int32_t* __restrict__ order,
+                                                         int64_t n, EnvTree T, EpsParams E,
+                                                         uint8_t* __restrict__ out,
+                                                         unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    TravStats st;
+    uint32_t nq = 0;
+    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - (threadIdx.x & 31);
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + (threadIdx.x & 31);
+        if (i < n) {
+            const int64_t j = order ? (int64_t)__ldg(order + i) : i;
+            const V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
+            const CertQuery q = cert_query(p, E, T.scale_hi);
+            out[j] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
+            ++nq;
+        }
+    }
+    flush_stats(st, counters, nq);
+}
+
+// ---- grid build ----------------------------------------------------------------------
+// Sum over facets of the largest box extent (for the cell size).
+__global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
+                                   double* __restrict__ sum) {
+    double acc = 0.0;
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        const double* t = tri + 9 * f;
+        double ext = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double lo = fmin(t[k], fmin(t[3 + k], t[6 + k]));
+            const double hi = fmax(t[k], fmax(t[3 + k], t[6 + k]));
+            ext = fmax(ext, hi - lo);
+        }
+        acc += ext;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+}
+
+// Count (list == nullptr) or fill the cells of every leaf's grown box.  A
+// leaf spanning more than 2^16 cells marks the grid unsuitable (*too_big).
+__global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
+                             double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
+                             double Rm, uint32_t* __restrict__ count,
+                             const uint32_t* __restrict__ off, int32_t* __restrict__ list,
+                             unsigned long long* __restrict__ total, int* __restrict__ too_big) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const double* t = tri + 9 * f;
+    const double lo[3] = {lo0, lo1, lo2};
+    const int32_t n[3] = {n0, n1, n2};
+    int i0[3], i1[3];
+    for (int k = 0; k < 3; ++k) {
+        const double a = fmin(t[k], fmin(t[3 + k], t[6 + k])) - Rm;
+        const double b = fmax(t[k], fmax(t[3 + k], t[6 + k])) + Rm;
+        double u = floor((a - lo[k]) * inv_c), v = floor((b - lo[k]) * inv_c);
+        u = fmin(fmax(u, 0.0), (double)(n[k] - 1));
+        v = fmin(fmax(v, 0.0), (double)(n[k] - 1));
+        i0[k] = (int)u;
+        i1[k] = (int)v;
+    }
+    const int64_t cells = (int64_t)(i1[0] - i0[0] + 1) * (i1[1] - i0[1] + 1) * (i1[2] - i0[2] + 1);
+    if (cells > 65536) {
+        if (too_big) atomicExch(too_big, 1);
+        return;
+    }
+    if (!list) atomicAdd(total, (unsigned long long)cells);
+    for (int z = i0[2]; z <= i1[2]; ++z)
+        for (int y = i0[1]; y <= i1[1]; ++y)
+            for (int x = i0[0]; x <= i1[0]; ++x) {
+                const int64_t cell = ((int64_t)z * n1 + y) * n0 + x;
+                const uint32_t k = atomicAdd(count + cell, 1u);
+                if (list) list[off[cell] + k] = (int32_t)f;
+            }
+}
+
 // 30-bit Morton code of each query point on the tree's centroid grid
 // (points outside the grid clamp to its faces).
 // The order only changes how much work the traversal does, never its
@@ -406,11 +552,14 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
                                         s);
         order = L.idx2;
     }
-    const EnvTree T = env_tree(S);
+    const EnvTree T = env_tree_for(S, eps2);
     const EpsParams E = eps_params(eps2);
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
-    if (precision == TW_PRECISION_FP32_CERTIFIED && order)
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
+        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
+                                                                      counters);
+    else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
         k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
     else if (precision == TW_PRECISION_FP32_CERTIFIED)
@@ -649,7 +798,7 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
         // warp (see k_env_points_warp); -1 when above 32 (per-sample walks)
         int32_t cand = -1;
         int cnt = -1, kh = 0;
-        if (FP32) {
+        if (FP32 && !F.T.goff) {
             float qlo[3], qhi[3];
             face_query_box(t, F, qlo, qhi);
             cnt = warp_candidates32(F.T, qlo, qhi, lane, cand);
@@ -661,6 +810,11 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
         }
         // out iff the lane's sample (have) is out; called by the whole warp
         auto lane_out = [&](bool have, const V3& p) -> bool {
+            if (FP32 && F.T.goff) {
+                CertQuery q;
+                if (have) q = cert_query(p, F.E, F.T.scale_hi);
+                return have && !grid_point_in(F.T, F.E, have, p, q, st);
+            }
             if (cnt < 0) {
                 bool o = false;
                 if (have) o = sample_out<FP32>(F, p, hint, st);
@@ -778,7 +932,7 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
     const int block = 128;
     int64_t warps_needed = n;
     int grid = grid_for(warps_needed * 32, block, 16);
-    FaceCtx F{env_tree(S), eps_params(eps2), counters};
+    FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED) {
         k_env_faces<true><<<grid, block, 0, s>>>(tris, n, F, sd, out);
     } else {
@@ -803,7 +957,7 @@ void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned l
     if (cap <= 0) return;
     const int block = 128;
     int grid = grid_for(cap * 32, block, 16);
-    FaceCtx F{env_tree(S), eps_params(eps2), counters};
+    FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_faces_dev<true><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
     else
@@ -826,7 +980,7 @@ size_t env_seg_bytes() { return sizeof(EnvSeg); }
 void fill_env_seg(void* dst, const Surface& S, int64_t begin, double eps2, double sd) {
     EnvSeg g;
     g.begin = begin;
-    g.T = env_tree(S);
+    g.T = env_tree_for(S, eps2);
     g.E = eps_params(eps2);
     g.sd = sd;
     std::memcpy(dst, &g, sizeof g);
@@ -1045,6 +1199,151 @@ __global__ void k_nearest_points(EnvTree T, const double* __restrict__ P, int64_
         if (D) D[i] = d;
         if (Fo) Fo[i] = f;
     }
+}
+
+void free_env_grid(tw_ctx* c, EnvGrid& G) {
+    if (G.off) dev_free(c, G.off, G.off_bytes);
+    if (G.list) dev_free(c, G.list, G.list_bytes);
+    G = EnvGrid{};
+}
+
+int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s) {
+    if (S.nf <= 0 || !(eps2 >= 0.0)) return TW_OK;
+    if (S.grid.off && S.grid.eps2 == eps2) return TW_OK;
+    free_env_grid(c, S.grid);
+    const int32_t nf = S.nf;
+    // bounding box of the facets: the root's two child boxes, or the facet
+    double blo[3], bhi[3];
+    if (nf > 1) {
+        BvhNode root;
+        cudaMemcpyAsync(&root, S.nodes, sizeof root, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
+        for (int k = 0; k < 3; ++k) {
+            blo[k] = std::min(root.lo0[k], root.lo1[k]);
+            bhi[k] = std::max(root.hi0[k], root.hi1[k]);
+        }
+    } else {
+        double t[9];
+        cudaMemcpyAsync(t, S.tri, sizeof t, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
+        for (int k = 0; k < 3; ++k) {
+            blo[k] = std::min(t[k], std::min(t[3 + k], t[6 + k]));
+            bhi[k] = std::max(t[k], std::max(t[3 + k], t[6 + k]));
+        }
+    }
+    // acc: [0] sum of extents (double), [1] entry total, [2] too-big flag
+    void* acc = nullptr;
+    int st = dev_alloc(c, 32, &acc);
+    if (st != TW_OK) return st;
+    double* d_sum = (double*)acc;
+    unsigned long long* d_total = (unsigned long long*)acc + 1;
+    int* d_big = (int*)((unsigned long long*)acc + 2);
+    cudaMemsetAsync(acc, 0, 32, s);
+    k_grid_mean_extent<<<grid_for(nf, 256, 4), 256, 0, s>>>(S.tri, nf, d_sum);
+    double sum_ext = 0.0;
+    cudaMemcpyAsync(&sum_ext, d_sum, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        dev_free(c, acc, 32);
+        return cuda_fail(c, e, "grid build");
+    }
+    // culling radius of any point of the grown box, plus the cell-index margin
+    const double eps = std::sqrt(eps2);
+    double M = S.scale;
+    for (int k = 0; k < 3; ++k) M = std::max(M, std::max(std::fabs(blo[k]), std::fabs(bhi[k])));
+    M = M + 2.0 * eps + 1e-300;
+    const double Rm = eps * (1.0 + std::ldexp(1.0, -18)) + std::ldexp(M, -17);
+    double cs = std::max(sum_ext / nf, 2.0 * Rm);
+    int64_t n[3];
+    float lo[3];
+    float inv = 0.0f;
+    for (int iter = 0; iter < 64; ++iter) {
+        inv = (float)(1.0 / cs);
+        int64_t cells = 1;
+        for (int k = 0; k < 3; ++k) {
+            const double a = blo[k] - Rm;
+            float f = (float)a;
+            if ((double)f > a) f = std::nextafter(f, -INFINITY);
+            lo[k] = f;
+            n[k] = (int64_t)std::floor((bhi[k] + Rm - (double)f) * (double)inv) + 2;
+            cells *= n[k];
+        }
+        if (cells <= (int64_t(1) << 24)) break;
+        cs *= 1.25;
+    }
+    const int64_t ncells = n[0] * n[1] * n[2];
+    if (ncells > (int64_t(1) << 24)) {  // no grid: the tree walk serves the queries
+        dev_free(c, acc, 32);
+        return TW_OK;
+    }
+    void *cnt = nullptr, *off = nullptr, *temp = nullptr;
+    size_t temp_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, temp_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                  (int)(ncells + 1), s);
+    const size_t off_bytes = 4 * (size_t)(ncells + 1);
+    if ((st = dev_alloc(c, off_bytes, &cnt)) != TW_OK) {
+        dev_free(c, acc, 32);
+        return st;
+    }
+    if ((st = dev_alloc(c, off_bytes, &off)) != TW_OK) {
+        dev_free(c, cnt, off_bytes);
+        dev_free(c, acc, 32);
+        return st;
+    }
+    if ((st = dev_alloc(c, temp_bytes + 16, &temp)) != TW_OK) {
+        dev_free(c, cnt, off_bytes);
+        dev_free(c, off, off_bytes);
+        dev_free(c, acc, 32);
+        return st;
+    }
+    const int B = 256;
+    const int G = (int)((nf + B - 1) / B);
+    cudaMemsetAsync(cnt, 0, off_bytes, s);
+    k_grid_cells<<<G, B, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                 (int32_t)n[1], (int32_t)n[2], Rm, (uint32_t*)cnt, nullptr, nullptr,
+                                 d_total, d_big);
+    cub::DeviceScan::ExclusiveSum(temp, temp_bytes, (const uint32_t*)cnt, (uint32_t*)off,
+                                  (int)(ncells + 1), s);
+    unsigned long long hacc[2] = {0, 0};
+    cudaMemcpyAsync(hacc, d_total, 16, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    dev_free(c, temp, temp_bytes + 16);
+    dev_free(c, acc, 32);
+    const unsigned long long total = hacc[0];
+    const bool unsuitable = (hacc[1] & 0xffffffffULL) != 0 || total > (1ULL << 28);
+    void* list = nullptr;
+    if (e == cudaSuccess && !unsuitable) st = dev_alloc(c, 4 * (size_t)total + 16, &list);
+    if (e != cudaSuccess || st != TW_OK || unsuitable) {
+        dev_free(c, cnt, off_bytes);
+        dev_free(c, off, off_bytes);
+        if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
+        return unsuitable ? TW_OK : st;   // unsuitable: the tree walk serves the queries
+    }
+    cudaMemsetAsync(cnt, 0, off_bytes, s);
+    k_grid_cells<<<G, B, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                 (int32_t)n[1], (int32_t)n[2], Rm, (uint32_t*)cnt,
+                                 (const uint32_t*)off, (int32_t*)list, nullptr, nullptr);
+    e = cudaStreamSynchronize(s);
+    dev_free(c, cnt, off_bytes);
+    if (e != cudaSuccess) {
+        dev_free(c, off, off_bytes);
+        dev_free(c, list, 4 * (size_t)total + 16);
+        return cuda_fail(c, e, "grid build");
+    }
+    EnvGrid& g = S.grid;
+    for (int k = 0; k < 3; ++k) {
+        g.lo[k] = lo[k];
+        g.n[k] = (int32_t)n[k];
+    }
+    g.inv_c = inv;
+    g.off = (uint32_t*)off;
+    g.list = (int32_t*)list;
+    g.eps2 = eps2;
+    g.off_bytes = off_bytes;
+    g.list_bytes = 4 * (size_t)total + 16;
+    return TW_OK;
 }
 
 void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,

@@ -55,6 +55,23 @@ struct alignas(16) FacetCull {
 };
 static_assert(sizeof(FacetCull) == 128, "FacetCull must be 128 bytes");
 
+// Uniform grid over the surface for the certified envelope test: cell size c
+// (the same on every axis), origin lo; cell (i, j, k) lists every leaf whose
+// box, grown by R = eps (1 + 2^-18) + 2^-17 M (M = the largest coordinate
+// magnitude of the grown box), meets the cell.  Any point within the
+// certified culling radius of a leaf finds that leaf in the list of its own
+// cell (the margin covers the binary32 cell index), so one cell's list
+// replaces the tree walk.  Built for one eps2 (rebuilt when it changes).
+struct EnvGrid {
+    float lo[3] = {0, 0, 0};
+    float inv_c = 0.0f;
+    int32_t n[3] = {0, 0, 0};
+    uint32_t* off = nullptr;   // n0 n1 n2 + 1 offsets into list
+    int32_t* list = nullptr;   // leaf indices
+    double eps2 = -1.0;        // the eps2 it was built for (-1: none)
+    size_t off_bytes = 0, list_bytes = 0;
+};
+
 struct Surface {
     int32_t nf = 0;
     BvhNode* nodes = nullptr;   // nf-1 internal nodes (none when nf == 1)
@@ -66,6 +83,7 @@ struct Surface {
     double lo[3] = {0, 0, 0};   // box of the facet centroids (Morton grid of the tree;
     double hi[3] = {0, 0, 0};   // query points are ordered on the same grid)
     size_t bytes = 0;
+    EnvGrid grid;
 };
 
 // Device scratch for ordering query points along the Morton curve before
@@ -152,6 +170,9 @@ void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, co
 int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int32_t* dF,
                   int32_t nf, cudaStream_t s);
 void free_surface(tw_ctx* c, Surface& S);
+// (Re)builds S.grid for eps2 when it was built for another one (tw_envelope.cu).
+int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s);
+void free_env_grid(tw_ctx* c, EnvGrid& G);
 
 // ---- launchers (tw_envelope.cu) ----
 // err: device word; bit 0 = traversal exceeded its bounds, bit 1 = a face

@@ -268,6 +268,7 @@ __global__ void k_facet_cull(const double* __restrict__ tri, int32_t nf,
 }
 
 void free_surface(tw_ctx* c, Surface& S) {
+    free_env_grid(c, S.grid);
     const size_t ni = (size_t)(S.nf > 1 ? S.nf - 1 : 1);
     if (S.nodes) dev_free(c, S.nodes, sizeof(BvhNode) * ni);
     if (S.nodes32) dev_free(c, S.nodes32, sizeof(BvhNode32) * ni);
