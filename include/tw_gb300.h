@@ -268,6 +268,57 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
                                   const uint8_t* kinds, int32_t nstars, int64_t ntets, double* out,
                                   uint8_t* status);
 
+/* ---- tuning knobs (work only, never results) ---------------------------------------
+ * TW_TUNE_GRID_CELL: cell size of the certified envelope grid as a multiple
+ *   of the mean facet extent (default 0.25; the grid is rebuilt).
+ * TW_TUNE_SORT_POINTS: 1 (default) orders point queries along the Morton
+ *   curve before the certified test, 0 keeps the caller's order.
+ * No counterpart in the reference.                                          */
+#define TW_TUNE_GRID_CELL 0
+#define TW_TUNE_SORT_POINTS 1
+TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
+
+/* ---- energy sweeps -------------------------------------------------------------------
+ * Replaces: LocalOperations::getAvgMaxEnergy, getMaxEnergy, getSecondMaxEnergy
+ * and the histogram of getFilterEnergy (LocalOperations.cpp:605-693, decl
+ * LocalOperations.h:103-107) over tets (ids into the resident mesh: the tets
+ * that are not removed) with calTetQuality_AMIPS at the resident positions.
+ * locked[i] != 0 (NULL: none) excludes tet i from avg / max / second max
+ * (isTetLocked_ui).  avg is the mean over the unlocked tets (MAX_ENERGY when
+ * the sum overflows) from a double-double sum: within a few ulps of the
+ * exact mean, where the reference's sequential sum may differ from it by
+ * n ulps.  buckets[11]: getFilterEnergy's counts; tw_filter_energy applies
+ * its rule to them.                                                        */
+TW_API int tw_energy_stats(tw_ctx* ctx, const int32_t* tets, int64_t n, const uint8_t* locked,
+                           double filter_energy_thres, double* avg, double* max_e,
+                           double* second_max, int64_t* buckets);
+TW_API double tw_filter_energy(const int64_t* buckets, double filter_energy_thres,
+                               int* is_clean_up);
+
+/* ---- edge-collapse checks ------------------------------------------------------------
+ * Replaces: the checks of EdgeCollapser::collapseAnEdge (EdgeCollapser.cpp:
+ * 284-446, decl EdgeCollapser.h:31) with isCollapsable_epsilon (:727-775)
+ * for a batch of candidate collapses v12[i] = (v1, v2) against the resident
+ * mesh (checks only; the caller applies the successful ones).  Star i =
+ * conn_tets of v1 (tets[off[i]..off[i+1]), caller order), face_flags per tet
+ * as for tw_smooth_stars; flags[i] = TW_CV_* of the two vertices (after the
+ * reference's isIsolated / isBoundaryPoint updates).  check_quality =
+ * is_check_quality; soft_energy >= 0 replaces the old energy (is_soft).
+ * result[i] = TW_COLLAPSE_SUCCESS / _FLIP / _QUALITY / _ENVELOP (the
+ * reference's codes, EdgeCollapser.h:52-55).                               */
+#define TW_CV_V1_SURFACE 1
+#define TW_CV_V1_BOUNDARY 2
+#define TW_CV_V2_SURFACE 4
+#define TW_CV_V2_BOUNDARY 8
+#define TW_CV_V1_UNROUNDED 16
+#define TW_COLLAPSE_SUCCESS 0
+#define TW_COLLAPSE_FLIP 1
+#define TW_COLLAPSE_QUALITY 2
+#define TW_COLLAPSE_ENVELOP 3
+TW_API int tw_collapse_check(tw_ctx* ctx, const int32_t* v12, const uint8_t* flags,
+                             const int32_t* off, const int32_t* tets, const uint8_t* face_flags,
+                             int32_t n, int check_quality, double soft_energy, uint8_t* result);
+
 /* ---- CUDA graphs of the context stream -------------------------------------------
  * Capture the _device calls issued between begin and end into an executable
  * graph and replay it with one launch (the inputs are re-read from the same

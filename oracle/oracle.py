@@ -88,6 +88,10 @@ class Oracle:
             "two_smooth_star": ([_P, _P, _P, _I32, _I32, _I, _P, _P, _D, _D, _I, _I, _P], _I),
             "two_smooth_stars_batch": ([_P, _P, _P, _P, _P, _P, _I64, _P, _P, _D, _D, _I, _I, _P,
                                         _P, _I], None),
+            "two_collapse_check_batch": ([_P, _P, _P, _P, _P, _P, _I64, _P, _P, _D, _D, _I, _D,
+                                          _P, _I], None),
+            "two_energy_stats": ([_P, _P, _I64, _P, _D, _P, _P, _P, _P], None),
+            "two_filter_energy": ([_P, _D, _P], _D),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -177,6 +181,44 @@ class Oracle:
                                       boundary.h if boundary is not None else None,
                                       eps2, sd, max_step, max_it, _p(out), _p(st), nthreads)
         return out, st
+
+
+    def collapse_check(self, xyz, off, tets, face_flags, v12, flags, surface=None,
+                       boundary=None, eps2=0.0, sd=0.0, check_quality=True, soft_energy=-1.0,
+                       nthreads=1):
+        """Checks of candidate collapses v12[i] = (v1, v2) (two_collapse_check): codes [n]."""
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        O = _c(off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        FF = _c(face_flags, np.uint8)
+        V = _c(v12, np.int32).reshape(-1, 2)
+        FL = _c(flags, np.uint8)
+        n = V.shape[0]
+        out = np.empty(n, np.uint8)
+        self.L.two_collapse_check_batch(_p(X), _p(O), _p(T), _p(FF), _p(V), _p(FL), n,
+                                        surface.h if surface is not None else None,
+                                        boundary.h if boundary is not None else None, eps2, sd,
+                                        1 if check_quality else 0, soft_energy, _p(out), nthreads)
+        return out
+
+
+    def energy_stats(self, xyz, tets, locked=None, thres=10.0):
+        """(avg, max, second max, buckets[11]) of getAvgMaxEnergy / getMaxEnergy /
+        getSecondMaxEnergy / getFilterEnergy's histogram."""
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        L = None if locked is None else _c(locked, np.uint8)
+        a, m, m2 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        b = np.zeros(11, np.int64)
+        self.L.two_energy_stats(_p(X), _p(T), T.shape[0], _p(L), thres, ctypes.byref(a),
+                                ctypes.byref(m), ctypes.byref(m2), _p(b))
+        return a.value, m.value, m2.value, b
+
+    def filter_energy(self, buckets, thres=10.0):
+        b = _c(buckets, np.int64)
+        c = ctypes.c_int()
+        e = self.L.two_filter_energy(_p(b), thres, ctypes.byref(c))
+        return e, bool(c.value)
 
 
 class OracleSurface:

@@ -1196,6 +1196,167 @@ int two_smooth_star(const double* xyz, const int32_t* tets, const uint8_t* fflag
 }
 
 /* =========================================================================
+ * The checks of one edge collapse v1 -> v2 (EdgeCollapser::collapseAnEdge,
+ * EdgeCollapser.cpp:284-446, with isCollapsable_epsilon :727-775), with
+ * isBoundarySlide returning false (LocalOperations.cpp:1123-1124), energy
+ * AMIPS with use_energy_max (State.h:53), the stored qualities equal to
+ * calTetQuality at the current positions, and the caller's vertex flags
+ * already updated by isIsolated / isBoundaryPoint (:299-308).  tets: the
+ * conn_tets of v1 (caller order); fflags as for two_smooth_star.  Returns
+ * SUCCESS 0, FLIP 1, QUALITY 2 or ENVELOP 3 (EdgeCollapser.h:52-55).
+ *   1. degenerate edge: |v1 - v2| == 0 (skips the envelope and quality tests);
+ *   2. v1 on the boundary, v2 not: v2 out of the boundary envelope -> ENVELOP;
+ *      v1 on the surface, v2 not: v2 out of the envelope -> ENVELOP;
+ *   3. new tets (those without v2, v1 replaced by v2) not all POSITIVE -> FLIP;
+ *   4. check_quality: old max (soft_energy >= 0: soft_energy), new max (0 for
+ *      an unrounded v1); new > old -> QUALITY;
+ *   5. v1 on the surface: the surface faces through v1 (sorted triples without
+ *      repeats) not through v2, v1 replaced by v2 in place, each out of the
+ *      envelope -> ENVELOP.
+ * ========================================================================= */
+int two_collapse_check(const double* xyz, const int32_t* tets, const uint8_t* fflags, int32_t nt,
+                       int32_t v1, int32_t v2, int flags, const two_surface* s_in,
+                       const two_surface* s_b, double eps2, double sd, int check_quality,
+                       double soft_energy)
+{
+    const double* p1 = xyz + 3 * (size_t)v1;
+    const double* p2 = xyz + 3 * (size_t)v2;
+    double dx = p1[0] - p2[0], dy = p1[1] - p2[1], dz = p1[2] - p2[2];
+    const int degenerate = sqrt(dx * dx + dy * dy + dz * dz) == 0.0;
+    if ((flags & TWO_CV_V1_BOUNDARY) && !(flags & TWO_CV_V2_BOUNDARY) && !degenerate)
+        if (!s_b || two_point_out(s_b, p2, eps2)) return 3;
+    if ((flags & TWO_CV_V1_SURFACE) && !(flags & TWO_CV_V2_SURFACE) && !degenerate)
+        if (!s_in || two_point_out(s_in, p2, eps2)) return 3;
+    double T[12];
+    for (int32_t i = 0; i < nt; ++i) {
+        const int32_t* t = tets + 4 * i;
+        if (t[0] == v2 || t[1] == v2 || t[2] == v2 || t[3] == v2) continue;
+        tw_gather(xyz, t, v1, p2, 0, T);
+        if (two_orient3d(T, T + 3, T + 6, T + 9) != 1) return 1;
+    }
+    if (check_quality) {
+        double old_max = 0.0, new_max = 0.0;
+        for (int32_t i = 0; i < nt; ++i) {
+            const int32_t* t = tets + 4 * i;
+            tw_gather(xyz, t, v1, p1, 0, T);
+            double e = two_tet_quality(T);
+            if (e > old_max) old_max = e;
+            if (t[0] == v2 || t[1] == v2 || t[2] == v2 || t[3] == v2) continue;
+            tw_gather(xyz, t, v1, p2, 0, T);
+            e = two_tet_quality(T);
+            if (e > new_max) new_max = e;
+        }
+        if (soft_energy >= 0.0) old_max = soft_energy;
+        if (flags & TWO_CV_V1_UNROUNDED) new_max = 0.0;
+        if (!degenerate && !(new_max <= old_max)) return 2;
+    }
+    if ((flags & TWO_CV_V1_SURFACE) && !degenerate) {
+        for (int32_t i = 0; i < nt; ++i) {
+            const int32_t* t = tets + 4 * i;
+            for (int j = 0; j < 4; ++j) {
+                if (t[j] == v1 || !((fflags[i] >> j) & 1)) continue;
+                int32_t key[3] = {t[(j + 1) % 4], t[(j + 2) % 4], t[(j + 3) % 4]};
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2 - a; ++b)
+                        if (key[b] > key[b + 1]) { int32_t x = key[b]; key[b] = key[b + 1]; key[b + 1] = x; }
+                int seen = 0;
+                for (int32_t i2 = 0; i2 <= i && !seen; ++i2) {
+                    const int32_t* t2 = tets + 4 * i2;
+                    for (int j2 = 0; j2 < 4 && !seen; ++j2) {
+                        if (i2 == i && j2 >= j) break;
+                        if (t2[j2] == v1 || !((fflags[i2] >> j2) & 1)) continue;
+                        int32_t k2[3] = {t2[(j2 + 1) % 4], t2[(j2 + 2) % 4], t2[(j2 + 3) % 4]};
+                        for (int a = 0; a < 2; ++a)
+                            for (int b = 0; b < 2 - a; ++b)
+                                if (k2[b] > k2[b + 1]) { int32_t x = k2[b]; k2[b] = k2[b + 1]; k2[b + 1] = x; }
+                        seen = (tw_tri_key_cmp(key, k2) == 0);
+                    }
+                }
+                if (seen) continue;
+                if (key[0] == v2 || key[1] == v2 || key[2] == v2) continue;
+                double tri[9];
+                for (int k = 0; k < 3; ++k) {
+                    const double* q = (key[k] == v1) ? p2 : xyz + 3 * (size_t)key[k];
+                    tri[3 * k] = q[0];
+                    tri[3 * k + 1] = q[1];
+                    tri[3 * k + 2] = q[2];
+                }
+                if (!s_in || two_face_out(s_in, tri, eps2, sd)) return 3;
+            }
+        }
+    }
+    return 0;
+}
+
+/* =========================================================================
+ * Energy sweeps over a tet list (LocalOperations.cpp:605-693) on qualities
+ * computed by calTetQuality_AMIPS at the current positions; the list holds
+ * the tets that are not removed.  avg / max over the tets with no locked
+ * vertex (locked[i] != 0 marks one, NULL: none), avg sequential in list
+ * order (MAX_ENERGY when it overflows); second max also skips MAX_ENERGY;
+ * buckets of getFilterEnergy over every tet.
+ * ========================================================================= */
+void two_energy_stats(const double* xyz, const int32_t* tets, int64_t n, const uint8_t* locked,
+                      double thres, double* avg, double* max_e, double* second_max,
+                      int64_t buckets[11])
+{
+    double sum = 0.0, mx = 0.0, mx2 = 0.0;
+    int64_t cnt = 0;
+    static const double p10[11] = {1.0, 1e1, 1e2, 1e3, 1e4, 1e5, 1e6, 1e7, 1e8, 1e9, 1e10};
+    for (int k = 0; k < 11; ++k) buckets[k] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double T[12];
+        for (int j = 0; j < 4; ++j) {
+            const double* src = xyz + 3 * (size_t)tets[4 * i + j];
+            T[3 * j] = src[0];
+            T[3 * j + 1] = src[1];
+            T[3 * j + 2] = src[2];
+        }
+        const double e = two_tet_quality(T);
+        if (e > thres - 1 + 1e10) {
+            buckets[10]++;
+        } else {
+            for (int j = 0; j < 10; ++j)
+                if (e > thres - 1 + p10[j] && e <= thres - 1 + p10[j + 1]) {
+                    buckets[j]++;
+                    break;
+                }
+        }
+        if (locked && locked[i]) continue;
+        if (e > mx) mx = e;
+        if (e != TWO_MAX_ENERGY && e > mx2) mx2 = e;
+        sum += e;
+        cnt++;
+    }
+    double a = sum / (double)cnt;
+    if (isinf(a)) a = TWO_MAX_ENERGY;
+    *avg = a;
+    *max_e = mx;
+    *second_max = mx2;
+}
+
+/* getFilterEnergy's choice over the buckets (LocalOperations.cpp:674-692). */
+double two_filter_energy(const int64_t buckets[11], double thres, int* is_clean_up)
+{
+    int64_t t1[10], t2[10];
+    for (int i = 0; i < 10; ++i) {
+        t1[i] = 0;
+        t2[i] = 0;
+        for (int k = 0; k <= i; ++k) t1[i] += buckets[k];
+        for (int k = i + 1; k < 11; ++k) t2[i] += buckets[k];
+    }
+    *is_clean_up = 0;
+    if (t1[0] >= t2[0]) {
+        *is_clean_up = t2[5] > 0;
+        return 8;
+    }
+    if (t1[8] <= t2[8]) return 1e11;
+    for (int i = 0; i < 8; ++i)
+        if (t1[i] < t2[i] && t1[i + 1] > t2[i + 1]) return thres - 1 + 5 * pow(10, i + 1);
+    return 8;
+}
+
+/* =========================================================================
  * Threaded batch drivers.
  * ========================================================================= */
 typedef struct {
@@ -1209,7 +1370,7 @@ typedef struct {
     const void* a5;
     const void* a6;
     const void* a7;
-    double d0, d1;
+    double d0, d1, d2;
     int i0, i1, i2;
     void* o0;
     void* o1;
@@ -1307,10 +1468,28 @@ static void tw_run_nearest(tw_job* j)
         if (F) F[i] = f;
     }
 }
+static void tw_run_collapse(tw_job* j)
+{
+    const double* xyz = (const double*)j->a0;
+    const int32_t* off = (const int32_t*)j->a1;
+    const int32_t* tets = (const int32_t*)j->a2;
+    const int32_t* v12 = (const int32_t*)j->a3;
+    const uint8_t* ff = (const uint8_t*)j->a4;
+    const uint8_t* fl = (const uint8_t*)j->a5;
+    uint8_t* res = (uint8_t*)j->o0;
+    for (int64_t i = j->lo; i < j->hi; ++i) {
+        int32_t b = off[i], e = off[i + 1];
+        res[i] = (uint8_t)two_collapse_check(xyz, tets + 4 * (size_t)b, ff + b, e - b, v12[2 * i],
+                                             v12[2 * i + 1], fl[i], (const two_surface*)j->a6,
+                                             (const two_surface*)j->a7, j->d0, j->d1, j->i0,
+                                             j->d2);
+    }
+}
 static void* tw_thread_main(void* arg)
 {
     tw_job* j = (tw_job*)arg;
     switch (j->kind) {
+    case 6: tw_run_collapse(j); break;
     case 0: tw_run_amips(j); break;
     case 1: tw_run_points(j); break;
     case 2: tw_run_faces(j); break;
@@ -1437,5 +1616,30 @@ void two_nearest_batch(const two_surface* s, const double* P, int64_t n, double*
     j.o0 = Q;
     j.o1 = D;
     j.o2 = F;
+    tw_parallel(j, n, nthreads);
+}
+
+void two_collapse_check_batch(const double* xyz, const int32_t* off, const int32_t* tets,
+                              const uint8_t* fflags, const int32_t* v12, const uint8_t* flags,
+                              int64_t n, const two_surface* s_in, const two_surface* s_b,
+                              double eps2, double sd, int check_quality, double soft_energy,
+                              uint8_t* result, int nthreads)
+{
+    tw_job j;
+    memset(&j, 0, sizeof j);
+    j.kind = 6;
+    j.a0 = xyz;
+    j.a1 = off;
+    j.a2 = tets;
+    j.a3 = v12;
+    j.a4 = fflags;
+    j.a5 = flags;
+    j.a6 = s_in;
+    j.a7 = s_b;
+    j.d0 = eps2;
+    j.d1 = sd;
+    j.d2 = soft_energy;
+    j.i0 = check_quality;
+    j.o0 = result;
     tw_parallel(j, n, nthreads);
 }

@@ -100,6 +100,23 @@ int two_smooth_star(const double* xyz, const int32_t* tets, const uint8_t* fflag
                     int32_t v, int kind, const two_surface* s_in, const two_surface* s_b,
                     double eps2, double sampling_dist, int max_step, int max_it, double out[3]);
 
+/* ---- checks of one edge collapse (EdgeCollapser.cpp:284-446, :727-775) --- */
+#define TWO_CV_V1_SURFACE 1
+#define TWO_CV_V1_BOUNDARY 2
+#define TWO_CV_V2_SURFACE 4
+#define TWO_CV_V2_BOUNDARY 8
+#define TWO_CV_V1_UNROUNDED 16
+int two_collapse_check(const double* xyz, const int32_t* tets, const uint8_t* fflags, int32_t ntets,
+                       int32_t v1, int32_t v2, int flags, const two_surface* s_in,
+                       const two_surface* s_b, double eps2, double sampling_dist,
+                       int check_quality, double soft_energy);
+
+/* ---- energy sweeps (LocalOperations.cpp:605-693) ------------------------- */
+void two_energy_stats(const double* xyz, const int32_t* tets, int64_t n, const uint8_t* locked,
+                      double filter_energy_thres, double* avg, double* max_e,
+                      double* second_max, int64_t buckets[11]);
+double two_filter_energy(const int64_t buckets[11], double filter_energy_thres, int* is_clean_up);
+
 /* ---- batch drivers (pthreads; nthreads <= 0 means 1) --------------------- */
 /* T is SoA [12][n] (the energy_ispc layout).  Any output may be NULL.       *
  * J and H are SoA ([3][n], [9][n]).  flip[i] = two_tet_flip; E[i] is the    *
@@ -121,6 +138,11 @@ void two_smooth_stars_batch(const double* xyz, const int32_t* star_off, const in
                             double* out, int8_t* status, int nthreads);
 void two_nearest_batch(const two_surface* s, const double* P, int64_t n, double* Q, double* D,
                        int32_t* F, int nthreads);
+void two_collapse_check_batch(const double* xyz, const int32_t* off, const int32_t* tets,
+                              const uint8_t* fflags, const int32_t* v12, const uint8_t* flags,
+                              int64_t n, const two_surface* s_in, const two_surface* s_b,
+                              double eps2, double sampling_dist, int check_quality,
+                              double soft_energy, uint8_t* result, int nthreads);
 
 #ifdef __cplusplus
 }

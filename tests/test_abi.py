@@ -4,6 +4,8 @@ import ctypes
 import re
 import subprocess
 
+import numpy as np
+
 import pytest
 
 from conftest import ROOT
@@ -13,7 +15,7 @@ HEADER = ROOT / "include" / "tw_gb300.h"
 
 def declared_symbols():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^TW_API\s+(?:const\s+char\*|int)\s+(tw_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^TW_API\s+(?:const\s+char\*|int|double)\s+(tw_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -80,3 +82,20 @@ def test_synthetic_shapes():
     xyz, off, tets, cen = syn.star_batch(20, seed=0)
     n = off[1:] - off[:-1]
     assert n.min() >= 4 and n.max() <= 96 and len(cen) == 20
+
+
+def test_filter_energy_rule_matches_oracle(oracle):
+    """tw_filter_energy is host code: its choice over bucket histograms equals
+    the oracle's restatement of getFilterEnergy (LocalOperations.cpp:674-692)."""
+    import tetwild_gb300 as tw
+
+    rng = np.random.default_rng(0)
+    lib = tw.load_library()
+    for _ in range(2000):
+        b = np.zeros(11, np.int64)
+        k = rng.integers(1, 11)
+        b[rng.choice(11, k, replace=False)] = rng.integers(0, 50, k)
+        for thres in (10.0, 8.0):
+            c = ctypes.c_int()
+            e = lib.tw_filter_energy(b.ctypes.data, thres, ctypes.byref(c))
+            assert (e, bool(c.value)) == oracle.filter_energy(b, thres)

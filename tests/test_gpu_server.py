@@ -160,7 +160,7 @@ def test_server_matches_single_job_entry_points(workload, oracle):
 
 def test_admission_against_the_budget():
     V, F = syn.displaced_sphere(seed=4, n_lon=250, n_rings=100)   # ~50k facets
-    budget = 40 << 20   # one job (~20 MB resident, ~26 MB estimated) fits, two do not
+    budget = 160 << 20   # one job (~137 MB estimated, ~115 MB resident) fits, two do not
     with tw.Server(0, budget, lanes=1) as srv:
         a = srv.job_open(V, F, 1e-6, 5e-4)
         assert a is not None

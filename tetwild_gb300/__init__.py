@@ -41,6 +41,11 @@ TW_REQ_AMIPS = 2
 TW_REQ_SMOOTH = 3
 TW_REQ_RAW = 1
 TW_REQ_APPLY = 2
+TW_CV_V1_SURFACE = 1
+TW_CV_V1_BOUNDARY = 2
+TW_CV_V2_SURFACE = 4
+TW_CV_V2_BOUNDARY = 8
+TW_CV_V1_UNROUNDED = 16
 TW_STAR_INTERIOR = 0
 TW_STAR_SURFACE = 1
 TW_STAR_BOUNDARY = 2
@@ -124,9 +129,13 @@ _SIGS = {
     "tw_newton_stars": [_P, _P, _P, _P, _I32, _P, _P],
     "tw_newton_stars_device": [_P, _P, _P, _P, _I32, _P, _P],
     "tw_set_newton_shape": [_P, _I],
+    "tw_set_tuning": [_P, _I, _D],
     "tw_nearest_points": [_P, _P, _I64, _I, _P, _P, _P],
     "tw_nearest_points_device": [_P, _P, _I64, _I, _P, _P, _P],
     "tw_smooth_stars": [_P, _P, _P, _P, _P, _P, _I32, _P, _P],
+    "tw_collapse_check": [_P, _P, _P, _P, _P, _P, _I32, _I, _D, _P],
+    "tw_energy_stats": [_P, _P, _I64, _P, _D, _P, _P, _P, _P],
+    "tw_filter_energy": [_P, _D, _P],
     "tw_smooth_stars_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P],
     "tw_smooth_autotune_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P, ctypes.POINTER(_I),
                                   ctypes.POINTER(ctypes.c_float)],
@@ -170,7 +179,8 @@ def load_library() -> ctypes.CDLL:
     for name, args in _SIGS.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name.endswith("last_error") else _I
+        fn.restype = (ctypes.c_char_p if name.endswith("last_error")
+                      else _D if name == "tw_filter_energy" else _I)
     _LIB = lib
     return lib
 
@@ -361,6 +371,12 @@ class Context:
                                                     out_ptr, moved_ptr))
 
     NEWTON_SHAPES = 10
+    TUNE_GRID_CELL = 0
+    TUNE_SORT_POINTS = 1
+
+    def set_tuning(self, knob: int, value: float):
+        """Work-only knobs (TW_TUNE_*): results are the same for every value."""
+        self._check(self.lib.tw_set_tuning(self.h, knob, value))
 
     # -- smoothing pass ------------------------------------------------------------------
     def smooth_stars(self, star_off, tets, centers, face_flags=None, kinds=None):
@@ -393,6 +409,40 @@ class Context:
                                                        centers_ptr, kinds_ptr, nstars, ntets,
                                                        out_ptr, status_ptr, ctypes.byref(best), ms))
         return int(best.value), [float(x) for x in ms]
+
+    # -- energy sweeps -------------------------------------------------------------------
+    def energy_stats(self, tets, locked=None, filter_energy_thres=10.0):
+        """(avg, max, second max, buckets[11]) over tets of the resident mesh."""
+        T = _c(tets, np.int32).reshape(-1, 4)
+        L = None if locked is None else _c(locked, np.uint8)
+        a, m, m2 = _D(), _D(), _D()
+        b = np.zeros(11, np.int64)
+        self._check(self.lib.tw_energy_stats(self.h, _ptr(T), T.shape[0], _ptr(L),
+                                             filter_energy_thres, ctypes.byref(a), ctypes.byref(m),
+                                             ctypes.byref(m2), _ptr(b)))
+        return a.value, m.value, m2.value, b
+
+    def filter_energy(self, buckets, filter_energy_thres=10.0):
+        b = _c(buckets, np.int64)
+        c = _I()
+        e = self.lib.tw_filter_energy(_ptr(b), filter_energy_thres, ctypes.byref(c))
+        return e, bool(c.value)
+
+    # -- edge-collapse checks -----------------------------------------------------------
+    def collapse_check(self, v12, flags, star_off, tets, face_flags, check_quality=True,
+                       soft_energy=-1.0):
+        """Checks of candidate collapses (EdgeCollapser::collapseAnEdge): codes [n]."""
+        V = _c(v12, np.int32).reshape(-1, 2)
+        FL = _c(flags, np.uint8)
+        O = _c(star_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        FF = _c(face_flags, np.uint8)
+        n = V.shape[0]
+        out = np.empty(n, np.uint8)
+        self._check(self.lib.tw_collapse_check(self.h, _ptr(V), _ptr(FL), _ptr(O), _ptr(T),
+                                               _ptr(FF), n, 1 if check_quality else 0,
+                                               soft_energy, _ptr(out)))
+        return out
 
     # -- nearest facet -----------------------------------------------------------------
     def nearest_points(self, P, which=TW_SURFACE_INPUT):

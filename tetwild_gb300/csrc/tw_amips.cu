@@ -245,4 +245,114 @@ void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, co
         counters);
 }
 
+
+// ---------------------------------------------------------------------------
+// Energy sweeps (LocalOperations.cpp:605-693): per tet the calTetQuality_AMIPS
+// value at the resident positions; max and second max (skipping MAX_ENERGY)
+// over the unlocked tets as the largest bit pattern of a non-negative double
+// (order-free, exact); the sum of the unlocked energies as a double-double
+// per thread, per block (fixed tree) and over the blocks in block order
+// (deterministic, within a few ulps of the exact sum); getFilterEnergy's
+// eleven bucket counts over every tet.
+// ---------------------------------------------------------------------------
+struct DD {
+    double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+    double s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    double h, l;
+    fast_two_sum(s, e, h, l);
+    return DD{h, l};
+}
+
+constexpr int kStatsBlock = 256;
+
+__global__ void __launch_bounds__(kStatsBlock) k_energy_stats(
+    const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,
+    const double* __restrict__ vy, const double* __restrict__ vz,
+    const uint8_t* __restrict__ locked, double thres_m1, DD* __restrict__ block_sum,
+    unsigned long long* __restrict__ acc) {
+    // acc: [0] max bits, [1] second-max bits, [2] unlocked count, [3..13] buckets
+    __shared__ unsigned long long sb[11];
+    __shared__ DD ssum[kStatsBlock / 32];
+    if (threadIdx.x < 11) sb[threadIdx.x] = 0;
+    __syncthreads();
+    DD sum{0.0, 0.0};
+    unsigned long long mx = 0, mx2 = 0, cnt = 0;
+    const double p10[11] = {1.0, 1e1, 1e2, 1e3, 1e4, 1e5, 1e6, 1e7, 1e8, 1e9, 1e10};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int4 tv = __ldg(tets + i);
+        const int id[4] = {tv.x, tv.y, tv.z, tv.w};
+        double t[12];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            t[3 * j] = __ldg(vx + id[j]);
+            t[3 * j + 1] = __ldg(vy + id[j]);
+            t[3 * j + 2] = __ldg(vz + id[j]);
+        }
+        const double e = quality_from(orient3d(t, t + 3, t + 6, t + 9), amips_energy(t));
+        int bk = -1;
+        if (e > thres_m1 + 1e10) {
+            bk = 10;
+        } else {
+            for (int j = 0; j < 10; ++j)
+                if (e > thres_m1 + p10[j] && e <= thres_m1 + p10[j + 1]) {
+                    bk = j;
+                    break;
+                }
+        }
+        if (bk >= 0) atomicAdd(&sb[bk], 1ULL);
+        if (locked && __ldg(locked + i)) continue;
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(e);
+        mx = max(mx, bits);
+        if (e != kMaxEnergy) mx2 = max(mx2, bits);
+        sum = dd_add(sum, DD{e, 0.0});
+        ++cnt;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DD other{__shfl_down_sync(0xffffffffu, sum.hi, o), __shfl_down_sync(0xffffffffu, sum.lo, o)};
+        sum = dd_add(sum, other);
+        mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        mx2 = max(mx2, __shfl_down_sync(0xffffffffu, mx2, o));
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ssum[threadIdx.x >> 5] = sum;
+        atomicMax(acc + 0, mx);
+        atomicMax(acc + 1, mx2);
+        atomicAdd(acc + 2, cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        DD b = ssum[0];
+        for (int w = 1; w < kStatsBlock / 32; ++w) b = dd_add(b, ssum[w]);
+        block_sum[blockIdx.x] = b;
+    }
+    if (threadIdx.x < 11 && sb[threadIdx.x]) atomicAdd(acc + 3 + threadIdx.x, sb[threadIdx.x]);
+}
+
+__global__ void k_energy_stats_sum(const DD* __restrict__ block_sum, int nblocks,
+                                   double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    DD s{0.0, 0.0};
+    for (int b = 0; b < nblocks; ++b) s = dd_add(s, block_sum[b]);
+    out[0] = s.hi + s.lo;
+}
+
+int energy_stats_blocks(int64_t n) { return grid_for(n > 0 ? n : 1, kStatsBlock, 4); }
+
+void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                         const double* vz, const uint8_t* locked, double thres,
+                         void* block_sum, unsigned long long* acc, double* sum_out,
+                         cudaStream_t s) {
+    const int blocks = energy_stats_blocks(n);
+    k_energy_stats<<<blocks, kStatsBlock, 0, s>>>(reinterpret_cast<const int4*>(tets), n, vx, vy,
+                                                  vz, locked, thres - 1, (DD*)block_sum, acc);
+    k_energy_stats_sum<<<1, 32, 0, s>>>((const DD*)block_sum, blocks, sum_out);
+}
+
 }  // namespace tw

@@ -5,6 +5,7 @@
 // copies of one chunk overlap the kernels of the others.  _device calls
 // enqueue one kernel on the context stream and return.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -179,6 +180,12 @@ __global__ void k_check_ids(const int32_t* __restrict__ ids, int64_t n, int32_t 
 
 using namespace tw;
 
+static double __longlong_as_double_host(unsigned long long b) {
+    double d;
+    std::memcpy(&d, &b, sizeof d);
+    return d;
+}
+
 namespace {
 
 constexpr int kNumPipe = 3;
@@ -297,10 +304,29 @@ int tw_set_params(tw_ctx* c, double eps_2, double sampling_dist, int newton_max_
     c->newton_max_it = newton_max_it;
     Guard g(c->device);
     for (auto& S : c->surf) {
-        int st = build_env_grid(c, S, eps_2, c->stream);
+        int st = build_env_grid(c, S, eps_2, c->grid_cell, c->stream);
         if (st != TW_OK) return st;
     }
     return TW_OK;
+}
+
+int tw_set_tuning(tw_ctx* c, int knob, double value) {
+    if (!c) return TW_ERR_ARG;
+    Guard g(c->device);
+    if (knob == TW_TUNE_GRID_CELL) {
+        if (!(value >= 0.05 && value <= 64.0)) return fail(c, TW_ERR_ARG, "grid cell factor");
+        c->grid_cell = value;
+        for (auto& S : c->surf) {
+            int st = build_env_grid(c, S, c->eps2, c->grid_cell, c->stream);
+            if (st != TW_OK) return st;
+        }
+        return TW_OK;
+    }
+    if (knob == TW_TUNE_SORT_POINTS) {
+        c->sort_points = value != 0.0;
+        return TW_OK;
+    }
+    return fail(c, TW_ERR_ARG, "unknown tuning knob");
 }
 
 int tw_stream(tw_ctx* c, void** s) {
@@ -561,7 +587,7 @@ int tw_surface_upload(tw_ctx* c, const double* V, int32_t nv, const int32_t* F, 
     st = build_surface(c, c->surf[which], (const double*)dV, nv, (const int32_t*)dF, nf, c->stream);
     dev_free(c, dV, 24 * (size_t)nv);
     dev_free(c, dF, 12 * (size_t)nf);
-    if (st == TW_OK) st = build_env_grid(c, c->surf[which], c->eps2, c->stream);
+    if (st == TW_OK) st = build_env_grid(c, c->surf[which], c->eps2, c->grid_cell, c->stream);
     return st;
 }
 
@@ -573,7 +599,8 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
     void* sort = nullptr;
     int st = ensure(c, 3, env_sort_scratch_bytes(n), &sort);
     if (st != TW_OK) return st;
-    launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters, sort,
+    launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters,
+                      c->sort_points ? sort : nullptr,
                       c->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
@@ -606,7 +633,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         const int64_t len = std::min<int64_t>(C, n - i0);
         cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
         launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->precision, c->counters,
-                          dS[k], s);
+                          c->sort_points ? dS[k] : nullptr, s);
         cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
     }
     return sync_status(c, "tw_envelope_points");
@@ -879,6 +906,150 @@ int tw_smooth_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
     cudaMemcpyAsync(out, dout, 24 * ns, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(status, dst, ns, cudaMemcpyDeviceToHost, c->stream);
     return sync_status(c, "tw_smooth_stars");
+}
+
+// ---- energy sweeps -------------------------------------------------------------------
+int tw_energy_stats(tw_ctx* c, const int32_t* tets, int64_t n, const uint8_t* locked,
+                    double thres, double* avg, double* max_e, double* second_max,
+                    int64_t* buckets) {
+    if (!c || n < 0 || (n > 0 && !tets) || !avg || !max_e || !second_max || !buckets)
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const int nb = energy_stats_blocks(n);
+    const size_t bytes = align(16 * (size_t)n) + align((size_t)n) + align(16 * (size_t)nb) +
+                         align(14 * 8) + align(8) + 256;
+    void* p;
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)n);
+    uint8_t* dl = (uint8_t*)q; q += align((size_t)n);
+    void* dbs = q; q += align(16 * (size_t)nb);
+    unsigned long long* dacc = (unsigned long long*)q; q += align(14 * 8);
+    double* dsum = (double*)q;
+    int* bad = (int*)(c->counters + kCntBad);
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(dacc, 0, 14 * 8, c->stream);
+    cudaMemsetAsync(dsum, 0, 8, c->stream);
+    if (n > 0) {
+        cudaMemcpyAsync(dt, tets, 16 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+        if (locked) cudaMemcpyAsync(dl, locked, (size_t)n, cudaMemcpyHostToDevice, c->stream);
+        k_check_ids<<<(unsigned)((4 * n + 255) / 256), 256, 0, c->stream>>>(dt, 4 * n, c->nv, bad);
+    }
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_energy_stats");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "tet vertex id out of range");
+    if (n > 0)
+        launch_energy_stats(dt, n, c->vx, c->vy, c->vz, locked ? dl : nullptr, thres, dbs, dacc,
+                            dsum, c->stream);
+    unsigned long long hacc[14];
+    double hsum = 0.0;
+    cudaMemcpyAsync(hacc, dacc, sizeof hacc, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(&hsum, dsum, 8, cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_energy_stats");
+    if (st != TW_OK) return st;
+    double a = hsum / (double)hacc[2];
+    if (std::isinf(a)) a = 1e50;
+    *avg = a;
+    *max_e = hacc[0] ? __longlong_as_double_host(hacc[0]) : 0.0;
+    *second_max = hacc[1] ? __longlong_as_double_host(hacc[1]) : 0.0;
+    for (int k = 0; k < 11; ++k) buckets[k] = (int64_t)hacc[3 + k];
+    return TW_OK;
+}
+
+double tw_filter_energy(const int64_t* b, double thres, int* is_clean_up) {
+    int64_t t1[10], t2[10];
+    for (int i = 0; i < 10; ++i) {
+        t1[i] = 0;
+        t2[i] = 0;
+        for (int k = 0; k <= i; ++k) t1[i] += b[k];
+        for (int k = i + 1; k < 11; ++k) t2[i] += b[k];
+    }
+    if (is_clean_up) *is_clean_up = 0;
+    if (t1[0] >= t2[0]) {
+        if (is_clean_up) *is_clean_up = t2[5] > 0;
+        return 8;
+    }
+    if (t1[8] <= t2[8]) return 1e11;
+    double p = 10.0;
+    for (int i = 0; i < 8; ++i, p *= 10.0)
+        if (t1[i] < t2[i] && t1[i + 1] > t2[i + 1]) return thres - 1 + 5 * p;
+    return 8;
+}
+
+// ---- edge-collapse checks ------------------------------------------------------------
+int tw_collapse_check(tw_ctx* c, const int32_t* v12, const uint8_t* flags, const int32_t* off,
+                      const int32_t* tets, const uint8_t* face_flags, int32_t n, int check_quality,
+                      double soft_energy, uint8_t* result) {
+    if (!c || n < 0 ||
+        (n > 0 && (!v12 || !flags || !off || !tets || !face_flags || !result)))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (n == 0) return TW_OK;
+    if (off[0] != 0) return fail(c, TW_ERR_ARG, "star offsets must start at 0");
+    bool any_surface = false, any_boundary = false;
+    for (int32_t i = 0; i < n; ++i) {
+        if (off[i + 1] < off[i]) return fail(c, TW_ERR_ARG, "star offsets decrease");
+        any_surface = any_surface || (flags[i] & TW_CV_V1_SURFACE);
+        any_boundary = any_boundary || (flags[i] & TW_CV_V1_BOUNDARY);
+    }
+    if (any_surface && c->surf[TW_SURFACE_INPUT].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no input surface uploaded");
+    if (any_boundary && c->surf[TW_SURFACE_BOUNDARY].nf == 0)
+        return fail(c, TW_ERR_NO_SURFACE, "no boundary surface uploaded");
+    const int64_t nt = off[n];
+    Guard g(c->device);
+    SmoothScratch S;
+    int st = smooth_scratch(c, n, nt, S);
+    if (st != TW_OK) return st;
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t ns = (size_t)n;
+    const size_t bytes = align(8 * ns) + align(ns) + align(4 * (ns + 1)) + align(16 * (size_t)nt) +
+                         align((size_t)nt) + 2 * align(ns) + 256;
+    void* p;
+    st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dv = (int32_t*)q; q += align(8 * ns);
+    uint8_t* dfl = (uint8_t*)q; q += align(ns);
+    int32_t* doff = (int32_t*)q; q += align(4 * (ns + 1));
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)nt);
+    uint8_t* dff = (uint8_t*)q; q += align((size_t)nt);
+    uint8_t* dst = (uint8_t*)q; q += align(ns);
+    uint8_t* ddeg = (uint8_t*)q; q += align(ns);
+    int* bad = (int*)q;
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemcpyAsync(dv, v12, 8 * ns, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dfl, flags, ns, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(doff, off, 4 * (ns + 1), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dff, face_flags, (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    if (nt > 0)
+        k_check_ids<<<(unsigned)((4 * nt + 255) / 256), 256, 0, c->stream>>>(dt, 4 * nt, c->nv, bad);
+    k_check_ids<<<(unsigned)((2 * ns + 255) / 256), 256, 0, c->stream>>>(dv, 2 * n, c->nv, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_collapse_check");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "vertex id out of range");
+    cudaMemsetAsync(S.face_count, 0, sizeof(unsigned long long), c->stream);
+    launch_collapse_points(c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], c->eps2,
+                           c->precision, c->vx, c->vy, c->vz, dv, dfl, n, dst, ddeg, c->counters,
+                           c->stream);
+    launch_collapse_stage(c->newton_shape, c->vx, c->vy, c->vz, doff, dt, dff, dv, dfl, ddeg, n,
+                          check_quality, soft_energy, dst, S.faces, S.face_count, S.face_cap,
+                          S.face_base, S.face_cnt, c->counters, c->stream);
+    if (any_surface)
+        launch_env_faces_dev(c->surf[TW_SURFACE_INPUT], S.faces, S.face_count, S.face_cap,
+                             c->eps2, c->sampling_dist, S.face_out, c->precision, c->counters,
+                             c->stream);
+    launch_collapse_finalize(n, S.face_base, S.face_cnt, S.face_out, dst, c->stream);
+    cudaMemcpyAsync(result, dst, ns, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_collapse_check");
 }
 
 // ---- misc ---------------------------------------------------------------------------

@@ -773,25 +773,13 @@ __device__ __forceinline__ void face_query_box(const double* t, const FaceCtx& F
     }
 }
 
-// One face, the whole warp: 1 if some sample is out, 0 otherwise (and for a
-// degenerate face); a face beyond the per-row sample bound sets error bit 2
-// and counts as out.
+// The samples of one face with its header already computed, the whole warp:
+// 1 if some sample is out, 0 otherwise.
 template <bool FP32>
-__device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
-                                                 const FaceCtx& F, double sd, TravStats& st,
-                                                 uint32_t& nq) {
+__device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const FaceCtx& F,
+                                                    double sd, TravStats& st, uint32_t& nq) {
     const int lane = threadIdx.x & 31;
     {
-        double t[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + k);
-        if (tri_collinear(t)) return 0;
-        SampleHeader h;
-        sample_header(t, sd, h);
-        if (header_too_large(h)) {
-            if (lane == 0) atomicOr(F.counters + kCntError, 2ULL);
-            return 1;
-        }
         int32_t hint = -1;
         bool out_found = false;
         // certified mode: the leaves within reach of the face, shared by the
@@ -800,6 +788,8 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
         int cnt = -1, kh = 0;
         if (FP32 && !F.T.goff) {
             float qlo[3], qhi[3];
+            const double t[9] = {h.vs[0].x, h.vs[0].y, h.vs[0].z, h.vs[1].x, h.vs[1].y,
+                                 h.vs[1].z, h.vs[2].x, h.vs[2].y, h.vs[2].z};
             face_query_box(t, F, qlo, qhi);
             cnt = warp_candidates32(F.T, qlo, qhi, lane, cand);
             if (cnt == kTraversalError) {
@@ -904,20 +894,105 @@ __device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
     }
 }
 
+// Header stage of one face (one thread): 0 = degenerate (not out), 1 = beyond
+// the per-row sample bound (error bit 2, counted out), 2 = sample it.
+__device__ __forceinline__ int face_prepare(const double* __restrict__ tri, double sd,
+                                            SampleHeader& h, unsigned long long* counters) {
+    double t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + k);
+    if (tri_collinear(t)) return 0;
+    sample_header(t, sd, h);
+    if (header_too_large(h)) {
+        atomicOr(counters + kCntError, 2ULL);
+        return 1;
+    }
+    return 2;
+}
+
+// One face, the whole warp (every lane computes the header).
+template <bool FP32>
+__device__ __forceinline__ uint8_t env_face_warp(const double* __restrict__ tri,
+                                                 const FaceCtx& F, double sd, TravStats& st,
+                                                 uint32_t& nq) {
+    SampleHeader h;
+    double t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + k);
+    if (tri_collinear(t)) return 0;
+    sample_header(t, sd, h);
+    if (header_too_large(h)) {
+        if ((threadIdx.x & 31) == 0) atomicOr(F.counters + kCntError, 2ULL);
+        return 1;
+    }
+    return env_face_samples<FP32>(h, F, sd, st, nq);
+}
+
+// Faces in blocks of kFaceBlock: first every thread prepares one face's header
+// into shared memory (the FP64 header and the exact degeneracy test run once
+// per face instead of once per lane), then each warp samples its share of the
+// block's faces.  Ctx(f, F, sd) gives face f's tree, eps and sampling distance.
+constexpr int kFaceBlock = 128;
+
+struct FaceSlot {
+    SampleHeader h;
+    int32_t state;  // face_prepare's result, or -1 past the end
+    int32_t seg;
+};
+
+template <bool FP32, class Ctx>
+__device__ __forceinline__ void faces_blocked(const double* __restrict__ tris, int64_t n,
+                                              unsigned long long* counters, Ctx ctx,
+                                              uint8_t* __restrict__ out) {
+    __shared__ FaceSlot slot[kFaceBlock];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    TravStats st;
+    uint32_t nq = 0;
+    for (int64_t base = (int64_t)blockIdx.x * kFaceBlock; base < n;
+         base += (int64_t)gridDim.x * kFaceBlock) {
+        for (int k = threadIdx.x; k < kFaceBlock; k += blockDim.x) {
+            const int64_t f = base + k;
+            FaceSlot& fs = slot[k];
+            if (f >= n) {
+                fs.state = -1;
+                continue;
+            }
+            FaceCtx F;
+            double sd;
+            fs.seg = ctx(f, F, sd);
+            fs.state = face_prepare(tris + 9 * f, sd, fs.h, counters);
+        }
+        __syncthreads();
+        for (int k = warp; k < kFaceBlock; k += nwarps) {
+            const int64_t f = base + k;
+            const FaceSlot& fs = slot[k];
+            if (fs.state < 0) break;
+            uint8_t o = (uint8_t)fs.state;
+            if (fs.state == 2) {
+                FaceCtx F;
+                double sd;
+                ctx(f, F, sd);
+                o = env_face_samples<FP32>(fs.h, F, sd, st, nq);
+            }
+            if (lane == 0) out[f] = o;
+        }
+        __syncthreads();
+    }
+    flush_stats(st, counters, nq);
+}
+
 template <bool FP32>
 __device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris, int64_t n,
                                                  const FaceCtx& F, double sd,
                                                  uint8_t* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    TravStats st;
-    uint32_t nq = 0;
-    for (int64_t f = warp; f < n; f += nwarps) {
-        uint8_t o = env_face_warp<FP32>(tris + 9 * f, F, sd, st, nq);
-        if (lane == 0) out[f] = o;
-    }
-    flush_stats(st, F.counters, nq);
+    faces_blocked<FP32>(tris, n, F.counters,
+                        [&](int64_t, FaceCtx& Fo, double& sdo) {
+                            Fo = F;
+                            sdo = sd;
+                            return 0;
+                        },
+                        out);
 }
 
 template <bool FP32>
@@ -929,9 +1004,8 @@ __global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tr
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0) return;
-    const int block = 128;
-    int64_t warps_needed = n;
-    int grid = grid_for(warps_needed * 32, block, 16);
+    const int block = kFaceBlock;
+    int grid = grid_for(n, block, 3);
     FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED) {
         k_env_faces<true><<<grid, block, 0, s>>>(tris, n, F, sd, out);
@@ -955,8 +1029,8 @@ void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned l
                           int64_t cap, double eps2, double sd, uint8_t* out, int precision,
                           unsigned long long* counters, cudaStream_t s) {
     if (cap <= 0) return;
-    const int block = 128;
-    int grid = grid_for(cap * 32, block, 16);
+    const int block = kFaceBlock;
+    int grid = grid_for(cap, block, 3);
     FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_faces_dev<true><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
@@ -1027,18 +1101,15 @@ __global__ void __launch_bounds__(128) k_env_faces_segs(const double* __restrict
                                                         const EnvSeg* __restrict__ segs, int nsegs,
                                                         uint8_t* __restrict__ out,
                                                         unsigned long long* __restrict__ counters) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    TravStats st;
-    uint32_t nq = 0;
-    for (int64_t f = warp; f < n; f += nwarps) {
-        const EnvSeg& g = segs[find_seg(segs, nsegs, f)];
-        FaceCtx F{g.T, g.E, counters};
-        uint8_t o = env_face_warp<FP32>(tris + 9 * f, F, g.sd, st, nq);
-        if (lane == 0) out[f] = o;
-    }
-    flush_stats(st, counters, nq);
+    faces_blocked<FP32>(tris, n, counters,
+                        [&](int64_t f, FaceCtx& Fo, double& sdo) {
+                            const int k = find_seg(segs, nsegs, f);
+                            const EnvSeg& g = segs[k];
+                            Fo = FaceCtx{g.T, g.E, counters};
+                            sdo = g.sd;
+                            return k;
+                        },
+                        out);
 }
 
 void launch_env_points_segs(const double* P, int64_t n, const void* segs, int nsegs, uint8_t* out,
@@ -1056,8 +1127,8 @@ void launch_env_points_segs(const double* P, int64_t n, const void* segs, int ns
 void launch_env_faces_segs(const double* tris, int64_t n, const void* segs, int nsegs, uint8_t* out,
                            int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0 || nsegs <= 0) return;
-    const int block = 128;
-    const int grid = grid_for(n * 32, block, 16);
+    const int block = kFaceBlock;
+    const int grid = grid_for(n, block, 3);
     const EnvSeg* g = static_cast<const EnvSeg*>(segs);
     if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_faces_segs<true><<<grid, block, 0, s>>>(tris, n, g, nsegs, out, counters);
@@ -1207,9 +1278,9 @@ void free_env_grid(tw_ctx* c, EnvGrid& G) {
     G = EnvGrid{};
 }
 
-int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s) {
+int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaStream_t s) {
     if (S.nf <= 0 || !(eps2 >= 0.0)) return TW_OK;
-    if (S.grid.off && S.grid.eps2 == eps2) return TW_OK;
+    if (S.grid.off && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
     free_env_grid(c, S.grid);
     const int32_t nf = S.nf;
     // bounding box of the facets: the root's two child boxes, or the facet
@@ -1255,7 +1326,11 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s) {
     for (int k = 0; k < 3; ++k) M = std::max(M, std::max(std::fabs(blo[k]), std::fabs(bhi[k])));
     M = M + 2.0 * eps + 1e-300;
     const double Rm = eps * (1.0 + std::ldexp(1.0, -18)) + std::ldexp(M, -17);
-    double cs = std::max(sum_ext / nf, 2.0 * Rm);
+    double cs = std::max(cell_factor * sum_ext / nf, 2.0 * Rm);
+    // at most 256 cells per facet (and 2^26 in all): the grid is dense, and
+    // a surface fills only a thin shell of it
+    const int64_t max_cells =
+        std::min<int64_t>(int64_t(1) << 26, std::max<int64_t>(int64_t(1) << 18, 256 * (int64_t)nf));
     int64_t n[3];
     float lo[3];
     float inv = 0.0f;
@@ -1270,11 +1345,11 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s) {
             n[k] = (int64_t)std::floor((bhi[k] + Rm - (double)f) * (double)inv) + 2;
             cells *= n[k];
         }
-        if (cells <= (int64_t(1) << 24)) break;
+        if (cells <= max_cells) break;
         cs *= 1.25;
     }
     const int64_t ncells = n[0] * n[1] * n[2];
-    if (ncells > (int64_t(1) << 24)) {  // no grid: the tree walk serves the queries
+    if (ncells > max_cells) {  // no grid: the tree walk serves the queries
         dev_free(c, acc, 32);
         return TW_OK;
     }
@@ -1341,9 +1416,72 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s) {
     g.off = (uint32_t*)off;
     g.list = (int32_t*)list;
     g.eps2 = eps2;
+    g.cell_factor = cell_factor;
     g.off_bytes = off_bytes;
     g.list_bytes = 4 * (size_t)total + 16;
     return TW_OK;
+}
+
+// Point checks of candidate collapses (EdgeCollapser.cpp:286-329): the
+// degenerate-edge flag, then v2 against the boundary envelope when v1 is on
+// the boundary and v2 is not, and against the envelope when v1 is on the
+// surface and v2 is not.  ENVELOP (3) or kCollapsePending.
+template <bool FP32>
+__global__ void k_collapse_points(EnvTree Tin, EnvTree Tb, EpsParams E,
+                                  const double* __restrict__ vx, const double* __restrict__ vy,
+                                  const double* __restrict__ vz, const int32_t* __restrict__ v12,
+                                  const uint8_t* __restrict__ flags, int32_t n,
+                                  uint8_t* __restrict__ status, uint8_t* __restrict__ degenerate,
+                                  unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    TravStats st;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int32_t v1 = v12[2 * i], v2 = v12[2 * i + 1];
+        const double dx = vx[v1] - vx[v2], dy = vy[v1] - vy[v2], dz = vz[v1] - vz[v2];
+        const bool deg = sqrt((dx * dx + dy * dy) + dz * dz) == 0.0;
+        degenerate[i] = deg;
+        const uint8_t fl = flags[i];
+        const V3 p{vx[v2], vy[v2], vz[v2]};
+        uint8_t res = kCollapsePending;
+        for (int pass = 0; pass < 2 && res == kCollapsePending; ++pass) {
+            const bool bnd = pass == 0;
+            const uint8_t need = bnd ? TW_CV_V1_BOUNDARY : TW_CV_V1_SURFACE;
+            const uint8_t has = bnd ? TW_CV_V2_BOUNDARY : TW_CV_V2_SURFACE;
+            if (!(fl & need) || (fl & has) || deg) continue;
+            const EnvTree& T = bnd ? Tb : Tin;
+            if (T.nf <= 0) {
+                atomicOr(counters + kCntError, 4ULL);
+                res = 3;
+                break;
+            }
+            int32_t f;
+            if (FP32 && T.goff) {
+                const CertQuery q = cert_query(p, E, T.scale_hi);
+                f = grid_point_in(T, E, true, p, q, st) ? 0 : -1;
+            } else {
+                f = query_point<FP32>(T, p, E, st);
+            }
+            if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
+            if (f == -1) res = 3;
+        }
+        status[i] = res;
+    }
+}
+
+void launch_collapse_points(const Surface& Sin, const Surface& Sb, double eps2, int precision,
+                            const double* vx, const double* vy, const double* vz,
+                            const int32_t* v12, const uint8_t* flags, int32_t n, uint8_t* status,
+                            uint8_t* degenerate, unsigned long long* counters, cudaStream_t s) {
+    if (n <= 0) return;
+    const int block = 128;
+    const EnvTree Ti = env_tree_for(Sin, eps2), Tb = env_tree_for(Sb, eps2);
+    const EpsParams E = eps_params(eps2);
+    if (precision == TW_PRECISION_FP32_CERTIFIED)
+        k_collapse_points<true><<<grid_for(n, block, 8), block, 0, s>>>(
+            Ti, Tb, E, vx, vy, vz, v12, flags, n, status, degenerate, counters);
+    else
+        k_collapse_points<false><<<grid_for(n, block, 8), block, 0, s>>>(
+            Ti, Tb, E, vx, vy, vz, v12, flags, n, status, degenerate, counters);
 }
 
 void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,

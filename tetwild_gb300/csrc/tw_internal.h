@@ -69,6 +69,7 @@ struct EnvGrid {
     uint32_t* off = nullptr;   // n0 n1 n2 + 1 offsets into list
     int32_t* list = nullptr;   // leaf indices
     double eps2 = -1.0;        // the eps2 it was built for (-1: none)
+    double cell_factor = 0.0;  // and the cell-size factor
     size_t off_bytes = 0, list_bytes = 0;
 };
 
@@ -121,6 +122,8 @@ struct tw_ctx {
     size_t mesh_bytes = 0;
     int precision = TW_PRECISION_FP64;
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
+    double grid_cell = 0.25;  // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
+    int sort_points = 1;     // Morton-order point queries (TW_TUNE_SORT_POINTS)
     tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
@@ -142,6 +145,9 @@ constexpr int kCntEnvWarpFallback = 9;  // warps whose shared candidate list ove
 // internal star states of a smoothing pass (the final ones are TW_SMOOTH_*)
 constexpr uint8_t kSmoothPendingProject = 6;   // surface star moved by Newton, not yet projected
 constexpr uint8_t kSmoothPendingEnvelope = 7;  // surface star waiting for its face tests
+// internal states of a collapse check (the final ones are the reference's 0..3)
+constexpr uint8_t kCollapsePending = 255;
+constexpr uint8_t kCollapsePendingEnvelope = 254;
 }  // namespace tw
 
 namespace tw {
@@ -166,12 +172,21 @@ void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, co
                             const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
                             uint8_t* needs_host, unsigned long long* counters, cudaStream_t s);
 
+// Energy sweeps: block_sum holds energy_stats_blocks(n) double-doubles; acc
+// 14 words zeroed by the caller (max bits, second-max bits, unlocked count,
+// 11 buckets); sum_out the unlocked energies' sum.
+int energy_stats_blocks(int64_t n);
+void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                         const double* vz, const uint8_t* locked, double thres,
+                         void* block_sum, unsigned long long* acc, double* sum_out,
+                         cudaStream_t s);
+
 // ---- launchers (tw_lbvh.cu) ----
 int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int32_t* dF,
                   int32_t nf, cudaStream_t s);
 void free_surface(tw_ctx* c, Surface& S);
 // (Re)builds S.grid for eps2 when it was built for another one (tw_envelope.cu).
-int build_env_grid(tw_ctx* c, Surface& S, double eps2, cudaStream_t s);
+int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaStream_t s);
 void free_env_grid(tw_ctx* c, EnvGrid& G);
 
 // ---- launchers (tw_envelope.cu) ----
@@ -258,6 +273,22 @@ int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S);
 void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uint8_t* ff,
                    const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
                    double* out, uint8_t* status, const SmoothScratch& S);
+
+// Collapse checks (tw_envelope.cu / tw_newton.cu): point envelopes and the
+// degenerate flag, then flip / quality / face list, then the face results.
+void launch_collapse_points(const Surface& Sin, const Surface& Sb, double eps2, int precision,
+                            const double* vx, const double* vy, const double* vz,
+                            const int32_t* v12, const uint8_t* flags, int32_t n, uint8_t* status,
+                            uint8_t* degenerate, unsigned long long* counters, cudaStream_t s);
+void launch_collapse_stage(int shape, const double* vx, const double* vy, const double* vz,
+                           const int32_t* off, const int32_t* tets, const uint8_t* face_flags,
+                           const int32_t* v12, const uint8_t* flags, const uint8_t* degenerate,
+                           int32_t n, int check_quality, double soft_energy, uint8_t* status,
+                           double* faces, unsigned long long* face_count, int64_t face_cap,
+                           int32_t* face_base, int32_t* face_cnt, unsigned long long* counters,
+                           cudaStream_t s);
+void launch_collapse_finalize(int32_t n, const int32_t* face_base, const int32_t* face_cnt,
+                              const uint8_t* face_out, uint8_t* status, cudaStream_t s);
 
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);

@@ -578,6 +578,161 @@ __global__ void __launch_bounds__(256) k_smooth_stage2(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Checks of candidate edge collapses v1 -> v2 (EdgeCollapser.cpp:284-446),
+// G lanes per edge; the point-envelope checks ran before
+// (launch_collapse_points) and left kCollapsePending where they passed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool tet_has(int4 tv, int32_t v) {
+    return tv.x == v || tv.y == v || tv.z == v || tv.w == v;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_collapse_stage(
+    const double* __restrict__ vx, const double* __restrict__ vy, const double* __restrict__ vz,
+    const int32_t* __restrict__ off, const int4* __restrict__ tets,
+    const uint8_t* __restrict__ face_flags, const int32_t* __restrict__ v12,
+    const uint8_t* __restrict__ flags, const uint8_t* __restrict__ degenerate, int32_t n,
+    int check_quality, double soft_energy, uint8_t* __restrict__ status,
+    double* __restrict__ faces, unsigned long long* __restrict__ face_count, int64_t face_cap,
+    int32_t* __restrict__ face_base, int32_t* __restrict__ face_cnt,
+    unsigned long long* __restrict__ counters) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const unsigned gm = group_mask<G>(lane);
+    const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t e = gid; e < n; e += ngroups) {
+        if (status[e] != kCollapsePending) continue;  // uniform within the group
+        const int32_t b = off[e], nt = off[e + 1] - b;
+        const int32_t v1 = v12[2 * e], v2 = v12[2 * e + 1];
+        StarView S{vx, vy, vz, tets + b, nt, v1};
+        const double p1[3] = {vx[v1], vy[v1], vz[v1]};
+        const double p2[3] = {vx[v2], vy[v2], vz[v2]};
+        const uint8_t fl = flags[e];
+        const bool deg = degenerate[e] != 0;
+        // isFlip of the new tets: those without v2, v1 moved onto v2 (:336-384)
+        bool bad = false;
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            const int4 tv = tet_at(S, c0);
+            if (tet_has(tv, v2)) continue;
+            double T[12];
+            gather_tet(S, tv, 0, p2, T);
+            bad = bad || (orient3d(T, T + 3, T + 6, T + 9) != 1);
+        }
+        if (__any_sync(gm, bad)) {
+            if (gl == 0) status[e] = 1;  // FLIP
+            continue;
+        }
+        // quality (:390-415): max over the old tets (stored quality) and the new
+        if (check_quality) {
+            double old_max = 0.0, new_max = 0.0;
+            for (int c0 = gl; c0 < nt; c0 += G) {
+                const int4 tv = tet_at(S, c0);
+                double T[12];
+                gather_tet(S, tv, 0, p1, T);
+                old_max = fmax(old_max, quality_from(orient3d(T, T + 3, T + 6, T + 9),
+                                                     amips_energy(T)));
+                if (tet_has(tv, v2)) continue;
+                gather_tet(S, tv, 0, p2, T);
+                new_max = fmax(new_max, positive_tet_quality(T));
+            }
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) {
+                old_max = fmax(old_max, __shfl_xor_sync(gm, old_max, o, G));
+                new_max = fmax(new_max, __shfl_xor_sync(gm, new_max, o, G));
+            }
+            if (soft_energy >= 0.0) old_max = soft_energy;
+            if (fl & TW_CV_V1_UNROUNDED) new_max = 0.0;
+            if (!deg && !(new_max <= old_max)) {
+                if (gl == 0) status[e] = 2;  // QUALITY
+                continue;
+            }
+        }
+        if (!(fl & TW_CV_V1_SURFACE) || deg) {
+            if (gl == 0) status[e] = 0;  // SUCCESS
+            continue;
+        }
+        // isCollapsable_epsilon (:727-775): the surface faces through v1 as
+        // sorted triples without repeats, those through v2 dropped, v1
+        // replaced by v2 in place
+        const uint8_t* ff = face_flags + b;
+        int nmine = 0;
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            const int4 tv = tet_at(S, c0);
+            const uint8_t f8 = __ldg(ff + c0);
+            for (int j = 0; j < 4; ++j) {
+                int32_t key[3];
+                if (!first_surface_face(S, ff, c0, tv, f8, j, key)) continue;
+                nmine += (key[0] != v2 && key[1] != v2 && key[2] != v2);
+            }
+        }
+        int incl = nmine;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            int v = __shfl_up_sync(gm, incl, o, G);
+            if (gl >= o) incl += v;
+        }
+        const int total = __shfl_sync(gm, incl, G - 1, G);
+        if (total == 0) {
+            if (gl == 0) status[e] = 0;
+            continue;
+        }
+        unsigned long long base = 0;
+        if (gl == 0) base = atomicAdd(face_count, (unsigned long long)total);
+        base = __shfl_sync(gm, base, 0, G);
+        if (base + (unsigned long long)total > (unsigned long long)face_cap) {
+            if (gl == 0) {
+                atomicOr(counters + kCntError, 8ULL);
+                status[e] = 3;
+            }
+            continue;
+        }
+        int64_t w = (int64_t)base + (incl - nmine);
+        for (int c0 = gl; c0 < nt; c0 += G) {
+            const int4 tv = tet_at(S, c0);
+            const uint8_t f8 = __ldg(ff + c0);
+            for (int j = 0; j < 4; ++j) {
+                int32_t key[3];
+                if (!first_surface_face(S, ff, c0, tv, f8, j, key)) continue;
+                if (key[0] == v2 || key[1] == v2 || key[2] == v2) continue;
+                double* f = faces + 9 * w;
+                for (int k = 0; k < 3; ++k) {
+                    if (key[k] == v1) {
+                        f[3 * k] = p2[0];
+                        f[3 * k + 1] = p2[1];
+                        f[3 * k + 2] = p2[2];
+                    } else {
+                        f[3 * k] = __ldg(vx + key[k]);
+                        f[3 * k + 1] = __ldg(vy + key[k]);
+                        f[3 * k + 2] = __ldg(vz + key[k]);
+                    }
+                }
+                ++w;
+            }
+        }
+        if (gl == 0) {
+            face_base[e] = (int32_t)base;
+            face_cnt[e] = total;
+            status[e] = kCollapsePendingEnvelope;
+        }
+    }
+}
+
+__global__ void k_collapse_finalize(int32_t n, const int32_t* __restrict__ face_base,
+                                    const int32_t* __restrict__ face_cnt,
+                                    const uint8_t* __restrict__ face_out,
+                                    uint8_t* __restrict__ status) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (status[i] != kCollapsePendingEnvelope) continue;
+        bool outside = false;
+        const int32_t b = face_base[i], m = face_cnt[i];
+        for (int32_t k = 0; k < m && !outside; ++k) outside = face_out[b + k] != 0;
+        status[i] = outside ? 3 : 0;
+    }
+}
+
 __global__ void k_smooth_finalize(int32_t nstars, const int32_t* __restrict__ face_base,
                                   const int32_t* __restrict__ face_cnt,
                                   const uint8_t* __restrict__ face_out,
@@ -705,6 +860,37 @@ void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int3
     const int block = 256;
     k_smooth_finalize<<<grid_for(nstars, block, 8), block, 0, s>>>(nstars, face_base, face_cnt,
                                                                    face_out, pnew, out, status);
+}
+
+void launch_collapse_stage(int shape, const double* vx, const double* vy, const double* vz,
+                           const int32_t* off, const int32_t* tets, const uint8_t* face_flags,
+                           const int32_t* v12, const uint8_t* flags, const uint8_t* degenerate,
+                           int32_t n, int check_quality, double soft_energy, uint8_t* status,
+                           double* faces, unsigned long long* face_count, int64_t face_cap,
+                           int32_t* face_base, int32_t* face_cnt, unsigned long long* counters,
+                           cudaStream_t s) {
+    if (n <= 0) return;
+    int block;
+    const int G = smooth_group(shape, &block);
+    const int grid = grid_for((int64_t)n * G, block, 2048 / block);
+    const int4* t4 = reinterpret_cast<const int4*>(tets);
+#define TW_COLLAPSE_ARGS                                                                      \
+    vx, vy, vz, off, t4, face_flags, v12, flags, degenerate, n, check_quality, soft_energy, status, \
+        faces, face_count, face_cap, face_base, face_cnt, counters
+    if (G == 8)
+        k_collapse_stage<8><<<grid, block, 0, s>>>(TW_COLLAPSE_ARGS);
+    else if (G == 16)
+        k_collapse_stage<16><<<grid, block, 0, s>>>(TW_COLLAPSE_ARGS);
+    else
+        k_collapse_stage<32><<<grid, block, 0, s>>>(TW_COLLAPSE_ARGS);
+#undef TW_COLLAPSE_ARGS
+}
+
+void launch_collapse_finalize(int32_t n, const int32_t* face_base, const int32_t* face_cnt,
+                              const uint8_t* face_out, uint8_t* status, cudaStream_t s) {
+    if (n <= 0) return;
+    k_collapse_finalize<<<grid_for(n, 256, 8), 256, 0, s>>>(n, face_base, face_cnt, face_out,
+                                                            status);
 }
 
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,

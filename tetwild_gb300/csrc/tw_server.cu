@@ -544,7 +544,9 @@ int tw_server_job_open(tw_server* s, const double* V, int32_t nv, const int32_t*
     std::lock_guard<std::mutex> ak(s->admin);
     // footprint: nodes (128 + 64 B), facet records (128 + 72 + 4 B) per facet,
     // build temporaries, counters
-    const size_t est = 420 * (size_t)nf + 48 * (size_t)nv + (size_t(4) << 20);
+    // plus the certified-envelope grid: up to 256 cells (4 B) per facet and
+    // up to ~300 list entries (4 B) per facet
+    const size_t est = (420 + 1024 + 1200) * (size_t)nf + 48 * (size_t)nv + (size_t(4) << 20);
     size_t used;
     {
         std::lock_guard<std::mutex> lk(s->mu);
