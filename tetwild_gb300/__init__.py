@@ -130,6 +130,7 @@ _SIGS = {
     "tw_newton_stars_device": [_P, _P, _P, _P, _I32, _P, _P],
     "tw_set_newton_shape": [_P, _I],
     "tw_set_tuning": [_P, _I, _D],
+    "tw_kernel_times": [_P, _P, _I, ctypes.POINTER(_I)],
     "tw_nearest_points": [_P, _P, _I64, _I, _P, _P, _P],
     "tw_nearest_points_device": [_P, _P, _I64, _I, _P, _P, _P],
     "tw_smooth_stars": [_P, _P, _P, _P, _P, _P, _I32, _P, _P],
@@ -374,9 +375,18 @@ class Context:
     TUNE_GRID_CELL = 0
     TUNE_SORT_POINTS = 1
 
+    TUNE_TIME_KERNELS = 2
+
     def set_tuning(self, knob: int, value: float):
         """Work-only knobs (TW_TUNE_*): results are the same for every value."""
         self._check(self.lib.tw_set_tuning(self.h, knob, value))
+
+    def kernel_times(self, max_n: int = 64):
+        """Durations (ms) of the point-envelope kernel launches recorded since the last call."""
+        ms = np.zeros(max_n, np.float32)
+        cnt = _I()
+        self._check(self.lib.tw_kernel_times(self.h, _ptr(ms), max_n, ctypes.byref(cnt)))
+        return ms[:cnt.value].astype(float).tolist()
 
     # -- smoothing pass ------------------------------------------------------------------
     def smooth_stars(self, star_off, tets, centers, face_flags=None, kinds=None):

@@ -284,6 +284,8 @@ int tw_ctx_destroy(tw_ctx* c) {
     dev_free(c, c->counters, kNumCounters * sizeof(unsigned long long));
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto& ev : c->time_ev)
+        if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_in) cudaStreamDestroy(c->copy_in);
     if (c->copy_out) cudaStreamDestroy(c->copy_out);
@@ -326,7 +328,29 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         c->sort_points = value != 0.0;
         return TW_OK;
     }
+    if (knob == TW_TUNE_TIME_KERNELS) {
+        c->time_kernels = value != 0.0;
+        c->time_count = 0;
+        return TW_OK;
+    }
     return fail(c, TW_ERR_ARG, "unknown tuning knob");
+}
+
+int tw_kernel_times(tw_ctx* c, float* ms, int max, int* count) {
+    if (!c || !count || (max > 0 && !ms)) return TW_ERR_ARG;
+    Guard g(c->device);
+    const int n = std::min(c->time_count, tw_ctx::kTimeRing);
+    const int first = c->time_count - n;
+    int k = 0;
+    for (int i = first; i < c->time_count && k < max; ++i, ++k) {
+        const int r = i % tw_ctx::kTimeRing;
+        cudaError_t e = cudaEventSynchronize(c->time_ev[2 * r + 1]);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tw_kernel_times");
+        cudaEventElapsedTime(ms + k, c->time_ev[2 * r], c->time_ev[2 * r + 1]);
+    }
+    *count = k;
+    c->time_count = 0;
+    return TW_OK;
 }
 
 int tw_stream(tw_ctx* c, void** s) {
@@ -599,9 +623,19 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
     void* sort = nullptr;
     int st = ensure(c, 3, env_sort_scratch_bytes(n), &sort);
     if (st != TW_OK) return st;
+    cudaEvent_t eb = nullptr, ee = nullptr;
+    if (c->time_kernels) {
+        const int k = c->time_count % tw_ctx::kTimeRing;
+        if (!c->time_ev[2 * k]) {
+            cudaEventCreate(&c->time_ev[2 * k]);
+            cudaEventCreate(&c->time_ev[2 * k + 1]);
+        }
+        eb = c->time_ev[2 * k];
+        ee = c->time_ev[2 * k + 1];
+        ++c->time_count;
+    }
     launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters,
-                      c->sort_points ? sort : nullptr,
-                      c->stream);
+                      c->sort_points ? sort : nullptr, c->stream, eb, ee);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
     return TW_OK;

@@ -533,7 +533,7 @@ constexpr int64_t kSortMin = 4096;
 
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       cudaStream_t s) {
+                       cudaStream_t s, cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     if (n <= 0) return;
     const int block = 128;
     const int32_t* order = nullptr;
@@ -556,6 +556,7 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     const EpsParams E = eps_params(eps2);
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
+    if (ev_begin) cudaEventRecord(ev_begin, s);
     if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
         k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
@@ -568,6 +569,7 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     else
         k_env_points<false><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                      counters);
+    if (ev_end) cudaEventRecord(ev_end, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -123,6 +123,12 @@ struct tw_ctx {
     int precision = TW_PRECISION_FP64;
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
     double grid_cell = 0.25;  // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
+    // launch timing of the point-envelope test kernel (TW_TUNE_TIME_KERNELS):
+    // a ring of event pairs recorded around each launch
+    static constexpr int kTimeRing = 64;
+    int time_kernels = 0;
+    int time_count = 0;
+    cudaEvent_t time_ev[2 * kTimeRing] = {};
     int sort_points = 1;     // Morton-order point queries (TW_TUNE_SORT_POINTS)
     tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
@@ -198,7 +204,8 @@ void free_env_grid(tw_ctx* c, EnvGrid& G);
 // the context's counter array (error word and statistics).
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       cudaStream_t s);
+                       cudaStream_t s, cudaEvent_t ev_begin = nullptr,
+                       cudaEvent_t ev_end = nullptr);
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
 void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
