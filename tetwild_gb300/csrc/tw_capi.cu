@@ -224,6 +224,20 @@ cudaStream_t pipe_stream(tw_ctx* c, int k) {
     return k == 1 ? c->copy_in : c->copy_out;
 }
 
+// Device address of page-locked host memory (nullptr for pageable or device
+// memory, or nullptr in): on this system the GPU reads and writes it over the
+// coherent CPU-GPU link, so kernels can stream it without staging copies.
+const void* pinned_device_ptr(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost) return nullptr;
+    return a.devicePointer;
+}
+
 int64_t chunk_len(int64_t n, size_t bytes_per_item) {
     // ~96 MB of inputs+outputs per chunk, at least 64k items
     int64_t c = (int64_t)((96ull << 20) / std::max<size_t>(bytes_per_item, 1));
@@ -431,6 +445,24 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
         return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
     if (n == 0) return TW_OK;
     Guard g(c->device);
+    // every buffer page-locked: the kernel streams them in place
+    {
+        const void* dT = pinned_device_ptr(T);
+        const void* dE = pinned_device_ptr(E);
+        const void* dJ = pinned_device_ptr(J);
+        const void* dH = pinned_device_ptr(H);
+        const void* dF = pinned_device_ptr(flip);
+        if (dT && (!E || dE) && (!J || dJ) && (!H || dH) && (!flip || dF)) {
+            if (c->precision == TW_PRECISION_FP32_CERTIFIED)
+                launch_amips_soa_cert((const double*)dT, n, mode, (double*)dE, (double*)dJ,
+                                      (double*)dH, (uint8_t*)dF, c->counters, c->stream);
+            else
+                launch_amips_soa((const double*)dT, n, mode, (double*)dE, (double*)dJ,
+                                 (double*)dH, (uint8_t*)dF, c->counters + kCntExactOrient,
+                                 c->stream);
+            return sync_status(c, "tw_amips_soa");
+        }
+    }
     const size_t per = 96 + (E ? 8 : 0) + (J ? 24 : 0) + (H ? 72 : 0) + (flip ? 1 : 0);
     const int64_t C = chunk_len(n, per);
     double* dT[kNumPipe];

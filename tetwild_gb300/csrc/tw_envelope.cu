@@ -390,6 +390,21 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
     return in;
 }
 
+// The points in the sort's order: a pure gather (many independent loads in
+// flight), so the test kernel reads its points coalesced.
+__global__ void k_gather_points(const double* __restrict__ P, const int32_t* __restrict__ order,
+                                int64_t n, double* __restrict__ Ps) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int64_t j = __ldg(order + i);
+        Ps[3 * i] = __ldg(P + 3 * j);
+        Ps[3 * i + 1] = __ldg(P + 3 * j + 1);
+        Ps[3 * i + 2] = __ldg(P + 3 * j + 2);
+    }
+}
+
+// Ps: the points in order (sorted; order maps position i to input index), or
+// the input itself with order == nullptr.
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __restrict__ P,
                                                          const int32_t* __restrict__ order,
@@ -404,7 +419,7 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __r
         const int64_t i = b + (threadIdx.x & 31);
         if (i < n) {
             const int64_t j = order ? (int64_t)__ldg(order + i) : i;
-            const V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
+            const V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
             const CertQuery q = cert_query(p, E, T.scale_hi);
             out[j] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
             ++nq;
@@ -498,6 +513,7 @@ struct SortLayout {
     uint32_t* codes2;
     int32_t* idx;
     int32_t* idx2;
+    double* sorted;   // the points gathered into Morton order (certified grid path)
     void* temp;
     size_t temp_bytes;
 };
@@ -517,6 +533,7 @@ static SortLayout sort_layout(void* base, int64_t n) {
     L.codes2 = (uint32_t*)q; q += al(4 * (size_t)n);
     L.idx = (int32_t*)q; q += al(4 * (size_t)n);
     L.idx2 = (int32_t*)q; q += al(4 * (size_t)n);
+    L.sorted = (double*)q; q += al(24 * (size_t)n);
     L.temp = q;
     L.temp_bytes = cub_sort_bytes(n);
     return L;
@@ -524,7 +541,7 @@ static SortLayout sort_layout(void* base, int64_t n) {
 
 size_t env_sort_scratch_bytes(int64_t n) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    return 4 * al(4 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
+    return 4 * al(4 * (size_t)n) + al(24 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
 }
 
 // Batches below this size are traversed in input order (sorting would cost
@@ -557,9 +574,16 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
-        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff) {
+        const double* Pg = P;
+        if (order) {
+            SortLayout L = sort_layout(sort_scratch, n);
+            k_gather_points<<<grid_for(n, 256, 8), 256, 0, s>>>(P, order, n, L.sorted);
+            Pg = L.sorted;
+        }
+        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(Pg, order, n, T, E, out,
                                                                       counters);
+    }
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
         k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
@@ -1089,9 +1113,14 @@ __global__ void __launch_bounds__(128) k_env_points_segs(const double* __restric
             const EnvTree T = g.T;
             const EpsParams E = g.E;
             V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
-            int32_t f = query_point<FP32>(T, p, E, st);
-            if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
-            out[i] = (uint8_t)(f == -1);
+            if (FP32 && T.goff) {
+                const CertQuery q = cert_query(p, E, T.scale_hi);
+                out[i] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
+            } else {
+                int32_t f = query_point<FP32>(T, p, E, st);
+                if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
+                out[i] = (uint8_t)(f == -1);
+            }
             ++nq;
         }
     }
