@@ -390,21 +390,6 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
     return in;
 }
 
-// The points in the sort's order: a pure gather (many independent loads in
-// flight), so the test kernel reads its points coalesced.
-__global__ void k_gather_points(const double* __restrict__ P, const int32_t* __restrict__ order,
-                                int64_t n, double* __restrict__ Ps) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const int64_t j = __ldg(order + i);
-        Ps[3 * i] = __ldg(P + 3 * j);
-        Ps[3 * i + 1] = __ldg(P + 3 * j + 1);
-        Ps[3 * i + 2] = __ldg(P + 3 * j + 2);
-    }
-}
-
-// Ps: the points in order (sorted; order maps position i to input index), or
-// the input itself with order == nullptr.
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __restrict__ P,
                                                          const int32_t* __restrict__ order,
@@ -419,7 +404,7 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __r
         const int64_t i = b + (threadIdx.x & 31);
         if (i < n) {
             const int64_t j = order ? (int64_t)__ldg(order + i) : i;
-            const V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
+            const V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
             const CertQuery q = cert_query(p, E, T.scale_hi);
             out[j] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
             ++nq;
@@ -513,7 +498,6 @@ struct SortLayout {
     uint32_t* codes2;
     int32_t* idx;
     int32_t* idx2;
-    double* sorted;   // the points gathered into Morton order (certified grid path)
     void* temp;
     size_t temp_bytes;
 };
@@ -533,7 +517,6 @@ static SortLayout sort_layout(void* base, int64_t n) {
     L.codes2 = (uint32_t*)q; q += al(4 * (size_t)n);
     L.idx = (int32_t*)q; q += al(4 * (size_t)n);
     L.idx2 = (int32_t*)q; q += al(4 * (size_t)n);
-    L.sorted = (double*)q; q += al(24 * (size_t)n);
     L.temp = q;
     L.temp_bytes = cub_sort_bytes(n);
     return L;
@@ -541,7 +524,7 @@ static SortLayout sort_layout(void* base, int64_t n) {
 
 size_t env_sort_scratch_bytes(int64_t n) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    return 4 * al(4 * (size_t)n) + al(24 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
+    return 4 * al(4 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
 }
 
 // Batches below this size are traversed in input order (sorting would cost
@@ -574,16 +557,9 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff) {
-        const double* Pg = P;
-        if (order) {
-            SortLayout L = sort_layout(sort_scratch, n);
-            k_gather_points<<<grid_for(n, 256, 8), 256, 0, s>>>(P, order, n, L.sorted);
-            Pg = L.sorted;
-        }
-        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(Pg, order, n, T, E, out,
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
+        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
-    }
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
         k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
@@ -857,64 +833,79 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
             out_found = __any_sync(0xffffffffu, out_found);
             return out_found ? 1 : 0;
         }
-        // Row break: first m in [1, M] with distance(v0_m, v1_m) <= sd.
-        int mstop = h.M + 1;
-        if (h.M >= 1) {
-            for (int base = 1; base <= h.M; base += 32) {
-                int m = base + lane;
-                V3 v;
-                int N1 = 0;
-                bool brk = (m <= h.M) && !sample_row(h, sd, m, v, N1);
-                unsigned bal = __ballot_sync(0xffffffffu, brk);
-                if (bal) {
-                    mstop = base + __ffs(bal) - 1;
-                    break;
-                }
-            }
-        }
+        // The samples as flat index ranges that the 32 lanes walk in step (the
+        // order of the tests changes only the work: the face is out iff some
+        // sample is).  First the base row, v1, v2 and the two other edges...
         const int NA = count_upto(h.N, 0);
         const int NE = (h.M >= 1 && h.hasE) ? count_upto(h.NE, 1) : 0;
         const int NF = (h.M >= 1 && h.hasF) ? count_upto(h.NF, 1) : 0;
-        // Work list per lane: phase 0 base row (strided), 1 vertices v1/v2,
-        // 2 rows (one row per lane at a time), 3 edge v1->v2, 4 edge v2->v0.
-        int phase = 0, idx = lane, row = 1 + lane, rpos = 0, rN1 = -1;
-        V3 rv{0.0, 0.0, 0.0};
-        while (true) {
-            bool have = false;
+        const int NX = NA + 2 + NE + NF;
+        for (int s0 = 0; s0 < NX; s0 += 32) {
+            const int s = s0 + lane;
+            const bool have = s < NX;
             V3 p{0.0, 0.0, 0.0};
-            while (!have && phase < 5) {
-                if (phase == 0) {
-                    if (idx < NA) { p = base_point(h, sd, idx); idx += 32; have = true; }
-                    else { phase = 1; }
-                } else if (phase == 1) {
-                    phase = 2;
-                    if (lane == 0) { p = h.v1; have = true; }
-                    else if (lane == 1) { p = h.v2; have = true; }
-                } else if (phase == 2) {
-                    if (rpos <= rN1) { p = row_point(h, rv, sd, rpos); ++rpos; have = true; }
-                    else if (row < mstop) {
-                        int N1 = -1;
-                        sample_row(h, sd, row, rv, N1);
-                        if (N1 > (int)kMaxSamplesPerRow) {
-                            atomicOr(F.counters + kCntError, 2ULL);
-                            N1 = -1;
-                        }
-                        rN1 = N1;
-                        rpos = 0;
-                        row += 32;
-                    } else { phase = 3; idx = 1 + lane; }
-                } else if (phase == 3) {
-                    if (idx <= NE) { p = edge_point(h.v1, h.nE, sd, idx); idx += 32; have = true; }
-                    else { phase = 4; idx = 1 + lane; }
-                } else {
-                    if (idx <= NF) { p = edge_point(h.v2, h.nF, sd, idx); idx += 32; have = true; }
-                    else { phase = 5; }
-                }
+            if (have) {
+                if (s < NA) p = base_point(h, sd, s);
+                else if (s == NA) p = h.v1;
+                else if (s == NA + 1) p = h.v2;
+                else if (s < NA + 2 + NE) p = edge_point(h.v1, h.nE, sd, s - NA - 1);
+                else p = edge_point(h.v2, h.nF, sd, s - NA - 1 - NE);
             }
             const bool o = lane_out(have, p);
             if (have) ++nq;
-            if (__any_sync(0xffffffffu, o)) { out_found = true; break; }
-            if (__all_sync(0xffffffffu, !have)) break;
+            if (__any_sync(0xffffffffu, o)) return 1;
+        }
+        // ...then the rows 1..M, 32 at a time: each lane sets up one row
+        // (start point and last index), the reference's break (the first row
+        // with distance(v0_m, v1_m) <= sd) ends the rows, and the lanes walk
+        // the chunk's samples by flat index.
+        for (int base = 1; base <= h.M; base += 32) {
+            const int m = base + lane;
+            V3 v{0.0, 0.0, 0.0};
+            int N1 = -1;
+            const bool valid = m <= h.M;
+            const bool brk = valid && !sample_row(h, sd, m, v, N1);
+            const unsigned bal = __ballot_sync(0xffffffffu, brk);
+            const int first_brk = bal ? __ffs(bal) - 1 : 32;
+            int cnt = 0;
+            if (valid && lane < first_brk) {
+                if (N1 > (int)kMaxSamplesPerRow) {
+                    atomicOr(F.counters + kCntError, 2ULL);
+                } else {
+                    cnt = N1 + 1;
+                }
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int excl = incl - cnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int s0 = 0; s0 < total; s0 += 32) {
+                const int s = s0 + lane;
+                const bool have = s < total;
+                // the row holding flat index s: the last lane whose first index is
+                // <= s (first indices never decrease; empty rows share the next one's)
+                int r = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int c = r + step;
+                    const int ex = __shfl_sync(0xffffffffu, excl, c & 31);
+                    if (c < 32 && ex <= s) r = c;
+                }
+                const double vx = __shfl_sync(0xffffffffu, v.x, r);
+                const double vy = __shfl_sync(0xffffffffu, v.y, r);
+                const double vz = __shfl_sync(0xffffffffu, v.z, r);
+                const int ex = __shfl_sync(0xffffffffu, excl, r);
+                V3 p{0.0, 0.0, 0.0};
+                if (have) p = row_point(h, V3{vx, vy, vz}, sd, s - ex);
+                const bool o = lane_out(have, p);
+                if (have) ++nq;
+                if (__any_sync(0xffffffffu, o)) return 1;
+            }
+            if (bal) break;
         }
         return out_found ? 1 : 0;
     }
