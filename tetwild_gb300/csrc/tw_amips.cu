@@ -8,6 +8,7 @@
 // k_tet_quality_idx: calTetQualities over ids into the resident mesh
 // (LocalOperations.cpp:695-773): gathers the 4 vertices, orientation, energy
 // with the calTetQuality_AMIPS sentinel.
+#include <cstdint>
 #include <utility>
 
 #include "tw_device.cuh"
@@ -61,23 +62,14 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
 // in FP64 (amips_egh).  Outputs are FP64 like k_amips_soa.
 constexpr float kAmipsTol32 = 1e-5f;
 
+// One tet of the certified kernel: coordinates t in, outputs at index i.
 template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
-__global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict__ T, int64_t n,
-                                                        double* __restrict__ E,
-                                                        double* __restrict__ J,
-                                                        double* __restrict__ H,
-                                                        uint8_t* __restrict__ flip,
-                                                        unsigned long long* __restrict__ counters) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
-    uint32_t ntet = 0, nfp64 = 0, nexact = 0;
-    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane;
-    for (int64_t b = base0; b < n; b += stride) {
-        const int64_t i = b + lane;
-        if (i >= n) continue;
-        double t[12];
-#pragma unroll
-        for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
+__device__ __forceinline__ void amips_cert_tet(const double* t, int64_t i, int64_t n,
+                                               double* __restrict__ E, double* __restrict__ J,
+                                               double* __restrict__ H,
+                                               uint8_t* __restrict__ flip, uint32_t& ntet,
+                                               uint32_t& nfp64, uint32_t& nexact) {
+    {
         float d1[3], d2[3], d3[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -130,6 +122,10 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
             for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
         }
     }
+}
+
+__device__ __forceinline__ void flush_amips_stats(uint32_t ntet, uint32_t nfp64, uint32_t nexact,
+                                                  unsigned long long* counters) {
     unsigned long long a = ntet, f = nfp64, x = nexact;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -137,11 +133,147 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
         f += __shfl_xor_sync(0xffffffffu, f, o);
         x += __shfl_xor_sync(0xffffffffu, x, o);
     }
-    if (lane == 0) {
+    if ((threadIdx.x & 31) == 0) {
         if (a) atomicAdd(counters + kCntAmipsTets, a);
         if (f) atomicAdd(counters + kCntAmipsFp64, f);
         if (x) atomicAdd(counters + kCntExactOrient, x);
     }
+}
+
+template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
+__global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict__ T, int64_t n,
+                                                        double* __restrict__ E,
+                                                        double* __restrict__ J,
+                                                        double* __restrict__ H,
+                                                        uint8_t* __restrict__ flip,
+                                                        unsigned long long* __restrict__ counters) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    uint32_t ntet = 0, nfp64 = 0, nexact = 0;
+    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane;
+    for (int64_t b = base0; b < n; b += stride) {
+        const int64_t i = b + lane;
+        if (i >= n) continue;
+        double t[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact);
+    }
+    flush_amips_stats(ntet, nfp64, nexact, counters);
+}
+
+// ---------------------------------------------------------------------------
+// The same with the coordinates staged by the bulk-copy engine: tiles of 256
+// tets, the 12 SoA rows of a tile (2 KB each) copied into shared memory by
+// cp.async.bulk on an mbarrier, two tiles in flight per block while the
+// threads compute the previous one.  Needs n even and T 16-byte aligned (so
+// every row segment starts on a 16-byte boundary); partial tail tiles are
+// read directly.  A wait that does not complete within its iteration limit
+// sets error bit 32 and ends the block.
+// ---------------------------------------------------------------------------
+constexpr int kBulkTile = 256;
+constexpr int kBulkStages = 2;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// true when the barrier's phase with this parity completed within the limit
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 20); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n"
+            ".reg .pred p;\n"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n"
+            "}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
+__global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
+    const double* __restrict__ T, int64_t n, double* __restrict__ E, double* __restrict__ J,
+    double* __restrict__ H, uint8_t* __restrict__ flip, unsigned long long* __restrict__ counters) {
+    extern __shared__ __align__(128) double stage_mem[];   // kBulkStages x 12 x kBulkTile
+    double(*stage)[12 * kBulkTile] = reinterpret_cast<double(*)[12 * kBulkTile]>(stage_mem);
+    __shared__ __align__(8) uint64_t bar[kBulkStages];
+    __shared__ int abort_flag;
+    uint32_t ntet = 0, nfp64 = 0, nexact = 0;
+    const int64_t full = n / kBulkTile;               // full tiles
+    const int64_t ntiles = (n + kBulkTile - 1) / kBulkTile;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int64_t tile, int k) {
+        mbar_expect_tx(&bar[k], 12 * kBulkTile * 8);
+        for (int c = 0; c < 12; ++c)
+            bulk_g2s(&stage[k][c * kBulkTile], T + (int64_t)c * n + tile * kBulkTile,
+                     kBulkTile * 8, &bar[k]);
+    };
+    // prologue: the first kBulkStages tiles of this block
+    if (threadIdx.x == 0)
+        for (int k = 0; k < kBulkStages; ++k) {
+            const int64_t tile = blockIdx.x + (int64_t)k * gridDim.x;
+            if (tile < full) issue(tile, k);
+        }
+    uint32_t phase[kBulkStages] = {0, 0};
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t i = tile * kBulkTile + threadIdx.x;
+        double t[12];
+        if (tile < full) {
+            if (!mbar_wait(&bar[k], phase[k])) atomicExch(&abort_flag, 1);
+            phase[k] ^= 1u;
+            __syncthreads();
+            if (abort_flag) {
+                if (threadIdx.x == 0) atomicOr(counters + kCntError, 32ULL);
+                break;
+            }
+#pragma unroll
+            for (int c = 0; c < 12; ++c) t[c] = stage[k][c * kBulkTile + threadIdx.x];
+            __syncthreads();  // every thread has its coordinates: the stage may be refilled
+            if (threadIdx.x == 0) {
+                const int64_t next = tile + (int64_t)kBulkStages * gridDim.x;
+                if (next < full) issue(next, k);
+            }
+            k = (k + 1) % kBulkStages;
+        } else {
+            if (i >= n) continue;
+#pragma unroll
+            for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
+        }
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact);
+    }
+    flush_amips_stats(ntet, nfp64, nexact, counters);
 }
 
 int grid_for(int64_t n, int block, int blocks_per_sm) {
@@ -196,11 +328,41 @@ static AmipsKernel amips_cert_table(int bits, std::integer_sequence<int, B...>) 
     return table[bits];
 }
 
+template <int BITS>
+static AmipsKernel pick_amips_bulk() {
+    return k_amips_soa_cert_bulk<(BITS & 1) != 0, (BITS & 2) != 0, (BITS & 4) != 0,
+                                 (BITS & 8) != 0, (BITS & 16) != 0>;
+}
+
+template <int... B>
+static AmipsKernel amips_bulk_table(int bits, std::integer_sequence<int, B...>) {
+    static const AmipsKernel table[] = {pick_amips_bulk<B>()...};
+    return table[bits];
+}
+
 void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
                            uint8_t* flip, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0) return;
     int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
                ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
+    // bulk staging needs every row segment 16-byte aligned and is worth it
+    // for batches of at least a few tiles per SM; the coordinates must be in
+    // device memory (the copy engine path, not a host mapping)
+    cudaPointerAttributes a;
+    const bool device_mem = cudaPointerGetAttributes(&a, T) == cudaSuccess &&
+                            a.type == cudaMemoryTypeDevice;
+    if (!device_mem) cudaGetLastError();
+    if (device_mem && n % 2 == 0 && ((uintptr_t)T & 15) == 0 && n >= 64 * kBulkTile) {
+        AmipsKernel k = amips_bulk_table(bits, std::make_integer_sequence<int, 32>{});
+        const int smem = kBulkStages * 12 * kBulkTile * (int)sizeof(double);
+        static bool attr_set[32] = {};
+        if (!attr_set[bits]) {
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            attr_set[bits] = true;
+        }
+        k<<<grid_for(n, kBulkTile, 2), kBulkTile, smem, s>>>(T, n, E, J, H, flip, counters);
+        return;
+    }
     AmipsKernel k = amips_cert_table(bits, std::make_integer_sequence<int, 32>{});
     const int block = 256;
     int grid = grid_for(n, block, 8);
