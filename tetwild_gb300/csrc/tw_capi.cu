@@ -810,7 +810,7 @@ int tw_nearest_points_device(tw_ctx* c, const double* P, int64_t n, int which, d
     if (which != TW_SURFACE_INPUT && which != TW_SURFACE_BOUNDARY) return TW_ERR_ARG;
     if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
     Guard g(c->device);
-    launch_nearest_points(c->surf[which], P, n, Q, D, F, c->counters, c->stream);
+    launch_nearest_points(c->surf[which], c->eps2, P, n, Q, D, F, c->counters, c->stream);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_nearest_points_device");
     return TW_OK;
@@ -834,7 +834,7 @@ int tw_nearest_points(tw_ctx* c, const double* P, int64_t n, int which, double* 
     double* dD = (double*)q; q += align(8 * (size_t)n);
     int32_t* dF = (int32_t*)q;
     cudaMemcpyAsync(dP, P, 24 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
-    launch_nearest_points(c->surf[which], dP, n, Q ? dQ : nullptr, D ? dD : nullptr,
+    launch_nearest_points(c->surf[which], c->eps2, dP, n, Q ? dQ : nullptr, D ? dD : nullptr,
                           F ? dF : nullptr, c->counters, c->stream);
     if (Q) cudaMemcpyAsync(Q, dQ, 24 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
     if (D) cudaMemcpyAsync(D, dD, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
@@ -873,7 +873,8 @@ void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uin
                          c->newton_max_step, c->newton_max_it, out, S.pnew, status, c->stream);
     if (!any_surface) return;
     cudaMemsetAsync(S.face_count, 0, sizeof(unsigned long long), c->stream);
-    launch_smooth_project(c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], kinds, nstars,
+    launch_smooth_project(c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], c->eps2, kinds,
+                          nstars,
                           status, S.pnew, c->counters, c->stream);
     launch_smooth_stage2(c->newton_shape, c->vx, c->vy, c->vz, off, tets, ff, cen, nstars, S.pnew,
                          status, S.faces, S.face_count, S.face_cap, S.face_base, S.face_cnt,

@@ -1271,7 +1271,31 @@ __device__ int32_t nearest_facet(const EnvTree& T, const V3& p, V3& q, double& s
     return kTraversalError;
 }
 
-__global__ void k_nearest_points(EnvTree T, const double* __restrict__ P, int64_t n,
+// The nearest facet through the envelope grid: the minimum over the leaves of
+// the point's cell.  When that minimum is <= eps2 it is the minimum over all
+// facets (every facet within eps of the point is in the cell's list, see
+// EnvGrid), ties included; otherwise it returns false and the tree decides.
+__device__ __forceinline__ bool nearest_facet_grid(const EnvTree& T, double eps2, const V3& p,
+                                                   V3& q, double& sqd, int32_t& fid) {
+    if (!T.goff) return false;
+    CertQuery cq;
+    cq.ph[0] = d2f_rn(p.x);
+    cq.ph[1] = d2f_rn(p.y);
+    cq.ph[2] = d2f_rn(p.z);
+    uint32_t b, e;
+    grid_cell_range(T, cq, b, e);
+    double best = INFINITY;
+    int32_t best_id = 0x7fffffff;
+    V3 best_q{0.0, 0.0, 0.0};
+    for (uint32_t k = b; k < e; ++k) nearest_leaf(T, __ldg(T.glist + k), p, best, best_id, best_q);
+    if (!(best <= eps2)) return false;
+    q = best_q;
+    sqd = best;
+    fid = best_id;
+    return true;
+}
+
+__global__ void k_nearest_points(EnvTree T, double eps2, const double* __restrict__ P, int64_t n,
                                  double* __restrict__ Q, double* __restrict__ D,
                                  int32_t* __restrict__ Fo, unsigned long long* __restrict__ counters) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1279,7 +1303,8 @@ __global__ void k_nearest_points(EnvTree T, const double* __restrict__ P, int64_
         V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
         V3 q;
         double d;
-        int32_t f = nearest_facet(T, p, q, d);
+        int32_t f;
+        if (!nearest_facet_grid(T, eps2, p, q, d, f)) f = nearest_facet(T, p, q, d);
         if (f == kTraversalError) {
             atomicOr(counters + kCntError, 1ULL);
             q = p;
@@ -1508,11 +1533,12 @@ void launch_collapse_points(const Surface& Sin, const Surface& Sb, double eps2, 
             Ti, Tb, E, vx, vy, vz, v12, flags, n, status, degenerate, counters);
 }
 
-void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,
-                           int32_t* F, unsigned long long* counters, cudaStream_t s) {
+void launch_nearest_points(const Surface& S, double eps2, const double* P, int64_t n, double* Q,
+                           double* D, int32_t* F, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0 || S.nf <= 0) return;
     const int block = 128;
-    k_nearest_points<<<grid_for(n, block, 8), block, 0, s>>>(env_tree(S), P, n, Q, D, F, counters);
+    k_nearest_points<<<grid_for(n, block, 8), block, 0, s>>>(env_tree_for(S, eps2), eps2, P, n, Q,
+                                                             D, F, counters);
 }
 
 // Projection step of surface smoothing (VertexSmoother.cpp:353-363): every
@@ -1520,7 +1546,8 @@ void launch_nearest_points(const Surface& S, const double* P, int64_t n, double*
 // closest point of the nearest facet of the input surface (kind 1) or of the
 // boundary surface (kind 2).  A boundary star without a boundary surface is
 // an argument error (error bit 4) and is left invalid.
-__global__ void k_smooth_project(EnvTree Tin, EnvTree Tb, const uint8_t* __restrict__ kinds,
+__global__ void k_smooth_project(EnvTree Tin, EnvTree Tb, double eps2,
+                                 const uint8_t* __restrict__ kinds,
                                  int32_t nstars, uint8_t* __restrict__ status,
                                  double* __restrict__ pnew,
                                  unsigned long long* __restrict__ counters) {
@@ -1537,7 +1564,8 @@ __global__ void k_smooth_project(EnvTree Tin, EnvTree Tb, const uint8_t* __restr
         V3 p{pnew[3 * i], pnew[3 * i + 1], pnew[3 * i + 2]};
         V3 q;
         double d;
-        if (nearest_facet(T, p, q, d) == kTraversalError) {
+        int32_t f;
+        if (!nearest_facet_grid(T, eps2, p, q, d, f) && nearest_facet(T, p, q, d) == kTraversalError) {
             atomicOr(counters + kCntError, 1ULL);
             status[i] = TW_SMOOTH_INVALID;
             continue;
@@ -1548,13 +1576,14 @@ __global__ void k_smooth_project(EnvTree Tin, EnvTree Tb, const uint8_t* __restr
     }
 }
 
-void launch_smooth_project(const Surface& Sin, const Surface& Sb, const uint8_t* kinds,
-                           int32_t nstars, uint8_t* status, double* pnew,
+void launch_smooth_project(const Surface& Sin, const Surface& Sb, double eps2,
+                           const uint8_t* kinds, int32_t nstars, uint8_t* status, double* pnew,
                            unsigned long long* counters, cudaStream_t s) {
     if (nstars <= 0) return;
     const int block = 128;
-    k_smooth_project<<<grid_for(nstars, block, 8), block, 0, s>>>(env_tree(Sin), env_tree(Sb), kinds,
-                                                                 nstars, status, pnew, counters);
+    k_smooth_project<<<grid_for(nstars, block, 8), block, 0, s>>>(
+        env_tree_for(Sin, eps2), env_tree_for(Sb, eps2), eps2, kinds, nstars, status, pnew,
+        counters);
 }
 
 // One thread generates the full sample list in the reference order with the

@@ -222,10 +222,11 @@ void launch_env_points_segs(const double* P, int64_t n, const void* segs, int ns
                             int precision, unsigned long long* counters, cudaStream_t s);
 void launch_env_faces_segs(const double* tris, int64_t n, const void* segs, int nsegs, uint8_t* out,
                            int precision, unsigned long long* counters, cudaStream_t s);
-void launch_nearest_points(const Surface& S, const double* P, int64_t n, double* Q, double* D,
-                           int32_t* F, unsigned long long* counters, cudaStream_t s);
-void launch_smooth_project(const Surface& Sin, const Surface& Sb, const uint8_t* kinds,
-                           int32_t nstars, uint8_t* status, double* pnew,
+// eps2: the grid shortcut applies when a surface's grid was built for it
+void launch_nearest_points(const Surface& S, double eps2, const double* P, int64_t n, double* Q,
+                           double* D, int32_t* F, unsigned long long* counters, cudaStream_t s);
+void launch_smooth_project(const Surface& Sin, const Surface& Sb, double eps2,
+                           const uint8_t* kinds, int32_t nstars, uint8_t* status, double* pnew,
                            unsigned long long* counters, cudaStream_t s);
 
 // ---- launchers (tw_newton.cu) ----
