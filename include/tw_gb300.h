@@ -273,8 +273,6 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
  *   of the mean facet extent (default 0.25; the grid is rebuilt).
  * TW_TUNE_SORT_POINTS: 1 (default) orders point queries along the Morton
  *   curve before the certified test, 0 keeps the caller's order.
- * TW_TUNE_POINTS_PER_THREAD: 1 (default) or 2 points per thread in the
- *   certified point test (two interleaved cell walks per thread).
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.
@@ -282,7 +280,6 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 #define TW_TUNE_GRID_CELL 0
 #define TW_TUNE_SORT_POINTS 1
 #define TW_TUNE_TIME_KERNELS 2
-#define TW_TUNE_POINTS_PER_THREAD 3
 TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
 TW_API int tw_kernel_times(tw_ctx* ctx, float* ms, int max, int* count);
 

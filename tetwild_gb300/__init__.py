@@ -376,7 +376,6 @@ class Context:
     TUNE_SORT_POINTS = 1
 
     TUNE_TIME_KERNELS = 2
-    TUNE_POINTS_PER_THREAD = 3
 
     def set_tuning(self, knob: int, value: float):
         """Work-only knobs (TW_TUNE_*): results are the same for every value."""

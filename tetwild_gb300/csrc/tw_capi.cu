@@ -342,11 +342,6 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         c->sort_points = value != 0.0;
         return TW_OK;
     }
-    if (knob == TW_TUNE_POINTS_PER_THREAD) {
-        if (value != 1.0 && value != 2.0) return fail(c, TW_ERR_ARG, "points per thread: 1 or 2");
-        c->points_per_thread = (int)value;
-        return TW_OK;
-    }
     if (knob == TW_TUNE_TIME_KERNELS) {
         c->time_kernels = value != 0.0;
         c->time_count = 0;
@@ -672,7 +667,7 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
         ++c->time_count;
     }
     launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters,
-                      c->sort_points ? sort : nullptr, c->stream, eb, ee, c->points_per_thread);
+                      c->sort_points ? sort : nullptr, c->stream, eb, ee);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
     return TW_OK;
@@ -704,8 +699,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         const int64_t len = std::min<int64_t>(C, n - i0);
         cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
         launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->precision, c->counters,
-                          c->sort_points ? dS[k] : nullptr, s, nullptr, nullptr,
-                          c->points_per_thread);
+                          c->sort_points ? dS[k] : nullptr, s);
         cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
     }
     return sync_status(c, "tw_envelope_points");

@@ -413,48 +413,6 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __r
     flush_stats(st, counters, nq);
 }
 
-// Two points per thread (positions i and i + half of the grid's stride): the
-// two cell walks are interleaved so that each thread keeps two independent
-// chains of loads in flight.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_env_points_grid2(const double* __restrict__ P,
-                                                          const int32_t* __restrict__ order,
-                                                          int64_t n, EnvTree T, EpsParams E,
-                                                          uint8_t* __restrict__ out,
-                                                          unsigned long long* __restrict__ counters) {
-    const int64_t half = (int64_t)gridDim.x * blockDim.x;
-    const int64_t stride = 2 * half;
-    TravStats st;
-    uint32_t nq = 0;
-    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += stride) {
-        const int64_t i1 = i0 + half;
-        const bool v1 = i1 < n;
-        const int64_t j0 = order ? (int64_t)__ldg(order + i0) : i0;
-        const int64_t j1 = v1 ? (order ? (int64_t)__ldg(order + i1) : i1) : j0;
-        const V3 p0{__ldg(P + 3 * j0), __ldg(P + 3 * j0 + 1), __ldg(P + 3 * j0 + 2)};
-        const V3 p1{__ldg(P + 3 * j1), __ldg(P + 3 * j1 + 1), __ldg(P + 3 * j1 + 2)};
-        const CertQuery q0 = cert_query(p0, E, T.scale_hi);
-        const CertQuery q1 = cert_query(p1, E, T.scale_hi);
-        uint32_t b0, e0, b1 = 0, e1 = 0;
-        grid_cell_range(T, q0, b0, e0);
-        if (v1) grid_cell_range(T, q1, b1, e1);
-        bool in0 = false, in1 = !v1;
-        for (uint32_t k0 = b0, k1 = b1; (!in0 && k0 < e0) || (!in1 && k1 < e1); ++k0, ++k1) {
-            if (!in0 && k0 < e0)
-                in0 = cert_leaf_within(T.cull, T.tri, __ldg(T.glist + k0), p0, q0, E.eps2, st);
-            if (!in1 && k1 < e1)
-                in1 = cert_leaf_within(T.cull, T.tri, __ldg(T.glist + k1), p1, q1, E.eps2, st);
-        }
-        out[j0] = (uint8_t)!in0;
-        ++nq;
-        if (v1) {
-            out[j1] = (uint8_t)!in1;
-            ++nq;
-        }
-    }
-    flush_stats(st, counters, nq);
-}
-
 // ---- grid build ----------------------------------------------------------------------
 // Sum over facets of the largest box extent (for the cell size).
 __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
@@ -575,8 +533,7 @@ constexpr int64_t kSortMin = 4096;
 
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       cudaStream_t s, cudaEvent_t ev_begin, cudaEvent_t ev_end,
-                       int points_per_thread) {
+                       cudaStream_t s, cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     if (n <= 0) return;
     const int block = 128;
     const int32_t* order = nullptr;
@@ -602,10 +559,7 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff && points_per_thread == 2)
-        k_env_points_grid2<4><<<grid_for((n + 1) / 2, block, 16), block, 0, s>>>(P, order, n, T, E,
-                                                                                out, counters);
-    else if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
         k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)

@@ -130,7 +130,6 @@ struct tw_ctx {
     int time_count = 0;
     cudaEvent_t time_ev[2 * kTimeRing] = {};
     int sort_points = 1;     // Morton-order point queries (TW_TUNE_SORT_POINTS)
-    int points_per_thread = 1;  // certified point test, 1 or 2 (TW_TUNE_POINTS_PER_THREAD)
     tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
@@ -206,7 +205,7 @@ void free_env_grid(tw_ctx* c, EnvGrid& G);
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
                        cudaStream_t s, cudaEvent_t ev_begin = nullptr,
-                       cudaEvent_t ev_end = nullptr, int points_per_thread = 1);
+                       cudaEvent_t ev_end = nullptr);
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
 void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
