@@ -15,11 +15,14 @@
 // held its previous sample (the reference's prev_facet hint, :1080-1083),
 // and the warp stops at the first sample that is out.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_run_length_encode.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "tw_device.cuh"
 #include "tw_internal.h"
@@ -139,11 +142,13 @@ struct EnvTree {
     double scale;
     float scale_hi;  // scale rounded up to binary32
     const int32_t* facet_id;  // input facet index of each leaf
-    // the uniform grid of the certified test (goff == nullptr: none)
+    // the uniform grid of the certified test (gkey == nullptr: none)
     float glo[3];
     float ginv;
     int32_t gn[3];
-    const uint32_t* goff;
+    const uint32_t* gkey;
+    const uint2* grange;
+    uint32_t gshift, gmask;
     const int32_t* glist;
 };
 
@@ -176,7 +181,8 @@ static EnvTree env_tree(const Surface& S);
 static EnvTree env_tree_for(const Surface& S, double eps2) {
     EnvTree T = env_tree(S);
     if (S.grid.eps2 != eps2) {
-        T.goff = nullptr;
+        T.gkey = nullptr;
+        T.grange = nullptr;
         T.glist = nullptr;
     }
     return T;
@@ -189,7 +195,10 @@ static EnvTree env_tree(const Surface& S) {
         T.gn[k] = S.grid.n[k];
     }
     T.ginv = S.grid.inv_c;
-    T.goff = S.grid.off;
+    T.gkey = S.grid.key;
+    T.grange = S.grid.range;
+    T.gshift = S.grid.shift;
+    T.gmask = S.grid.mask;
     T.glist = S.grid.list;
     return T;
 }
@@ -370,9 +379,21 @@ __device__ __forceinline__ void grid_cell_range(const EnvTree& T, const CertQuer
         else i = min((int)t, T.gn[k] - 1);
         ix[k] = i;
     }
-    const int64_t cell = ((int64_t)ix[2] * T.gn[1] + ix[1]) * T.gn[0] + ix[0];
-    b = __ldg(T.goff + cell);
-    e = __ldg(T.goff + cell + 1);
+    const uint32_t cell = ((uint32_t)ix[2] * (uint32_t)T.gn[1] + (uint32_t)ix[1]) *
+                              (uint32_t)T.gn[0] + (uint32_t)ix[0];
+    uint32_t slot = (cell * 0x9E3779B1u) >> T.gshift;
+    b = e = 0;
+    for (uint32_t probe = 0; probe <= T.gmask; ++probe) {
+        const uint32_t k = __ldg(T.gkey + slot);
+        if (k == cell) {
+            const uint2 r = __ldg(T.grange + slot);
+            b = r.x;
+            e = r.x + r.y;
+            return;
+        }
+        if (k == 0xffffffffu) return;   // an empty cell: no leaf within reach
+        slot = (slot + 1) & T.gmask;
+    }
 }
 
 // in iff a leaf of the point's cell tests in; every lane of the warp calls it
@@ -434,13 +455,13 @@ __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
 }
 
-// Count (list == nullptr) or fill the cells of every leaf's grown box.  A
-// leaf spanning more than 2^16 cells marks the grid unsuitable (*too_big).
+// The cells of every leaf's grown box: counted (pairs == nullptr) or written
+// as (cell << 32 | leaf) pairs at an atomically reserved position.  A leaf
+// spanning more than 2^16 cells marks the grid unsuitable (*too_big).
 __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
                              double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
-                             double Rm, uint32_t* __restrict__ count,
-                             const uint32_t* __restrict__ off, int32_t* __restrict__ list,
-                             unsigned long long* __restrict__ total, int* __restrict__ too_big) {
+                             double Rm, unsigned long long* __restrict__ total,
+                             unsigned long long* __restrict__ pairs, int* __restrict__ too_big) {
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const double* t = tri + 9 * f;
@@ -461,14 +482,46 @@ __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double 
         if (too_big) atomicExch(too_big, 1);
         return;
     }
-    if (!list) atomicAdd(total, (unsigned long long)cells);
+    const unsigned long long base = atomicAdd(total, (unsigned long long)cells);
+    if (!pairs) return;
+    unsigned long long w = base;
     for (int z = i0[2]; z <= i1[2]; ++z)
         for (int y = i0[1]; y <= i1[1]; ++y)
             for (int x = i0[0]; x <= i1[0]; ++x) {
-                const int64_t cell = ((int64_t)z * n1 + y) * n0 + x;
-                const uint32_t k = atomicAdd(count + cell, 1u);
-                if (list) list[off[cell] + k] = (int32_t)f;
+                const uint32_t cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 +
+                                      (uint32_t)x;
+                pairs[w++] = ((unsigned long long)cell << 32) | (uint32_t)f;
             }
+}
+
+// Sorted pairs -> the cell of each entry and the leaf list.
+__global__ void k_grid_split(const unsigned long long* __restrict__ pairs, int64_t n,
+                             uint32_t* __restrict__ cells, int32_t* __restrict__ list) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long v = pairs[i];
+    cells[i] = (uint32_t)(v >> 32);
+    list[i] = (int32_t)(v & 0xffffffffu);
+}
+
+// Inserts the distinct cells into the hash table (bounded linear probing).
+__global__ void k_grid_insert(const uint32_t* __restrict__ uniq, const uint32_t* __restrict__ cnt,
+                              const uint32_t* __restrict__ start, const int* __restrict__ nuniq,
+                              uint32_t* __restrict__ key, uint2* __restrict__ range,
+                              uint32_t shift, uint32_t mask, int* __restrict__ failed) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nuniq) return;
+    const uint32_t c = uniq[i];
+    uint32_t slot = (c * 0x9E3779B1u) >> shift;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint32_t prev = atomicCAS(key + slot, 0xffffffffu, c);
+        if (prev == 0xffffffffu || prev == c) {
+            range[slot] = make_uint2(start[i], cnt[i]);
+            return;
+        }
+        slot = (slot + 1) & mask;
+    }
+    atomicExch(failed, 1);
 }
 
 // 30-bit Morton code of each query point on the tree's centroid grid
@@ -559,7 +612,7 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.goff)
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gkey)
         k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
@@ -790,7 +843,7 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
         // warp (see k_env_points_warp); -1 when above 32 (per-sample walks)
         int32_t cand = -1;
         int cnt = -1, kh = 0;
-        if (FP32 && !F.T.goff) {
+        if (FP32 && !F.T.gkey) {
             float qlo[3], qhi[3];
             const double t[9] = {h.vs[0].x, h.vs[0].y, h.vs[0].z, h.vs[1].x, h.vs[1].y,
                                  h.vs[1].z, h.vs[2].x, h.vs[2].y, h.vs[2].z};
@@ -804,7 +857,7 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
         }
         // out iff the lane's sample (have) is out; called by the whole warp
         auto lane_out = [&](bool have, const V3& p) -> bool {
-            if (FP32 && F.T.goff) {
+            if (FP32 && F.T.gkey) {
                 CertQuery q;
                 if (have) q = cert_query(p, F.E, F.T.scale_hi);
                 return have && !grid_point_in(F.T, F.E, have, p, q, st);
@@ -1106,7 +1159,7 @@ __global__ void __launch_bounds__(128) k_env_points_segs(const double* __restric
             const EnvTree T = g.T;
             const EpsParams E = g.E;
             V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
-            if (FP32 && T.goff) {
+            if (FP32 && T.gkey) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
                 out[i] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
             } else {
@@ -1277,7 +1330,7 @@ __device__ int32_t nearest_facet(const EnvTree& T, const V3& p, V3& q, double& s
 // EnvGrid), ties included; otherwise it returns false and the tree decides.
 __device__ __forceinline__ bool nearest_facet_grid(const EnvTree& T, double eps2, const V3& p,
                                                    V3& q, double& sqd, int32_t& fid) {
-    if (!T.goff) return false;
+    if (!T.gkey) return false;
     CertQuery cq;
     cq.ph[0] = d2f_rn(p.x);
     cq.ph[1] = d2f_rn(p.y);
@@ -1322,14 +1375,32 @@ __global__ void k_nearest_points(EnvTree T, double eps2, const double* __restric
 }
 
 void free_env_grid(tw_ctx* c, EnvGrid& G) {
-    if (G.off) dev_free(c, G.off, G.off_bytes);
+    if (G.key) dev_free(c, G.key, G.key_bytes);
+    if (G.range) dev_free(c, G.range, G.range_bytes);
     if (G.list) dev_free(c, G.list, G.list_bytes);
     G = EnvGrid{};
 }
 
+namespace {
+// Scratch blocks of a grid build, released on every exit path.
+struct BuildScratch {
+    tw_ctx* c;
+    std::vector<std::pair<void*, size_t>> blocks;
+    void* get(size_t bytes, int& st) {
+        void* p = nullptr;
+        st = dev_alloc(c, bytes, &p);
+        if (st == TW_OK) blocks.emplace_back(p, bytes);
+        return p;
+    }
+    ~BuildScratch() {
+        for (auto& b : blocks) dev_free(c, b.first, b.second);
+    }
+};
+}  // namespace
+
 int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaStream_t s) {
     if (S.nf <= 0 || !(eps2 >= 0.0)) return TW_OK;
-    if (S.grid.off && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
+    if (S.grid.key && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
     free_env_grid(c, S.grid);
     const int32_t nf = S.nf;
     // bounding box of the facets: the root's two child boxes, or the facet
@@ -1353,22 +1424,23 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
             bhi[k] = std::max(t[k], std::max(t[3 + k], t[6 + k]));
         }
     }
-    // acc: [0] sum of extents (double), [1] entry total, [2] too-big flag
-    void* acc = nullptr;
-    int st = dev_alloc(c, 32, &acc);
+    BuildScratch B{c, {}};
+    int st = TW_OK;
+    // acc: [0] sum of extents (double), [1] entry total, [2] too-big flag,
+    // [3] distinct cells, [4] insert failure
+    void* acc = B.get(64, st);
     if (st != TW_OK) return st;
     double* d_sum = (double*)acc;
     unsigned long long* d_total = (unsigned long long*)acc + 1;
     int* d_big = (int*)((unsigned long long*)acc + 2);
-    cudaMemsetAsync(acc, 0, 32, s);
+    int* d_nuniq = (int*)((unsigned long long*)acc + 3);
+    int* d_failed = (int*)((unsigned long long*)acc + 4);
+    cudaMemsetAsync(acc, 0, 64, s);
     k_grid_mean_extent<<<grid_for(nf, 256, 4), 256, 0, s>>>(S.tri, nf, d_sum);
     double sum_ext = 0.0;
     cudaMemcpyAsync(&sum_ext, d_sum, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        dev_free(c, acc, 32);
-        return cuda_fail(c, e, "grid build");
-    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
     // culling radius of any point of the grown box, plus the cell-index margin
     const double eps = std::sqrt(eps2);
     double M = S.scale;
@@ -1376,10 +1448,6 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     M = M + 2.0 * eps + 1e-300;
     const double Rm = eps * (1.0 + std::ldexp(1.0, -18)) + std::ldexp(M, -17);
     double cs = std::max(cell_factor * sum_ext / nf, 2.0 * Rm);
-    // at most 256 cells per facet (and 2^26 in all): the grid is dense, and
-    // a surface fills only a thin shell of it
-    const int64_t max_cells =
-        std::min<int64_t>(int64_t(1) << 26, std::max<int64_t>(int64_t(1) << 18, 256 * (int64_t)nf));
     int64_t n[3];
     float lo[3];
     float inv = 0.0f;
@@ -1394,67 +1462,94 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
             n[k] = (int64_t)std::floor((bhi[k] + Rm - (double)f) * (double)inv) + 2;
             cells *= n[k];
         }
-        if (cells <= max_cells) break;
+        if (cells < (int64_t(1) << 31)) break;
         cs *= 1.25;
     }
-    const int64_t ncells = n[0] * n[1] * n[2];
-    if (ncells > max_cells) {  // no grid: the tree walk serves the queries
-        dev_free(c, acc, 32);
-        return TW_OK;
-    }
-    void *cnt = nullptr, *off = nullptr, *temp = nullptr;
-    size_t temp_bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, temp_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                  (int)(ncells + 1), s);
-    const size_t off_bytes = 4 * (size_t)(ncells + 1);
-    if ((st = dev_alloc(c, off_bytes, &cnt)) != TW_OK) {
-        dev_free(c, acc, 32);
-        return st;
-    }
-    if ((st = dev_alloc(c, off_bytes, &off)) != TW_OK) {
-        dev_free(c, cnt, off_bytes);
-        dev_free(c, acc, 32);
-        return st;
-    }
-    if ((st = dev_alloc(c, temp_bytes + 16, &temp)) != TW_OK) {
-        dev_free(c, cnt, off_bytes);
-        dev_free(c, off, off_bytes);
-        dev_free(c, acc, 32);
-        return st;
-    }
-    const int B = 256;
-    const int G = (int)((nf + B - 1) / B);
-    cudaMemsetAsync(cnt, 0, off_bytes, s);
-    k_grid_cells<<<G, B, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                 (int32_t)n[1], (int32_t)n[2], Rm, (uint32_t*)cnt, nullptr, nullptr,
-                                 d_total, d_big);
-    cub::DeviceScan::ExclusiveSum(temp, temp_bytes, (const uint32_t*)cnt, (uint32_t*)off,
-                                  (int)(ncells + 1), s);
+    if (n[0] * n[1] * n[2] >= (int64_t(1) << 31)) return TW_OK;   // the tree walk serves
+    const int Bk = 256;
+    const int G = (int)((nf + Bk - 1) / Bk);
+    k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                  (int32_t)n[1], (int32_t)n[2], Rm, d_total, nullptr, d_big);
     unsigned long long hacc[2] = {0, 0};
     cudaMemcpyAsync(hacc, d_total, 16, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
-    dev_free(c, temp, temp_bytes + 16);
-    dev_free(c, acc, 32);
+    if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
     const unsigned long long total = hacc[0];
-    const bool unsuitable = (hacc[1] & 0xffffffffULL) != 0 || total > (1ULL << 28);
-    void* list = nullptr;
-    if (e == cudaSuccess && !unsuitable) st = dev_alloc(c, 4 * (size_t)total + 16, &list);
-    if (e != cudaSuccess || st != TW_OK || unsuitable) {
-        dev_free(c, cnt, off_bytes);
-        dev_free(c, off, off_bytes);
-        if (e != cudaSuccess) return cuda_fail(c, e, "grid build");
-        return unsuitable ? TW_OK : st;   // unsuitable: the tree walk serves the queries
+    // unsuitable (a leaf over too many cells, or too many entries): the tree walk serves
+    if ((hacc[1] & 0xffffffffULL) != 0 || total == 0 || total > (1ULL << 27)) return TW_OK;
+    const int64_t nt = (int64_t)total;
+    // pairs (cell << 32 | leaf), sorted: cells in order, leaves ascending within a cell
+    unsigned long long* pairs = (unsigned long long*)B.get(8 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    unsigned long long* pairs2 = (unsigned long long*)B.get(8 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    cudaMemsetAsync(d_total, 0, 8, s);
+    k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                  (int32_t)n[1], (int32_t)n[2], Rm, d_total, pairs, nullptr);
+    int key_bits = 32;
+    while (key_bits < 64 && (1ULL << (key_bits - 32)) < (unsigned long long)(n[0] * n[1] * n[2]))
+        ++key_bits;
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, tb, pairs, pairs2, (int)nt, 0, key_bits, s);
+    void* temp = B.get(tb + 16, st);
+    if (st != TW_OK) return st;
+    cub::DeviceRadixSort::SortKeys(temp, tb, pairs, pairs2, (int)nt, 0, key_bits, s);
+    // the entry cells (into the unsorted buffer) and the final leaf list
+    uint32_t* ecell = (uint32_t*)pairs;
+    void* listp = nullptr;
+    if ((st = dev_alloc(c, 4 * (size_t)nt + 16, &listp)) != TW_OK) return st;
+    int32_t* list = (int32_t*)listp;
+    k_grid_split<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(pairs2, nt, ecell, list);
+    // distinct cells, their counts and first entries (in the sorted buffer, read by now)
+    uint32_t* uniq = (uint32_t*)pairs2;
+    uint32_t* cnt = uniq + nt;
+    uint32_t* start = (uint32_t*)B.get(4 * (size_t)nt + 16, st);
+    size_t tb2 = 0, tb3 = 0;
+    void* temp2 = nullptr;
+    if (st == TW_OK) {
+        cub::DeviceRunLengthEncode::Encode(nullptr, tb2, ecell, uniq, cnt, d_nuniq, (int)nt, s);
+        cub::DeviceScan::ExclusiveSum(nullptr, tb3, cnt, start, (int)nt, s);
+        temp2 = B.get(std::max(tb2, tb3) + 16, st);
     }
-    cudaMemsetAsync(cnt, 0, off_bytes, s);
-    k_grid_cells<<<G, B, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                 (int32_t)n[1], (int32_t)n[2], Rm, (uint32_t*)cnt,
-                                 (const uint32_t*)off, (int32_t*)list, nullptr, nullptr);
+    if (st != TW_OK) {
+        dev_free(c, listp, 4 * (size_t)nt + 16);
+        return st;
+    }
+    cub::DeviceRunLengthEncode::Encode(temp2, tb2, ecell, uniq, cnt, d_nuniq, (int)nt, s);
+    int nuniq = 0;
+    cudaMemcpyAsync(&nuniq, d_nuniq, 4, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
-    dev_free(c, cnt, off_bytes);
-    if (e != cudaSuccess) {
-        dev_free(c, off, off_bytes);
-        dev_free(c, list, 4 * (size_t)total + 16);
-        return cuda_fail(c, e, "grid build");
+    if (e != cudaSuccess || nuniq <= 0) {
+        dev_free(c, listp, 4 * (size_t)nt + 16);
+        return e != cudaSuccess ? cuda_fail(c, e, "grid build") : TW_OK;
+    }
+    cub::DeviceScan::ExclusiveSum(temp2, tb3, cnt, start, nuniq, s);
+    // the hash table: a power of two at least twice the distinct cells
+    uint32_t bits = 1;
+    while ((1ULL << bits) < 2ULL * (unsigned long long)nuniq) ++bits;
+    const size_t H = size_t(1) << bits;
+    void *hk = nullptr, *hr = nullptr;
+    if ((st = dev_alloc(c, 4 * H, &hk)) != TW_OK) {
+        dev_free(c, listp, 4 * (size_t)nt + 16);
+        return st;
+    }
+    if ((st = dev_alloc(c, 8 * H, &hr)) != TW_OK) {
+        dev_free(c, listp, 4 * (size_t)nt + 16);
+        dev_free(c, hk, 4 * H);
+        return st;
+    }
+    cudaMemsetAsync(hk, 0xff, 4 * H, s);
+    k_grid_insert<<<(unsigned)((nuniq + 255) / 256), 256, 0, s>>>(
+        uniq, cnt, start, d_nuniq, (uint32_t*)hk, (uint2*)hr, 32 - bits, (uint32_t)(H - 1),
+        d_failed);
+    int failed = 0;
+    cudaMemcpyAsync(&failed, d_failed, 4, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || failed) {
+        dev_free(c, listp, 4 * (size_t)nt + 16);
+        dev_free(c, hk, 4 * H);
+        dev_free(c, hr, 8 * H);
+        return e != cudaSuccess ? cuda_fail(c, e, "grid build") : TW_OK;
     }
     EnvGrid& g = S.grid;
     for (int k = 0; k < 3; ++k) {
@@ -1462,12 +1557,16 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
         g.n[k] = (int32_t)n[k];
     }
     g.inv_c = inv;
-    g.off = (uint32_t*)off;
-    g.list = (int32_t*)list;
+    g.key = (uint32_t*)hk;
+    g.range = (uint2*)hr;
+    g.shift = 32 - bits;
+    g.mask = (uint32_t)(H - 1);
+    g.list = list;
     g.eps2 = eps2;
     g.cell_factor = cell_factor;
-    g.off_bytes = off_bytes;
-    g.list_bytes = 4 * (size_t)total + 16;
+    g.key_bytes = 4 * H;
+    g.range_bytes = 8 * H;
+    g.list_bytes = 4 * (size_t)nt + 16;
     return TW_OK;
 }
 
@@ -1504,7 +1603,7 @@ __global__ void k_collapse_points(EnvTree Tin, EnvTree Tb, EpsParams E,
                 break;
             }
             int32_t f;
-            if (FP32 && T.goff) {
+            if (FP32 && T.gkey) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
                 f = grid_point_in(T, E, true, p, q, st) ? 0 : -1;
             } else {
