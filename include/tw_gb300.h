@@ -271,8 +271,10 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 /* ---- tuning knobs (work only, never results) ---------------------------------------
  * TW_TUNE_GRID_CELL: cell size of the certified envelope grid as a multiple
  *   of the mean facet extent (default 0.25; the grid is rebuilt).
- * TW_TUNE_SORT_POINTS: 1 (default) orders point queries along the Morton
- *   curve before the certified test, 0 keeps the caller's order.
+ * TW_TUNE_SORT_POINTS: 1 (default) orders point queries by Morton cell of
+ *   the surface box before the test (a counting sort; 2^(3b) cells with the
+ *   smallest b in 3..8 that gives at least one cell per point), 2..8 fixes b,
+ *   0 keeps the caller's order.  Results never depend on it.
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.

@@ -339,7 +339,10 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         return TW_OK;
     }
     if (knob == TW_TUNE_SORT_POINTS) {
-        c->sort_points = value != 0.0;
+        if (!(value == 0.0 || value == 1.0 || (value >= 2.0 && value <= 8.0 &&
+                                               value == (double)(int)value)))
+            return fail(c, TW_ERR_ARG, "sort_points: 0, 1 or 2..8");
+        c->sort_points = (int)value;
         return TW_OK;
     }
     if (knob == TW_TUNE_TIME_KERNELS) {
@@ -653,7 +656,7 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
     if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
     Guard g(c->device);
     void* sort = nullptr;
-    int st = ensure(c, 3, env_sort_scratch_bytes(n), &sort);
+    int st = ensure(c, 3, env_sort_scratch_bytes(n, c->sort_points), &sort);
     if (st != TW_OK) return st;
     cudaEvent_t eb = nullptr, ee = nullptr;
     if (c->time_kernels) {
@@ -667,7 +670,7 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
         ++c->time_count;
     }
     launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters,
-                      c->sort_points ? sort : nullptr, c->stream, eb, ee);
+                      c->sort_points ? sort : nullptr, c->sort_points, c->stream, eb, ee);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
     return TW_OK;
@@ -689,7 +692,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         if (st != TW_OK) return st;
         dP[k] = (double*)p;
         dO[k] = (uint8_t*)p + 24 * (size_t)C;
-        st = ensure(c, 3 + k, env_sort_scratch_bytes(C), &dS[k]);
+        st = ensure(c, 3 + k, env_sort_scratch_bytes(C, c->sort_points), &dS[k]);
         if (st != TW_OK) return st;
     }
     int64_t chunk = 0;
@@ -699,7 +702,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         const int64_t len = std::min<int64_t>(C, n - i0);
         cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
         launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->precision, c->counters,
-                          c->sort_points ? dS[k] : nullptr, s);
+                          c->sort_points ? dS[k] : nullptr, c->sort_points, s);
         cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
     }
     return sync_status(c, "tw_envelope_points");

@@ -524,60 +524,82 @@ __global__ void k_grid_insert(const uint32_t* __restrict__ uniq, const uint32_t*
     atomicExch(failed, 1);
 }
 
-// 30-bit Morton code of each query point on the tree's centroid grid
-// (points outside the grid clamp to its faces).
-// The order only changes how much work the traversal does, never its
-// results, so it is computed in binary32 (integer-rounded inputs).
-__global__ void k_point_codes(const double* __restrict__ P, int64_t n, float lx, float ly,
-                              float lz, float sx, float sy, float sz,
-                              uint32_t* __restrict__ codes, int32_t* __restrict__ idx) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Point order for the traversal: a counting sort of the query points into the
+// 2^(3b) Morton cells of the surface box (b bits a side).  The order only
+// changes how much work the traversal does, never its results, so the bin
+// is computed in binary32 (integer-rounded inputs) and the order of points
+// within a bin is whatever the atomic increments give.
+__global__ void k_point_bins(const double* __restrict__ P, int64_t n, float lx, float ly,
+                             float lz, float sx, float sy, float sz, float side,
+                             uint2* __restrict__ bin_rank, uint32_t* __restrict__ count) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float c[3] = {(d2f_rn(__ldg(P + 3 * i)) - lx) * sx, (d2f_rn(__ldg(P + 3 * i + 1)) - ly) * sy,
-                  (d2f_rn(__ldg(P + 3 * i + 2)) - lz) * sz};
+    const float c[3] = {(d2f_rn(__ldg(P + 3 * i)) - lx) * sx,
+                        (d2f_rn(__ldg(P + 3 * i + 1)) - ly) * sy,
+                        (d2f_rn(__ldg(P + 3 * i + 2)) - lz) * sz};
     uint32_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        float v = c[k] * 1024.0f;
-        v = fminf(fmaxf(v, 0.0f), 1023.0f);  // NaN -> 0
+        const float v = fminf(fmaxf(c[k] * side, 0.0f), side - 1.0f);   // NaN -> 0
         q[k] = (uint32_t)v;
     }
-    codes[i] = (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
-    idx[i] = (int32_t)i;
+    const uint32_t bin =
+        (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
+    bin_rank[i] = make_uint2(bin, atomicAdd(count + bin, 1u));
+}
+
+// idx[first of bin + rank] = i, with count holding each bin's first position
+__global__ void k_point_place(const uint2* __restrict__ bin_rank, int64_t n,
+                              const uint32_t* __restrict__ first, int32_t* __restrict__ idx) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 br = bin_rank[i];
+    idx[__ldg(first + br.x) + br.y] = (int32_t)i;
+}
+
+// bits a side of the sort grid: the knob (2..8), or the smallest b with
+// 2^(3b) >= n, between 3 and 8 (8: cells of 1/256 of the box, about one
+// envelope-grid cell on a 100k-facet surface)
+static int sort_bits(int64_t n, int knob) {
+    if (knob >= 2) return std::min(knob, 8);
+    int b = 3;
+    while (b < 8 && (int64_t(1) << (3 * b)) < n) ++b;
+    return b;
 }
 
 struct SortLayout {
-    uint32_t* codes;
-    uint32_t* codes2;
+    uint2* bin_rank;
     int32_t* idx;
-    int32_t* idx2;
+    uint32_t* count;
+    int64_t nbins;
     void* temp;
     size_t temp_bytes;
 };
 
-static size_t cub_sort_bytes(int64_t n) {
+static size_t cub_scan_bytes(int64_t nbins) {
     size_t b = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, b, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                    (int32_t*)nullptr, (int32_t*)nullptr, (int)n, 6, 30);
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (uint32_t*)nullptr, (int)nbins);
     return b;
 }
 
-static SortLayout sort_layout(void* base, int64_t n) {
+static SortLayout sort_layout(void* base, int64_t n, int knob) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     char* q = static_cast<char*>(base);
     SortLayout L;
-    L.codes = (uint32_t*)q; q += al(4 * (size_t)n);
-    L.codes2 = (uint32_t*)q; q += al(4 * (size_t)n);
+    L.nbins = int64_t(1) << (3 * sort_bits(n, knob));
+    L.bin_rank = (uint2*)q; q += al(8 * (size_t)n);
     L.idx = (int32_t*)q; q += al(4 * (size_t)n);
-    L.idx2 = (int32_t*)q; q += al(4 * (size_t)n);
+    L.count = (uint32_t*)q; q += al(4 * (size_t)L.nbins);
     L.temp = q;
-    L.temp_bytes = cub_sort_bytes(n);
+    L.temp_bytes = cub_scan_bytes(L.nbins);
     return L;
 }
 
-size_t env_sort_scratch_bytes(int64_t n) {
+size_t env_sort_scratch_bytes(int64_t n, int knob) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    return 4 * al(4 * (size_t)n) + al(cub_sort_bytes(n)) + 256;
+    const int64_t nbins = int64_t(1) << (3 * sort_bits(n, knob));
+    return al(8 * (size_t)n) + al(4 * (size_t)n) + al(4 * (size_t)nbins) +
+           al(cub_scan_bytes(nbins)) + 256;
 }
 
 // Batches below this size are traversed in input order (sorting would cost
@@ -586,26 +608,28 @@ constexpr int64_t kSortMin = 4096;
 
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       cudaStream_t s, cudaEvent_t ev_begin, cudaEvent_t ev_end) {
+                       int sort_knob, cudaStream_t s, cudaEvent_t ev_begin,
+                       cudaEvent_t ev_end) {
     if (n <= 0) return;
     const int block = 128;
     const int32_t* order = nullptr;
     if (sort_scratch && n >= kSortMin && n <= INT32_MAX) {
-        SortLayout L = sort_layout(sort_scratch, n);
+        SortLayout L = sort_layout(sort_scratch, n, sort_knob);
         double sc[3];
         for (int k = 0; k < 3; ++k) {
             double ext = S.hi[k] - S.lo[k];
             sc[k] = ext > 0.0 ? 1.0 / ext : 0.0;
         }
-        k_point_codes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-            P, n, (float)S.lo[0], (float)S.lo[1], (float)S.lo[2], (float)sc[0], (float)sc[1],
-            (float)sc[2], L.codes, L.idx);
+        const unsigned nb = (unsigned)((n + 255) / 256);
+        cudaMemsetAsync(L.count, 0, 4 * (size_t)L.nbins, s);
+        k_point_bins<<<nb, 256, 0, s>>>(P, n, (float)S.lo[0], (float)S.lo[1], (float)S.lo[2],
+                                        (float)sc[0], (float)sc[1], (float)sc[2],
+                                        std::ldexp(1.0f, sort_bits(n, sort_knob)),
+                                        L.bin_rank, L.count);
         size_t tb = L.temp_bytes;
-        // the top 24 bits (cells of 1/256 of the box, about one grid cell):
-        // three 8-bit passes instead of four; the order changes only the work
-        cub::DeviceRadixSort::SortPairs(L.temp, tb, L.codes, L.codes2, L.idx, L.idx2, (int)n, 6, 30,
-                                        s);
-        order = L.idx2;
+        cub::DeviceScan::ExclusiveSum(L.temp, tb, L.count, (int)L.nbins, s);
+        k_point_place<<<nb, 256, 0, s>>>(L.bin_rank, n, L.count, L.idx);
+        order = L.idx;
     }
     const EnvTree T = env_tree_for(S, eps2);
     const EpsParams E = eps_params(eps2);

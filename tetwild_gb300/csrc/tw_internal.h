@@ -94,10 +94,11 @@ struct Surface {
     EnvGrid grid;
 };
 
-// Device scratch for ordering query points along the Morton curve before
-// traversal: codes, permutation (double-buffered) and the radix-sort
-// temporaries.  Sized by env_sort_scratch_bytes(n).
-size_t env_sort_scratch_bytes(int64_t n);
+// Device scratch for ordering query points by Morton cell before traversal
+// (a counting sort): bin and rank per point, the permutation, the bin counts
+// and the scan temporaries.  knob: the sort_points tuning value (1 = bins
+// sized from n, 2..8 = bits a side).
+size_t env_sort_scratch_bytes(int64_t n, int knob);
 
 // Device memory block owned by a context, grown on demand.
 struct Buffer {
@@ -205,13 +206,13 @@ void free_env_grid(tw_ctx* c, EnvGrid& G);
 // ---- launchers (tw_envelope.cu) ----
 // err: device word; bit 0 = traversal exceeded its bounds, bit 1 = a face
 // exceeded the per-row sample bound.
-// sort_scratch (env_sort_scratch_bytes(n) bytes) enables Morton-ordered
+// sort_scratch (env_sort_scratch_bytes(n, sort_knob) bytes) enables Morton-ordered
 // traversal; with nullptr the points are traversed in input order.
 // precision: TW_PRECISION_FP64 or TW_PRECISION_FP32_CERTIFIED; counters is
 // the context's counter array (error word and statistics).
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       cudaStream_t s, cudaEvent_t ev_begin = nullptr,
+                       int sort_knob, cudaStream_t s, cudaEvent_t ev_begin = nullptr,
                        cudaEvent_t ev_end = nullptr);
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
