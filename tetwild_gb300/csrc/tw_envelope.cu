@@ -424,10 +424,12 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __r
     for (int64_t b = base0; b < n; b += stride) {
         const int64_t i = b + (threadIdx.x & 31);
         if (i < n) {
-            const int64_t j = order ? (int64_t)__ldg(order + i) : i;
-            const V3 p{__ldg(P + 3 * j), __ldg(P + 3 * j + 1), __ldg(P + 3 * j + 2)};
+            // the points, the order and the answers stream through once
+            // (evict-first), so the facet records and cell lists stay in L2
+            const int64_t j = order ? (int64_t)__ldcs(order + i) : i;
+            const V3 p{__ldcs(P + 3 * j), __ldcs(P + 3 * j + 1), __ldcs(P + 3 * j + 2)};
             const CertQuery q = cert_query(p, E, T.scale_hi);
-            out[j] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
+            __stcs(out + j, (uint8_t)!grid_point_in(T, E, true, p, q, st));
             ++nq;
         }
     }
@@ -534,9 +536,9 @@ __global__ void k_point_bins(const double* __restrict__ P, int64_t n, float lx, 
                              uint2* __restrict__ bin_rank, uint32_t* __restrict__ count) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float c[3] = {(d2f_rn(__ldg(P + 3 * i)) - lx) * sx,
-                        (d2f_rn(__ldg(P + 3 * i + 1)) - ly) * sy,
-                        (d2f_rn(__ldg(P + 3 * i + 2)) - lz) * sz};
+    const float c[3] = {(d2f_rn(__ldcs(P + 3 * i)) - lx) * sx,
+                        (d2f_rn(__ldcs(P + 3 * i + 1)) - ly) * sy,
+                        (d2f_rn(__ldcs(P + 3 * i + 2)) - lz) * sz};
     uint32_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -553,7 +555,7 @@ __global__ void k_point_place(const uint2* __restrict__ bin_rank, int64_t n,
                               const uint32_t* __restrict__ first, int32_t* __restrict__ idx) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint2 br = bin_rank[i];
+    const uint2 br = __ldcs(bin_rank + i);
     idx[__ldg(first + br.x) + br.y] = (int32_t)i;
 }
 
