@@ -402,11 +402,16 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
     uint32_t b = 0, e = 0;
     if (valid) grid_cell_range(T, q, b, e);
     bool in = false;
+    // the next list entry is loaded while the current facet is tested, so
+    // each test waits on one load (its record) instead of two
+    int32_t lf = b < e ? __ldg(T.glist + b) : 0;
     for (uint32_t k = b; k < e; ++k) {
-        if (cert_leaf_within(T.cull, T.tri, __ldg(T.glist + k), p, q, E.eps2, st)) {
+        const int32_t next = k + 1 < e ? __ldg(T.glist + k + 1) : 0;
+        if (cert_leaf_within(T.cull, T.tri, lf, p, q, E.eps2, st)) {
             in = true;
             break;
         }
+        lf = next;
     }
     return in;
 }
