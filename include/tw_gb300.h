@@ -275,6 +275,10 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
  *   the surface box before the test (a counting sort; 2^(3b) cells with the
  *   smallest b in 3..8 that gives at least one cell per point), 2..8 fixes b,
  *   0 keeps the caller's order.  Results never depend on it.
+ * TW_TUNE_POINT_BLOCK: threads per block of the certified grid point test
+ *   (128, 256, 384 default, or 768; 768 resident threads per SM in each): the
+ *   warps of a block test neighbouring sorted points together.  Results never
+ *   depend on it.
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.
@@ -282,6 +286,7 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 #define TW_TUNE_GRID_CELL 0
 #define TW_TUNE_SORT_POINTS 1
 #define TW_TUNE_TIME_KERNELS 2
+#define TW_TUNE_POINT_BLOCK 3
 TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
 TW_API int tw_kernel_times(tw_ctx* ctx, float* ms, int max, int* count);
 

@@ -374,8 +374,8 @@ class Context:
     NEWTON_SHAPES = 10
     TUNE_GRID_CELL = 0
     TUNE_SORT_POINTS = 1
-
     TUNE_TIME_KERNELS = 2
+    TUNE_POINT_BLOCK = 3
 
     def set_tuning(self, knob: int, value: float):
         """Work-only knobs (TW_TUNE_*): results are the same for every value."""

@@ -345,6 +345,12 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         c->sort_points = (int)value;
         return TW_OK;
     }
+    if (knob == TW_TUNE_POINT_BLOCK) {
+        if (!(value == 128.0 || value == 256.0 || value == 384.0 || value == 768.0))
+            return fail(c, TW_ERR_ARG, "point_block: 128, 256, 384 or 768");
+        c->point_block = (int)value;
+        return TW_OK;
+    }
     if (knob == TW_TUNE_TIME_KERNELS) {
         c->time_kernels = value != 0.0;
         c->time_count = 0;
@@ -670,7 +676,8 @@ int tw_envelope_points_device(tw_ctx* c, const double* P, int64_t n, int which, 
         ++c->time_count;
     }
     launch_env_points(c->surf[which], P, n, c->eps2, out, c->precision, c->counters,
-                      c->sort_points ? sort : nullptr, c->sort_points, c->stream, eb, ee);
+                      c->sort_points ? sort : nullptr, c->sort_points, c->point_block, c->stream,
+                      eb, ee);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_envelope_points_device");
     return TW_OK;
@@ -702,7 +709,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
         const int64_t len = std::min<int64_t>(C, n - i0);
         cudaMemcpyAsync(dP[k], P + 3 * i0, 24 * (size_t)len, cudaMemcpyHostToDevice, s);
         launch_env_points(c->surf[which], dP[k], len, c->eps2, dO[k], c->precision, c->counters,
-                          c->sort_points ? dS[k] : nullptr, c->sort_points, s);
+                          c->sort_points ? dS[k] : nullptr, c->sort_points, c->point_block, s);
         cudaMemcpyAsync(out + i0, dO[k], (size_t)len, cudaMemcpyDeviceToHost, s);
     }
     return sync_status(c, "tw_envelope_points");

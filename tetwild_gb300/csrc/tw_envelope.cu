@@ -416,18 +416,22 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
     return in;
 }
 
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_env_points_grid(const double* __restrict__ P,
-                                                         const int32_t* __restrict__ order,
-                                                         int64_t n, EnvTree T, EpsParams E,
-                                                         uint8_t* __restrict__ out,
-                                                         unsigned long long* __restrict__ counters) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+// Block b's warps take 32-point groups b*W .. b*W+W-1 together (W warps per
+// block), then stride by the grid: in Morton order the warps of a block test
+// neighbouring cells at the same time and share their facet records in L1.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_env_points_grid(const double* __restrict__ P,
+                                                           const int32_t* __restrict__ order,
+                                                           int64_t n, EnvTree T, EpsParams E,
+                                                           uint8_t* __restrict__ out,
+                                                           unsigned long long* __restrict__ counters) {
     TravStats st;
     uint32_t nq = 0;
-    const int64_t base0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - (threadIdx.x & 31);
-    for (int64_t b = base0; b < n; b += stride) {
-        const int64_t i = b + (threadIdx.x & 31);
+    const int64_t groups = (n + 31) >> 5;
+    const int64_t warps = (int64_t)gridDim.x * (BLOCK / 32);
+    for (int64_t g = (int64_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5); g < groups;
+         g += warps) {
+        const int64_t i = (g << 5) + (threadIdx.x & 31);
         if (i < n) {
             // the points, the order and the answers stream through once
             // (evict-first), so the facet records and cell lists stay in L2
@@ -615,7 +619,7 @@ constexpr int64_t kSortMin = 4096;
 
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       int sort_knob, cudaStream_t s, cudaEvent_t ev_begin,
+                       int sort_knob, int point_block, cudaStream_t s, cudaEvent_t ev_begin,
                        cudaEvent_t ev_end) {
     if (n <= 0) return;
     const int block = 128;
@@ -643,9 +647,26 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gkey)
-        k_env_points_grid<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
-                                                                      counters);
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gkey) {
+        // 768 resident threads per SM (85 registers) in every block shape
+        switch (point_block) {
+        case 256:
+            k_env_points_grid<256, 3><<<grid_for(n, 256, 8), 256, 0, s>>>(P, order, n, T, E, out,
+                                                                        counters);
+            break;
+        case 128:
+            k_env_points_grid<128, 6><<<grid_for(n, 128, 16), 128, 0, s>>>(P, order, n, T, E, out,
+                                                                         counters);
+            break;
+        case 768:
+            k_env_points_grid<768, 1><<<grid_for(n, 768, 3), 768, 0, s>>>(P, order, n, T, E, out,
+                                                                        counters);
+            break;
+        default:   // 384: measured best of the four on 10M points (1.11 vs 1.15 ms at 128)
+            k_env_points_grid<384, 2><<<grid_for(n, 384, 6), 384, 0, s>>>(P, order, n, T, E, out,
+                                                                        counters);
+        }
+    }
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
         k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
                                                                       counters);

@@ -138,6 +138,7 @@ struct tw_ctx {
     int time_count = 0;
     cudaEvent_t time_ev[2 * kTimeRing] = {};
     int sort_points = 1;     // Morton-order point queries (TW_TUNE_SORT_POINTS)
+    int point_block = 384;   // threads per block of the certified grid test (TW_TUNE_POINT_BLOCK)
     tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
@@ -212,7 +213,7 @@ void free_env_grid(tw_ctx* c, EnvGrid& G);
 // the context's counter array (error word and statistics).
 void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2, uint8_t* out,
                        int precision, unsigned long long* counters, void* sort_scratch,
-                       int sort_knob, cudaStream_t s, cudaEvent_t ev_begin = nullptr,
+                       int sort_knob, int point_block, cudaStream_t s, cudaEvent_t ev_begin = nullptr,
                        cudaEvent_t ev_end = nullptr);
 void launch_env_faces(const Surface& S, const double* tris, int64_t n, double eps2, double sd,
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s);
