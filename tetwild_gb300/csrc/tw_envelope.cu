@@ -1120,7 +1120,7 @@ __device__ __forceinline__ void k_env_faces_body(const double* __restrict__ tris
 }
 
 template <bool FP32>
-__global__ void __launch_bounds__(128) k_env_faces(const double* __restrict__ tris, int64_t n,
+__global__ void __launch_bounds__(128, 4) k_env_faces(const double* __restrict__ tris, int64_t n,
                                                    FaceCtx F, double sd, uint8_t* __restrict__ out) {
     k_env_faces_body<FP32>(tris, n, F, sd, out);
 }
@@ -1129,7 +1129,7 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
                       uint8_t* out, int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0) return;
     const int block = kFaceBlock;
-    int grid = grid_for(n, block, 3);
+    int grid = grid_for(n, block, 4);
     FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED) {
         k_env_faces<true><<<grid, block, 0, s>>>(tris, n, F, sd, out);
@@ -1141,7 +1141,7 @@ void launch_env_faces(const Surface& S, const double* tris, int64_t n, double ep
 // Envelope faces whose count is known only on the device (*n_dev, at most
 // cap): the grid is sized for cap and the warps beyond *n_dev exit at once.
 template <bool FP32>
-__global__ void __launch_bounds__(128) k_env_faces_dev(const double* __restrict__ tris,
+__global__ void __launch_bounds__(128, 4) k_env_faces_dev(const double* __restrict__ tris,
                                                        const unsigned long long* __restrict__ n_dev,
                                                        int64_t cap, FaceCtx F, double sd,
                                                        uint8_t* __restrict__ out) {
@@ -1154,7 +1154,7 @@ void launch_env_faces_dev(const Surface& S, const double* tris, const unsigned l
                           unsigned long long* counters, cudaStream_t s) {
     if (cap <= 0) return;
     const int block = kFaceBlock;
-    int grid = grid_for(cap, block, 3);
+    int grid = grid_for(cap, block, 4);
     FaceCtx F{env_tree_for(S, eps2), eps_params(eps2), counters};
     if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_faces_dev<true><<<grid, block, 0, s>>>(tris, n_dev, cap, F, sd, out);
@@ -1226,7 +1226,7 @@ __global__ void __launch_bounds__(128) k_env_points_segs(const double* __restric
 }
 
 template <bool FP32>
-__global__ void __launch_bounds__(128) k_env_faces_segs(const double* __restrict__ tris, int64_t n,
+__global__ void __launch_bounds__(128, 4) k_env_faces_segs(const double* __restrict__ tris, int64_t n,
                                                         const EnvSeg* __restrict__ segs, int nsegs,
                                                         uint8_t* __restrict__ out,
                                                         unsigned long long* __restrict__ counters) {
@@ -1257,7 +1257,7 @@ void launch_env_faces_segs(const double* tris, int64_t n, const void* segs, int 
                            int precision, unsigned long long* counters, cudaStream_t s) {
     if (n <= 0 || nsegs <= 0) return;
     const int block = kFaceBlock;
-    const int grid = grid_for(n, block, 3);
+    const int grid = grid_for(n, block, 4);
     const EnvSeg* g = static_cast<const EnvSeg*>(segs);
     if (precision == TW_PRECISION_FP32_CERTIFIED)
         k_env_faces_segs<true><<<grid, block, 0, s>>>(tris, n, g, nsegs, out, counters);
