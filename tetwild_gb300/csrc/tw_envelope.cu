@@ -142,12 +142,11 @@ struct EnvTree {
     double scale;
     float scale_hi;  // scale rounded up to binary32
     const int32_t* facet_id;  // input facet index of each leaf
-    // the uniform grid of the certified test (gkey == nullptr: none)
+    // the uniform grid of the certified test (gslot == nullptr: none)
     float glo[3];
     float ginv;
     int32_t gn[3];
-    const uint32_t* gkey;
-    const uint2* grange;
+    const uint4* gslot;   // (cell, first entry, count, -) per hash slot
     uint32_t gshift, gmask;
     const int32_t* glist;
 };
@@ -181,8 +180,7 @@ static EnvTree env_tree(const Surface& S);
 static EnvTree env_tree_for(const Surface& S, double eps2) {
     EnvTree T = env_tree(S);
     if (S.grid.eps2 != eps2) {
-        T.gkey = nullptr;
-        T.grange = nullptr;
+        T.gslot = nullptr;
         T.glist = nullptr;
     }
     return T;
@@ -195,8 +193,7 @@ static EnvTree env_tree(const Surface& S) {
         T.gn[k] = S.grid.n[k];
     }
     T.ginv = S.grid.inv_c;
-    T.gkey = S.grid.key;
-    T.grange = S.grid.range;
+    T.gslot = S.grid.slot;
     T.gshift = S.grid.shift;
     T.gmask = S.grid.mask;
     T.glist = S.grid.list;
@@ -384,14 +381,13 @@ __device__ __forceinline__ void grid_cell_range(const EnvTree& T, const CertQuer
     uint32_t slot = (cell * 0x9E3779B1u) >> T.gshift;
     b = e = 0;
     for (uint32_t probe = 0; probe <= T.gmask; ++probe) {
-        const uint32_t k = __ldg(T.gkey + slot);
-        if (k == cell) {
-            const uint2 r = __ldg(T.grange + slot);
-            b = r.x;
-            e = r.x + r.y;
+        const uint4 r = __ldg(T.gslot + slot);   // key and range in one load
+        if (r.x == cell) {
+            b = r.y;
+            e = r.y + r.z;
             return;
         }
-        if (k == 0xffffffffu) return;   // an empty cell: no leaf within reach
+        if (r.x == 0xffffffffu) return;   // an empty cell: no leaf within reach
         slot = (slot + 1) & T.gmask;
     }
 }
@@ -466,16 +462,71 @@ __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
 }
 
-// The cells of every leaf's grown box: counted (pairs == nullptr) or written
-// as (cell << 32 | leaf) pairs at an atomically reserved position.  A leaf
-// spanning more than 2^16 cells marks the grid unsuitable (*too_big).
+// Separating-axis test of triangle t against the axis-aligned cube of
+// half-size h centred at c (the three box axes, the triangle's normal and the
+// nine edge x box-axis products): false only when an axis separates them.
+// The cube grown by R contains the ball of radius R around every point of
+// the cell, so a facet it excludes is farther than R from the whole cell.
+__device__ bool tri_cube_overlap(const double* t, const double* c, double h) {
+    double v[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[i][k] = t[3 * i + k] - c[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (fmin(v[0][k], fmin(v[1][k], v[2][k])) > h) return false;
+        if (fmax(v[0][k], fmax(v[1][k], v[2][k])) < -h) return false;
+    }
+    double e[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e[0][k] = v[1][k] - v[0][k];
+        e[1][k] = v[2][k] - v[1][k];
+        e[2][k] = v[0][k] - v[2][k];
+    }
+    {
+        const double nx = e[0][1] * e[1][2] - e[0][2] * e[1][1];
+        const double ny = e[0][2] * e[1][0] - e[0][0] * e[1][2];
+        const double nz = e[0][0] * e[1][1] - e[0][1] * e[1][0];
+        const double d = nx * v[0][0] + ny * v[0][1] + nz * v[0][2];
+        if (fabs(d) > h * (fabs(nx) + fabs(ny) + fabs(nz))) return false;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            // axis = unit_k x e_j
+            double ax[3];
+            const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+            ax[k] = 0.0;
+            ax[k1] = -e[j][k2];
+            ax[k2] = e[j][k1];
+            const double p0 = ax[k1] * v[0][k1] + ax[k2] * v[0][k2];
+            const double p1 = ax[k1] * v[1][k1] + ax[k2] * v[1][k2];
+            const double p2 = ax[k1] * v[2][k1] + ax[k2] * v[2][k2];
+            const double r = h * (fabs(ax[k1]) + fabs(ax[k2]));
+            if (fmin(p0, fmin(p1, p2)) > r || fmax(p0, fmax(p1, p2)) < -r) return false;
+        }
+    }
+    return true;
+}
+
+// The cells within reach of every leaf: the cells of its box grown by Rm
+// that the separating-axis test cannot separate from the triangle (cube
+// half-size cell/2 + Rm + 2^-30 M, the last term covering the rounding of
+// the test), counted (pairs == nullptr) or written as (cell << 32 | leaf)
+// pairs at an atomically reserved position.  A leaf whose box spans more
+// than 2^16 cells marks the grid unsuitable (*too_big).
 __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
                              double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
-                             double Rm, unsigned long long* __restrict__ total,
+                             double Rm, double slack, unsigned long long* __restrict__ total,
                              unsigned long long* __restrict__ pairs, int* __restrict__ too_big) {
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
-    const double* t = tri + 9 * f;
+    double t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9 * f + k);
     const double lo[3] = {lo0, lo1, lo2};
     const int32_t n[3] = {n0, n1, n2};
     int i0[3], i1[3];
@@ -488,17 +539,30 @@ __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double 
         i0[k] = (int)u;
         i1[k] = (int)v;
     }
-    const int64_t cells = (int64_t)(i1[0] - i0[0] + 1) * (i1[1] - i0[1] + 1) * (i1[2] - i0[2] + 1);
-    if (cells > 65536) {
+    const int64_t box = (int64_t)(i1[0] - i0[0] + 1) * (i1[1] - i0[1] + 1) * (i1[2] - i0[2] + 1);
+    if (box > 65536) {
         if (too_big) atomicExch(too_big, 1);
         return;
     }
-    const unsigned long long base = atomicAdd(total, (unsigned long long)cells);
+    const double cs = 1.0 / inv_c;
+    const double h = 0.5 * cs + Rm + slack;
+    auto within = [&](int x, int y, int z) {
+        const double c[3] = {lo0 + ((double)x + 0.5) * cs, lo1 + ((double)y + 0.5) * cs,
+                             lo2 + ((double)z + 0.5) * cs};
+        return tri_cube_overlap(t, c, h);
+    };
+    unsigned long long cnt = 0;
+    for (int z = i0[2]; z <= i1[2]; ++z)
+        for (int y = i0[1]; y <= i1[1]; ++y)
+            for (int x = i0[0]; x <= i1[0]; ++x) cnt += within(x, y, z) ? 1 : 0;
+    if (cnt == 0) return;
+    const unsigned long long base = atomicAdd(total, cnt);
     if (!pairs) return;
     unsigned long long w = base;
     for (int z = i0[2]; z <= i1[2]; ++z)
         for (int y = i0[1]; y <= i1[1]; ++y)
             for (int x = i0[0]; x <= i1[0]; ++x) {
+                if (!within(x, y, z) || w >= base + cnt) continue;
                 const uint32_t cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 +
                                       (uint32_t)x;
                 pairs[w++] = ((unsigned long long)cell << 32) | (uint32_t)f;
@@ -518,16 +582,18 @@ __global__ void k_grid_split(const unsigned long long* __restrict__ pairs, int64
 // Inserts the distinct cells into the hash table (bounded linear probing).
 __global__ void k_grid_insert(const uint32_t* __restrict__ uniq, const uint32_t* __restrict__ cnt,
                               const uint32_t* __restrict__ start, const int* __restrict__ nuniq,
-                              uint32_t* __restrict__ key, uint2* __restrict__ range,
-                              uint32_t shift, uint32_t mask, int* __restrict__ failed) {
+                              uint4* __restrict__ slots, uint32_t shift, uint32_t mask,
+                              int* __restrict__ failed) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nuniq) return;
     const uint32_t c = uniq[i];
     uint32_t slot = (c * 0x9E3779B1u) >> shift;
     for (uint32_t probe = 0; probe <= mask; ++probe) {
-        const uint32_t prev = atomicCAS(key + slot, 0xffffffffu, c);
+        const uint32_t prev = atomicCAS(&slots[slot].x, 0xffffffffu, c);
         if (prev == 0xffffffffu || prev == c) {
-            range[slot] = make_uint2(start[i], cnt[i]);
+            slots[slot].y = start[i];
+            slots[slot].z = cnt[i];
+            slots[slot].w = 0u;
             return;
         }
         slot = (slot + 1) & mask;
@@ -647,7 +713,7 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // at least 6 blocks of 128 threads per SM (85 registers): measured best of
     // 1, 6 and 8 on the 10M-point workload (8 spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gkey) {
+    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gslot) {
         // 768 resident threads per SM (85 registers) in every block shape
         switch (point_block) {
         case 256:
@@ -895,7 +961,7 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
         // warp (see k_env_points_warp); -1 when above 32 (per-sample walks)
         int32_t cand = -1;
         int cnt = -1, kh = 0;
-        if (FP32 && !F.T.gkey) {
+        if (FP32 && !F.T.gslot) {
             float qlo[3], qhi[3];
             const double t[9] = {h.vs[0].x, h.vs[0].y, h.vs[0].z, h.vs[1].x, h.vs[1].y,
                                  h.vs[1].z, h.vs[2].x, h.vs[2].y, h.vs[2].z};
@@ -909,7 +975,7 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
         }
         // out iff the lane's sample (have) is out; called by the whole warp
         auto lane_out = [&](bool have, const V3& p) -> bool {
-            if (FP32 && F.T.gkey) {
+            if (FP32 && F.T.gslot) {
                 CertQuery q;
                 if (have) q = cert_query(p, F.E, F.T.scale_hi);
                 return have && !grid_point_in(F.T, F.E, have, p, q, st);
@@ -1211,7 +1277,7 @@ __global__ void __launch_bounds__(128) k_env_points_segs(const double* __restric
             const EnvTree T = g.T;
             const EpsParams E = g.E;
             V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
-            if (FP32 && T.gkey) {
+            if (FP32 && T.gslot) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
                 out[i] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
             } else {
@@ -1382,7 +1448,7 @@ __device__ int32_t nearest_facet(const EnvTree& T, const V3& p, V3& q, double& s
 // EnvGrid), ties included; otherwise it returns false and the tree decides.
 __device__ __forceinline__ bool nearest_facet_grid(const EnvTree& T, double eps2, const V3& p,
                                                    V3& q, double& sqd, int32_t& fid) {
-    if (!T.gkey) return false;
+    if (!T.gslot) return false;
     CertQuery cq;
     cq.ph[0] = d2f_rn(p.x);
     cq.ph[1] = d2f_rn(p.y);
@@ -1427,8 +1493,7 @@ __global__ void k_nearest_points(EnvTree T, double eps2, const double* __restric
 }
 
 void free_env_grid(tw_ctx* c, EnvGrid& G) {
-    if (G.key) dev_free(c, G.key, G.key_bytes);
-    if (G.range) dev_free(c, G.range, G.range_bytes);
+    if (G.slot) dev_free(c, G.slot, G.slot_bytes);
     if (G.list) dev_free(c, G.list, G.list_bytes);
     G = EnvGrid{};
 }
@@ -1452,7 +1517,7 @@ struct BuildScratch {
 
 int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaStream_t s) {
     if (S.nf <= 0 || !(eps2 >= 0.0)) return TW_OK;
-    if (S.grid.key && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
+    if (S.grid.slot && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
     free_env_grid(c, S.grid);
     const int32_t nf = S.nf;
     // bounding box of the facets: the root's two child boxes, or the facet
@@ -1520,8 +1585,10 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     if (n[0] * n[1] * n[2] >= (int64_t(1) << 31)) return TW_OK;   // the tree walk serves
     const int Bk = 256;
     const int G = (int)((nf + Bk - 1) / Bk);
+    const double slack = std::ldexp(M, -30);
     k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                  (int32_t)n[1], (int32_t)n[2], Rm, d_total, nullptr, d_big);
+                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, d_total, nullptr,
+                                  d_big);
     unsigned long long hacc[2] = {0, 0};
     cudaMemcpyAsync(hacc, d_total, 16, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
@@ -1537,7 +1604,8 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     if (st != TW_OK) return st;
     cudaMemsetAsync(d_total, 0, 8, s);
     k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                  (int32_t)n[1], (int32_t)n[2], Rm, d_total, pairs, nullptr);
+                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, d_total, pairs,
+                                  nullptr);
     int key_bits = 32;
     while (key_bits < 64 && (1ULL << (key_bits - 32)) < (unsigned long long)(n[0] * n[1] * n[2]))
         ++key_bits;
@@ -1580,27 +1648,20 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     uint32_t bits = 1;
     while ((1ULL << bits) < 2ULL * (unsigned long long)nuniq) ++bits;
     const size_t H = size_t(1) << bits;
-    void *hk = nullptr, *hr = nullptr;
-    if ((st = dev_alloc(c, 4 * H, &hk)) != TW_OK) {
+    void* hs = nullptr;
+    if ((st = dev_alloc(c, 16 * H, &hs)) != TW_OK) {
         dev_free(c, listp, 4 * (size_t)nt + 16);
         return st;
     }
-    if ((st = dev_alloc(c, 8 * H, &hr)) != TW_OK) {
-        dev_free(c, listp, 4 * (size_t)nt + 16);
-        dev_free(c, hk, 4 * H);
-        return st;
-    }
-    cudaMemsetAsync(hk, 0xff, 4 * H, s);
+    cudaMemsetAsync(hs, 0xff, 16 * H, s);
     k_grid_insert<<<(unsigned)((nuniq + 255) / 256), 256, 0, s>>>(
-        uniq, cnt, start, d_nuniq, (uint32_t*)hk, (uint2*)hr, 32 - bits, (uint32_t)(H - 1),
-        d_failed);
+        uniq, cnt, start, d_nuniq, (uint4*)hs, 32 - bits, (uint32_t)(H - 1), d_failed);
     int failed = 0;
     cudaMemcpyAsync(&failed, d_failed, 4, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess || failed) {
         dev_free(c, listp, 4 * (size_t)nt + 16);
-        dev_free(c, hk, 4 * H);
-        dev_free(c, hr, 8 * H);
+        dev_free(c, hs, 16 * H);
         return e != cudaSuccess ? cuda_fail(c, e, "grid build") : TW_OK;
     }
     EnvGrid& g = S.grid;
@@ -1609,15 +1670,13 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
         g.n[k] = (int32_t)n[k];
     }
     g.inv_c = inv;
-    g.key = (uint32_t*)hk;
-    g.range = (uint2*)hr;
+    g.slot = (uint4*)hs;
     g.shift = 32 - bits;
     g.mask = (uint32_t)(H - 1);
     g.list = list;
     g.eps2 = eps2;
     g.cell_factor = cell_factor;
-    g.key_bytes = 4 * H;
-    g.range_bytes = 8 * H;
+    g.slot_bytes = 16 * H;
     g.list_bytes = 4 * (size_t)nt + 16;
     return TW_OK;
 }
@@ -1655,7 +1714,7 @@ __global__ void k_collapse_points(EnvTree Tin, EnvTree Tb, EpsParams E,
                 break;
             }
             int32_t f;
-            if (FP32 && T.gkey) {
+            if (FP32 && T.gslot) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
                 f = grid_point_in(T, E, true, p, q, st) ? 0 : -1;
             } else {

@@ -56,28 +56,30 @@ struct alignas(16) FacetCull {
 static_assert(sizeof(FacetCull) == 128, "FacetCull must be 128 bytes");
 
 // Uniform grid over the surface for the certified envelope test: cell size c
-// (the same on every axis), origin lo; cell (i, j, k) lists every leaf whose
-// box, grown by R = eps (1 + 2^-18) + 2^-17 M (M = the largest coordinate
-// magnitude of the grown box), meets the cell.  Any point within the
+// (the same on every axis), origin lo; cell (i, j, k) lists every leaf within
+// R = eps (1 + 2^-18) + 2^-17 M (M = the largest coordinate magnitude of the
+// grown box) of the cell: the cells of the leaf's box grown by R that a
+// separating-axis test cannot separate from the triangle (the cube of
+// half-size c/2 + R around the cell's centre).  Any point within the
 // certified culling radius of a leaf finds that leaf in the list of its own
 // cell (the margin covers the binary32 cell index), so one cell's list
 // replaces the tree walk.  Built for one eps2 (rebuilt when it changes).
 // Only the non-empty cells are stored, in an open-addressing hash table
-// (power-of-two size, at most half full): key = cell index (i + n0 (j + n1 k),
-// below 2^32 - 1), range = (first entry in list, count); a cell's list holds
+// (power-of-two size, at most half full) of 16-byte slots read in one load:
+// key = cell index (i + n0 (j + n1 k), below 2^32 - 1), then the first entry
+// in list and the count; a cell's list holds
 // its leaves in ascending order.
 struct EnvGrid {
     float lo[3] = {0, 0, 0};
     float inv_c = 0.0f;
     int32_t n[3] = {0, 0, 0};
-    uint32_t* key = nullptr;   // hash slots: cell index or 0xffffffff (empty)
-    uint2* range = nullptr;    // (first, count) of the slot's cell
+    uint4* slot = nullptr;     // hash slots: (cell index or 0xffffffff (empty), first, count, -)
     uint32_t shift = 32;       // slot = (cell * 0x9E3779B1) >> shift
     uint32_t mask = 0;
     int32_t* list = nullptr;   // leaf indices
     double eps2 = -1.0;        // the eps2 it was built for (-1: none)
     double cell_factor = 0.0;  // and the cell-size factor
-    size_t key_bytes = 0, range_bytes = 0, list_bytes = 0;
+    size_t slot_bytes = 0, list_bytes = 0;
 };
 
 struct Surface {
