@@ -65,6 +65,43 @@ def test_certified_points_at_threshold(ctx, oracle, offset):
     assert 0 < want.sum() < len(P)
 
 
+def _soup(n, size, seed):
+    """n random triangles of edge ~size in every orientation inside the unit box."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3))
+    V = (c + (rng.random((n, 3, 3)) - 0.5) * size).reshape(-1, 3)
+    return V, np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+
+
+@pytest.mark.parametrize("cell", [0.05, 0.1, 0.2, 1.0])
+def test_certified_grid_keeps_every_facet_within_reach(ctx, oracle, cell):
+    """Points just inside eps of a random point of a random facet (interior, edges and
+    corners), in random directions: a facet dropped from a cell's list by the grid's
+    separating-axis culling would turn such a point out."""
+    V, F = _soup(3000, 0.05, seed=21)
+    eps = 2e-3
+    rng = np.random.default_rng(22)
+    n = 60000
+    f = rng.integers(0, len(F), n)
+    w = rng.random((n, 3)) ** 3          # many points near edges and corners
+    w /= w.sum(1, keepdims=True)
+    X = np.einsum("ij,ijk->ik", w, V[F[f]])
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = eps * np.where(rng.random(n) < 0.5, 1 - 1e-7, 1 + 1e-7)
+    P = X + d * r[:, None]
+    ctx.set_params(eps * eps, eps)
+    ctx.set_tuning(tw.Context.TUNE_GRID_CELL, cell)
+    try:
+        ctx.surface_upload(V, F)
+        a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P))
+    finally:
+        ctx.set_tuning(tw.Context.TUNE_GRID_CELL, 0.1)
+    want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
+    assert np.array_equal(a, want) and np.array_equal(b, want)
+    assert want.sum() < len(P) // 2        # the inner half is in by construction
+
+
 def test_certified_points_sliver_facets(ctx, oracle):
     rng = np.random.default_rng(13)
     # fan of slivers: long thin triangles with tiny angles, plus a degenerate one

@@ -462,68 +462,25 @@ __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
 }
 
-// Separating-axis test of triangle t against the axis-aligned cube of
-// half-size h centred at c (the three box axes, the triangle's normal and the
-// nine edge x box-axis products): false only when an axis separates them.
-// The cube grown by R contains the ball of radius R around every point of
-// the cell, so a facet it excludes is farther than R from the whole cell.
-__device__ bool tri_cube_overlap(const double* t, const double* c, double h) {
-    double v[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) v[i][k] = t[3 * i + k] - c[k];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (fmin(v[0][k], fmin(v[1][k], v[2][k])) > h) return false;
-        if (fmax(v[0][k], fmax(v[1][k], v[2][k])) < -h) return false;
-    }
-    double e[3][3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        e[0][k] = v[1][k] - v[0][k];
-        e[1][k] = v[2][k] - v[1][k];
-        e[2][k] = v[0][k] - v[2][k];
-    }
-    {
-        const double nx = e[0][1] * e[1][2] - e[0][2] * e[1][1];
-        const double ny = e[0][2] * e[1][0] - e[0][0] * e[1][2];
-        const double nz = e[0][0] * e[1][1] - e[0][1] * e[1][0];
-        const double d = nx * v[0][0] + ny * v[0][1] + nz * v[0][2];
-        if (fabs(d) > h * (fabs(nx) + fabs(ny) + fabs(nz))) return false;
-    }
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            // axis = unit_k x e_j
-            double ax[3];
-            const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-            ax[k] = 0.0;
-            ax[k1] = -e[j][k2];
-            ax[k2] = e[j][k1];
-            const double p0 = ax[k1] * v[0][k1] + ax[k2] * v[0][k2];
-            const double p1 = ax[k1] * v[1][k1] + ax[k2] * v[1][k2];
-            const double p2 = ax[k1] * v[2][k1] + ax[k2] * v[2][k2];
-            const double r = h * (fabs(ax[k1]) + fabs(ax[k2]));
-            if (fmin(p0, fmin(p1, p2)) > r || fmax(p0, fmax(p1, p2)) < -r) return false;
-        }
-    }
-    return true;
-}
-
 // The cells within reach of every leaf: the cells of its box grown by Rm
-// that the separating-axis test cannot separate from the triangle (cube
-// half-size cell/2 + Rm + 2^-30 M, the last term covering the rounding of
-// the test), counted (pairs == nullptr) or written as (cell << 32 | leaf)
-// pairs at an atomically reserved position.  A leaf whose box spans more
-// than 2^16 cells marks the grid unsuitable (*too_big).
+// that a separating-axis test (the three box axes, the triangle's normal and
+// the nine edge x box-axis products) cannot separate from the triangle.  The
+// test uses the cube of half-size cell/2 + Rm + slack around the cell's
+// centre, which holds the ball of radius Rm around every point of the cell
+// (slack = 2^-30 M covers the cell's placement), so a leaf it excludes is
+// farther than Rm from the whole cell.  Counting (fcnt != nullptr): the
+// leaf's count and the total; filling: the (cell << 32 | leaf) pairs from
+// foff[leaf] on.  A leaf whose box spans more than 2^16 cells marks the grid
+// unsuitable (*too_big).  One warp per leaf; the lanes take the box's cells
+// in turn.
 __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
                              double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
                              double Rm, double slack, unsigned long long* __restrict__ total,
+                             uint32_t* __restrict__ fcnt, const uint32_t* __restrict__ foff,
                              unsigned long long* __restrict__ pairs, int* __restrict__ too_big) {
-    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= nf) return;
+    const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (f >= nf) return;   // whole warps
     double t[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9 * f + k);
@@ -539,34 +496,125 @@ __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double 
         i0[k] = (int)u;
         i1[k] = (int)v;
     }
-    const int64_t box = (int64_t)(i1[0] - i0[0] + 1) * (i1[1] - i0[1] + 1) * (i1[2] - i0[2] + 1);
+    const int bx = i1[0] - i0[0] + 1, by = i1[1] - i0[1] + 1;
+    const int64_t box = (int64_t)bx * by * (i1[2] - i0[2] + 1);
     if (box > 65536) {
-        if (too_big) atomicExch(too_big, 1);
+        if (lane == 0) {
+            if (too_big) atomicExch(too_big, 1);
+            if (fcnt) fcnt[f] = 0;
+        }
         return;
     }
     const double cs = 1.0 / inv_c;
     const double h = 0.5 * cs + Rm + slack;
-    auto within = [&](int x, int y, int z) {
-        const double c[3] = {lo0 + ((double)x + 0.5) * cs, lo1 + ((double)y + 0.5) * cs,
-                             lo2 + ((double)z + 0.5) * cs};
-        return tri_cube_overlap(t, c, h);
+    // Binary32 separating-axis test, rigorous: any direction is a valid
+    // separating axis, so the binary32 axes themselves are used as exact
+    // vectors and only the projections carry rounding.  The vertices
+    // relative to t0 (rounded once) and the cell centre relative to t0 (from
+    // base = lo - t0 and (x + 1/2) cs) are within 2^-20 L of the exact values
+    // (L = 2 (M + the grid's extent) bounds every coordinate and offset), so
+    // each projection onto axis a is within |a|_1 2^-19 L; an axis separates
+    // only by more than |a|_1 2^-18 L.  Cells no axis separates by that
+    // margin are kept (a longer list, never a missing leaf).
+    double L = 0.0;
+    for (int k = 0; k < 3; ++k)
+        L = fmax(L, fmax(fabs(lo[k]), fabs(lo[k] + (double)n[k] * cs)) + fabs(t[k]));
+    L = 2.0 * L;
+    const float mL = (float)ldexp(L, -18) * 1.0001f;
+    const float hf = (float)h * 1.000001f;
+    const float csf = (float)cs;
+    const float basef[3] = {(float)(lo0 - t[0]), (float)(lo1 - t[1]), (float)(lo2 - t[2])};
+    float vf[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        vf[0][k] = 0.0f;
+        vf[1][k] = (float)(t[3 + k] - t[k]);
+        vf[2][k] = (float)(t[6 + k] - t[k]);
+    }
+    float ef[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        ef[0][k] = vf[1][k] - vf[0][k];
+        ef[1][k] = vf[2][k] - vf[1][k];
+        ef[2][k] = vf[0][k] - vf[2][k];
+    }
+    const float nmf[3] = {ef[0][1] * ef[1][2] - ef[0][2] * ef[1][1],
+                          ef[0][2] * ef[1][0] - ef[0][0] * ef[1][2],
+                          ef[0][0] * ef[1][1] - ef[0][1] * ef[1][0]};
+    // 2^-40 <= L < 2^40 and |a|_1 >= 2^-40 keep every product far from
+    // binary32 overflow, and underflow far below the margin (else the cell
+    // is kept)
+    const bool sat_ok = L >= 0x1p-40 && L < 0x1p40;
+    // true when axis a separates the triangle (projections p) from the cube
+    auto apart = [&](const float* p, float a1) {
+        if (!(a1 >= 0x1p-40f)) return false;
+        const float r = hf * a1 + a1 * mL;
+        return fminf(p[0], fminf(p[1], p[2])) > r || fmaxf(p[0], fmaxf(p[1], p[2])) < -r;
     };
-    unsigned long long cnt = 0;
-    for (int z = i0[2]; z <= i1[2]; ++z)
-        for (int y = i0[1]; y <= i1[1]; ++y)
-            for (int x = i0[0]; x <= i1[0]; ++x) cnt += within(x, y, z) ? 1 : 0;
-    if (cnt == 0) return;
-    const unsigned long long base = atomicAdd(total, cnt);
-    if (!pairs) return;
-    unsigned long long w = base;
-    for (int z = i0[2]; z <= i1[2]; ++z)
-        for (int y = i0[1]; y <= i1[1]; ++y)
-            for (int x = i0[0]; x <= i1[0]; ++x) {
-                if (!within(x, y, z) || w >= base + cnt) continue;
-                const uint32_t cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 +
-                                      (uint32_t)x;
-                pairs[w++] = ((unsigned long long)cell << 32) | (uint32_t)f;
+    // cell q of the box (x fastest): within reach of the leaf?
+    auto within = [&](int q, uint32_t& cell) {
+        const int x = i0[0] + q % bx, y = i0[1] + (q / bx) % by, z = i0[2] + q / (bx * by);
+        cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 + (uint32_t)x;
+        if (!sat_ok) return true;
+        const float w[3] = {basef[0] + ((float)x + 0.5f) * csf, basef[1] + ((float)y + 0.5f) * csf,
+                            basef[2] + ((float)z + 0.5f) * csf};
+        float u[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) u[i][k] = vf[i][k] - w[k];
+        float p[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {   // the box axes
+            p[0] = u[0][k];
+            p[1] = u[1][k];
+            p[2] = u[2][k];
+            if (apart(p, 1.0f)) return false;
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)   // the normal
+            p[i] = nmf[0] * u[i][0] + nmf[1] * u[i][1] + nmf[2] * u[i][2];
+        if (apart(p, fabsf(nmf[0]) + fabsf(nmf[1]) + fabsf(nmf[2]))) return false;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {   // unit_k x e_j
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+                const float a1 = -ef[j][k2], a2 = ef[j][k1];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) p[i] = a1 * u[i][k1] + a2 * u[i][k2];
+                if (apart(p, fabsf(a1) + fabsf(a2))) return false;
             }
+        }
+        return true;
+    };
+    const int nbox = (int)box;
+    if (fcnt) {
+        uint32_t cnt = 0;
+        for (int q = lane; q < nbox; q += 32) {
+            uint32_t cell;
+            cnt += within(q, cell) ? 1u : 0u;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (lane == 0) {
+            fcnt[f] = cnt;
+            if (cnt) atomicAdd(total, (unsigned long long)cnt);
+        }
+        return;
+    }
+    // foff: exclusive sums of the counts (nf + 1 entries)
+    uint32_t w = __ldg(foff + f);
+    const uint32_t end = __ldg(foff + f + 1);
+    for (int q0 = 0; q0 < nbox; q0 += 32) {
+        const int q = q0 + lane;
+        uint32_t cell = 0;
+        const bool in = q < nbox && within(q, cell);
+        const unsigned bal = __ballot_sync(0xffffffffu, in);
+        const uint32_t at = w + __popc(bal & ((1u << lane) - 1u));
+        if (in && at < end) pairs[at] = ((unsigned long long)cell << 32) | (uint32_t)f;
+        w += __popc(bal);
+    }
 }
 
 // Sorted pairs -> the cell of each entry and the leaf list.
@@ -1584,11 +1632,17 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     }
     if (n[0] * n[1] * n[2] >= (int64_t(1) << 31)) return TW_OK;   // the tree walk serves
     const int Bk = 256;
-    const int G = (int)((nf + Bk - 1) / Bk);
+    const int G = (int)(((int64_t)nf * 32 + Bk - 1) / Bk);   // one warp per leaf
     const double slack = std::ldexp(M, -30);
+    // per-leaf counts (nf + 1 entries, the last 0) and their exclusive sums
+    uint32_t* fcnt = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
+    if (st != TW_OK) return st;
+    uint32_t* foff = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
+    if (st != TW_OK) return st;
+    cudaMemsetAsync(fcnt + nf, 0, 4, s);
     k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, d_total, nullptr,
-                                  d_big);
+                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, d_total, fcnt,
+                                  nullptr, nullptr, d_big);
     unsigned long long hacc[2] = {0, 0};
     cudaMemcpyAsync(hacc, d_total, 16, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
@@ -1602,10 +1656,16 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     if (st != TW_OK) return st;
     unsigned long long* pairs2 = (unsigned long long*)B.get(8 * (size_t)nt, st);
     if (st != TW_OK) return st;
-    cudaMemsetAsync(d_total, 0, 8, s);
+    {
+        size_t tbs = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tbs, fcnt, foff, nf + 1, s);
+        void* tmp = B.get(tbs + 16, st);
+        if (st != TW_OK) return st;
+        cub::DeviceScan::ExclusiveSum(tmp, tbs, fcnt, foff, nf + 1, s);
+    }
     k_grid_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
-                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, d_total, pairs,
-                                  nullptr);
+                                  (int32_t)n[1], (int32_t)n[2], Rm, slack, nullptr, nullptr,
+                                  foff, pairs, nullptr);
     int key_bits = 32;
     while (key_bits < 64 && (1ULL << (key_bits - 32)) < (unsigned long long)(n[0] * n[1] * n[2]))
         ++key_bits;
