@@ -208,6 +208,7 @@ class Context:
         if st != TW_OK:
             raise TetWildGpuError(st, "tw_ctx_create failed (no usable CUDA device?)")
         self.h = h
+        self.device = device
         self.eps_2 = 0.0
         self.sampling_dist = 0.0
 
