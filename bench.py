@@ -38,6 +38,7 @@ sys.path.insert(0, str(ROOT))
 N_TETS = 4_000_000
 N_POINTS = 10_000_000
 EPS = 1e-3
+GRID_CELL = 0.1   # envelope grid cell / mean facet extent (TW_TUNE_GRID_CELL)
 METRIC = "AMIPS+envelope queries/s vs plain FP64 GPU at 0 decision mismatches; p99 ms"
 UNIT = "queries/s"
 BYTES_PER_TET = 96 + 8 + 24 + 72 + 1     # coords in; E, J, H, flip out
@@ -247,6 +248,9 @@ def run_ours(args):
     T, V, F, P = make_inputs(seed=rank)
     ctx = tw.Context(dev)
     ctx.set_params(EPS * EPS, EPS)
+    # a finer envelope grid than the default 0.2: 4% faster point tests on this
+    # surface for 4x the grid memory (256 MB); results never depend on it
+    ctx.set_tuning(tw.Context.TUNE_GRID_CELL, GRID_CELL)
     ctx.surface_upload(V, F)
     fp64_tflops, fp32_tflops = ctx.probe_peaks()
 
@@ -343,7 +347,7 @@ def run_ours(args):
                                "eps=1e-3; certified FP32 mode (decisions identical to FP64)",
                    "tets": N_TETS, "points": N_POINTS, "surface_tris": int(len(F)),
                    "l2": "inputs larger than L2 (384 MB tets, 240 MB points); no flush",
-                   "parallelism": f"replicas x{ws}"},
+                   "grid_cell": GRID_CELL, "parallelism": f"replicas x{ws}"},
         "p50_ms": float(np.percentile(cert["step_ms"], 50)),
         "p99_ms": float(np.percentile(cert["step_ms"], 99)),
         "kernels_ms": {"amips_step": ma, "envelope_step": me,

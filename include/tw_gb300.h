@@ -270,7 +270,7 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 
 /* ---- tuning knobs (work only, never results) ---------------------------------------
  * TW_TUNE_GRID_CELL: cell size of the certified envelope grid as a multiple
- *   of the mean facet extent (default 0.1; the grid is rebuilt).
+ *   of the mean facet extent (default 0.2; the grid is rebuilt).
  * TW_TUNE_SORT_POINTS: 1 (default) orders point queries by Morton cell of
  *   the surface box before the test (a counting sort; 2^(3b) cells with the
  *   smallest b in 3..8 that gives at least one cell per point), 2..8 fixes b,

@@ -96,7 +96,7 @@ def test_certified_grid_keeps_every_facet_within_reach(ctx, oracle, cell):
         ctx.surface_upload(V, F)
         a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P))
     finally:
-        ctx.set_tuning(tw.Context.TUNE_GRID_CELL, 0.1)
+        ctx.set_tuning(tw.Context.TUNE_GRID_CELL, 0.2)
     want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
     assert np.array_equal(a, want) and np.array_equal(b, want)
     assert want.sum() < len(P) // 2        # the inner half is in by construction

@@ -132,7 +132,7 @@ struct tw_ctx {
     size_t mesh_bytes = 0;
     int precision = TW_PRECISION_FP64;
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
-    double grid_cell = 0.1;   // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
+    double grid_cell = 0.2;   // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
     // launch timing of the point-envelope test kernel (TW_TUNE_TIME_KERNELS):
     // a ring of event pairs recorded around each launch
     static constexpr int kTimeRing = 64;

@@ -565,6 +565,11 @@ int tw_server_job_open(tw_server* s, const double* V, int32_t nv, const int32_t*
         return srv_fail(s, st, "job_open: " + m);
     }
     std::lock_guard<std::mutex> lk(s->mu);
+    // the estimate admitted it; the bytes the job actually holds decide
+    if (s->budget && jobs_bytes(s) + lanes_bytes(s) + c->used > s->budget) {
+        tw_ctx_destroy(c);
+        return srv_fail(s, TW_BUSY, "job does not fit in the HBM budget now");
+    }
     int32_t id = -1;
     for (size_t i = 0; i < s->jobs.size(); ++i)
         if (!s->jobs[i]->c) {
