@@ -1,0 +1,77 @@
+"""Empty batches through every batched entry point, in both precision modes:
+empty results, no error, and the context still answers the next call (the
+reference's loops simply run zero times)."""
+import numpy as np
+import pytest
+
+import tetwild_gb300 as tw
+from tetwild_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+MODES = [tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED]
+
+
+@pytest.fixture(scope="module")
+def setup():
+    V, F = syn.icosphere(3)
+    eps = 2e-3
+    xyz, off, tets, ff, cen, kinds = syn.mixed_star_batch(V, F, 40, eps, seed=8)
+    return V, F, eps, xyz, off, tets, ff, cen, kinds
+
+
+@pytest.mark.parametrize("precision", MODES)
+def test_empty_batches(ctx, oracle, setup, precision):
+    V, F, eps, xyz, off, tets, ff, cen, kinds = setup
+    ctx.set_params(eps * eps, eps / 2, 1, 8)
+    ctx.surface_upload(V, F)
+    ctx.mesh_upload(xyz)
+    ctx.set_precision(precision)
+    try:
+        assert ctx.envelope_points(np.zeros((0, 3))).shape == (0,)
+        assert ctx.envelope_faces(np.zeros((0, 9))).shape == (0,)
+        Q, D, Fi = ctx.nearest_points(np.zeros((0, 3)))
+        assert Q.shape == (0, 3) and D.shape == (0,) and Fi.shape == (0,)
+        g = ctx.amips(np.zeros((12, 0)))
+        assert g["E"].shape == (0,) and g["flip"].shape == (0,)
+        E, Fl, N, st = ctx.tet_quality(np.zeros((0, 4), np.int32))
+        assert E.shape == (0,) and st == tw.TW_OK
+        pos, moved = ctx.newton_stars(np.zeros(1, np.int32), np.zeros((0, 4), np.int32),
+                                      np.zeros(0, np.int32))
+        assert pos.shape == (0, 3) and moved.shape == (0,)
+        pos, status = ctx.smooth_stars(np.zeros(1, np.int32), np.zeros((0, 4), np.int32),
+                                       np.zeros(0, np.int32), np.zeros(0, np.uint8),
+                                       np.zeros(0, np.uint8))
+        assert pos.shape == (0, 3) and status.shape == (0,)
+        codes = ctx.collapse_check(np.zeros((0, 2), np.int32), np.zeros(0, np.uint8),
+                                   np.zeros(1, np.int32), np.zeros((0, 4), np.int32),
+                                   np.zeros(0, np.uint8))
+        assert codes.shape == (0,)
+        a, m, m2, buckets = ctx.energy_stats(np.zeros((0, 4), np.int32))
+        wa, wm, wm2, wb = oracle.energy_stats(xyz, np.zeros((0, 4), np.int32))
+        assert (np.isnan(a) and np.isnan(wa)) or a == wa      # 0 / 0, as the reference
+        assert m == wm and m2 == wm2 and np.array_equal(buckets, wb)
+        # the context still answers: one star batch against the oracle
+        got, st2 = ctx.smooth_stars(off, tets, cen, ff, kinds)
+        S = oracle.surface(V, F)
+        want, wst = oracle.smooth_stars(xyz, off, tets, cen, ff, kinds, surface=S, boundary=S,
+                                        eps2=eps * eps, sd=eps / 2, max_step=1, max_it=8)
+        assert np.array_equal(st2.astype(np.int8), wst) and np.array_equal(got, want)
+    finally:
+        ctx.set_precision(tw.TW_PRECISION_FP64)
+
+
+def test_server_empty_requests(setup):
+    V, F, eps, xyz, off, tets, ff, cen, kinds = setup
+    with tw.Server(0, 0, lanes=2) as srv:
+        j = srv.job_open(V, F, eps * eps, eps / 2)
+        srv.job_mesh(j, xyz)
+        t1, out = srv.submit_points(j, np.zeros((0, 3)))
+        t2, outf = srv.submit_faces(j, np.zeros((0, 9)))
+        t3, res = srv.submit_amips(j, np.zeros((12, 0)))
+        for t in (t1, t2, t3):
+            srv.wait(t)
+        assert out.shape == (0,) and outf.shape == (0,) and res[0].shape == (0,)
+        t4, P_out = srv.submit_points(j, syn.envelope_points(V, F, 1000, eps, seed=2))
+        srv.wait(t4)
+        assert P_out.shape == (1000,)
