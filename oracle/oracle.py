@@ -284,6 +284,7 @@ class RefLib:
             "twref_points_out": ([_P, _P, _I64, _D, _P, _I], None),
             "twref_faces_out": ([_P, _P, _I64, _D, _D, _P, _I], None),
             "twref_nearest": ([_P, _P, _I64, _P, _P, _I], None),
+            "twref_energy_sweeps": ([_P, _P, _P, _I64, _D, _P, _P], None),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -304,6 +305,18 @@ class RefLib:
         H = np.empty((9, n)) if hessian else None
         self.L.twref_amips_batch_soa(_p(T), n, _p(E), _p(J), _p(H), nthreads)
         return E, J, H
+
+    def energy_sweeps(self, E, removed=None, locked=None, thres=10.0):
+        """The reference's getAvgMaxEnergy / getMaxEnergy / getSecondMaxEnergy /
+        getFilterEnergy over per-tet energies: (avg, max, max, second max, filter, clean_up)."""
+        E = _c(E, np.float64)
+        R = None if removed is None else _c(removed, np.uint8)
+        L = None if locked is None else _c(locked, np.uint8)
+        out = np.empty(5)
+        c = ctypes.c_int()
+        self.L.twref_energy_sweeps(_p(E), _p(R), _p(L), E.shape[0], thres, _p(out),
+                                   ctypes.byref(c))
+        return (*out.tolist(), bool(c.value))
 
     def sample_triangle(self, tri9, sd):
         t = _c(tri9, np.float64).reshape(9)

@@ -36,6 +36,8 @@ SLICES = [
      "bool LocalOperations::isPointOutEnvelop"),
     ("src/tetwild/Common.cpp", 143, 255, "sample_slice.inc",
      "void sampleTriangle("),
+    ("src/tetwild/LocalOperations.cpp", 605, 693, "sweeps_slice.inc",
+     "void LocalOperations::getAvgMaxEnergy"),
 ]
 COPIES = [
     ("src/tetwild/geogram/mesh_AABB.cpp", "mesh_AABB.cpp"),
@@ -69,7 +71,7 @@ def do_slice() -> bool:
 
 
 def do_compile() -> Path | None:
-    if not (SRC / "amips_slice.inc").is_file():
+    if not all((SRC / name).is_file() for _, _, _, name, _ in SLICES):
         return None
     OUT.mkdir(parents=True, exist_ok=True)
     obj = OUT / "tw_oracle_ref.o"

@@ -6,6 +6,8 @@
 //   LocalOperations.cpp:28-291     comformalAMIPS{Energy,Jacobian,Hessian}_new
 //   LocalOperations.cpp:1034-1109  isPointOutEnvelop, isFaceOutEnvelop_sampling
 //   Common.cpp:143-255             sampleTriangle
+//   LocalOperations.cpp:605-693    getAvgMaxEnergy, getMaxEnergy, getSecondMaxEnergy,
+//                                  getFilterEnergy
 //   geogram/mesh_AABB.{h,cpp}      MeshFacetsAABBWithEps (whole files)
 //   DistanceQuery.h                get_point_facet_nearest_point
 // The library is the pin for the oracle restatement and the timed CPU
@@ -14,6 +16,8 @@
 // collinearity test, and geogram's point-triangle distance by the oracle's
 // (see shim/geo_shim.h).
 #include <array>
+#include <cmath>
+#include <numeric>
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -75,6 +79,33 @@ struct LocalOperations {
 #include "envelope_slice.inc"
 
 }  // namespace tetwild
+
+// The full-mesh energy sweeps run over a per-tet quality array; their own
+// LocalOperations holds just the members they read.
+namespace tetwild_sweeps {
+struct TetQualityRef {
+    double slim_energy = 0.0;
+};
+struct SweepArgs {
+    double filter_energy_thres = 10.0;
+};
+struct SweepState {
+    double MAX_ENERGY = 1e50;   // State.h:29
+};
+struct LocalOperations {
+    std::vector<TetQualityRef> tet_qualities;
+    std::vector<bool> t_is_removed;
+    const uint8_t* locked = nullptr;
+    SweepArgs args;
+    SweepState state;
+    bool isTetLocked_ui(int i) const { return locked && locked[i]; }
+    void getAvgMaxEnergy(double& avg_tq, double& max_tq);
+    double getMaxEnergy();
+    double getSecondMaxEnergy(double max_energy);
+    double getFilterEnergy(bool& is_clean_up);
+};
+#include "sweeps_slice.inc"
+}  // namespace tetwild_sweeps
 
 // geogram's MESH_ORDER_MORTON spatial sort: recursive median split of the
 // facet centroids along x, y, z in turn (affects the tree's shape only).
@@ -225,6 +256,35 @@ void twref_nearest(void* h, const double* P, int64_t n, double* Q, double* D, in
             D[i] = d;
         }
     });
+}
+
+// The reference's sweeps over per-tet energies E (removed / locked masks may
+// be NULL): out = {avg, max (getAvgMaxEnergy), getMaxEnergy, getSecondMaxEnergy
+// of that max, getFilterEnergy}; *is_clean_up as getFilterEnergy leaves it (0
+// when it does not set it).
+void twref_energy_sweeps(const double* E, const uint8_t* removed, const uint8_t* locked,
+                         int64_t n, double thres, double* out, int* is_clean_up) {
+    tetwild_sweeps::LocalOperations ops;
+    ops.tet_qualities.resize(size_t(n));
+    ops.t_is_removed.assign(size_t(n), false);
+    for (int64_t i = 0; i < n; ++i) {
+        ops.tet_qualities[size_t(i)].slim_energy = E[i];
+        if (removed) ops.t_is_removed[size_t(i)] = removed[i] != 0;
+    }
+    ops.locked = locked;
+    ops.args.filter_energy_thres = thres;
+    double avg = 0.0, mx = 0.0;
+    ops.getAvgMaxEnergy(avg, mx);
+    const double m = ops.getMaxEnergy();
+    const double m2 = ops.getSecondMaxEnergy(m);
+    bool clean = false;
+    const double f = ops.getFilterEnergy(clean);
+    out[0] = avg;
+    out[1] = mx;
+    out[2] = m;
+    out[3] = m2;
+    out[4] = f;
+    *is_clean_up = clean ? 1 : 0;
 }
 
 }  // extern "C"

@@ -399,3 +399,30 @@ def test_smooth_surface_outcomes_are_consistent(oracle):
             tri = X[[t[0], t[1], t[2]]]  # face opposite vertex 3 (the flagged one)
             tris.append(tri.reshape(9))
         assert not S.faces_out(np.asarray(tris), eps * eps, eps / 2).any()
+
+
+@pytest.mark.parametrize("sigma", [0.1, 0.6, 2.0])
+def test_energy_sweeps_match_reference_live(oracle, reflib, sigma):
+    """getAvgMaxEnergy / getMaxEnergy / getSecondMaxEnergy / getFilterEnergy
+    (LocalOperations.cpp:605-693, compiled from the reference) against the oracle's
+    one-pass sweep, on tets whose energies spread over the filter's buckets, with
+    inverted tets (the 1e50 sentinel) and locked tets."""
+    rng = np.random.default_rng(40 + int(10 * sigma))
+    n = 20000
+    T = syn.energy_batch(n, seed=41, sigma_rel=sigma)
+    flip = rng.random(n) < 0.02
+    T[0:3, flip], T[3:6, flip] = T[3:6, flip].copy(), T[0:3, flip].copy()
+    E = oracle.amips_batch_soa(T, quality=True, jacobian=False, hessian=False)[0]
+    assert (E == 1e50).any()
+    xyz = T.reshape(4, 3, n).transpose(2, 0, 1).reshape(-1, 3)
+    tets = np.arange(4 * n, dtype=np.int32).reshape(n, 4)
+    locked = (rng.random(n) < 0.1).astype(np.uint8)
+    seen = set()
+    for thres in (1.0, 3.0, 10.0):   # every branch of getFilterEnergy over the three batches
+        a, m, m2, buckets = oracle.energy_stats(xyz, tets, locked, thres)
+        f, clean = oracle.filter_energy(buckets, thres)
+        ra, rm, rm_, rm2, rf, rclean = reflib.energy_sweeps(E, None, locked, thres)
+        assert a == ra and m == rm == rm_ and m2 == rm2
+        assert f == rf and clean == rclean
+        seen.add((f, clean))
+    assert len(seen) >= 2
