@@ -539,8 +539,8 @@ def run_serving(args, dev):
     """Serving workload: 64 meshing jobs (icospheres, tori R=1 r=0.3, displaced spheres) of
     1k-200k triangles (log-uniform) resident in HBM under a 150 GB budget; requests of 1k-500k
     queries (log-uniform per kind: envelope points, AMIPS E/J/H, envelope faces, smoothing
-    stars) for uniformly chosen jobs.  A burst of 256 requests measures capacity in each
-    precision mode; then requests arrive as a Poisson process at 70% of the certified capacity
+    stars) for uniformly chosen jobs.  A burst of 256 requests (the median of three) measures
+    capacity in each precision mode; then requests arrive as a Poisson process at 70% of the certified capacity
     for SERVE_SECONDS, and the server-side latency of each (submit to results in host memory)
     gives p50 / p99."""
     import threading
@@ -670,9 +670,12 @@ def run_serving(args, dev):
                        ("fp32_certified", tw.TW_PRECISION_FP32_CERTIFIED)):
         srv.set_params(prec, 1, 8)
         run(burst[:32])                     # warm-up: lane scratch grows to size
-        lat, wall = run(burst)
+        # the median of three bursts (one burst lasts tens of ms: host jitter shows)
+        runs = sorted((run(burst) for _ in range(3)), key=lambda r: r[1])
+        lat, wall = runs[1]
         cap[name] = {"queries_per_s": q_burst / wall, "requests_per_s": len(burst) / wall,
-                     "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                     "wall_s": wall, "walls_s": [r[1] for r in runs],
+                     "p50_ms": float(np.percentile(lat, 50)),
                      "p99_ms": float(np.percentile(lat, 99))}
     rate = 0.7 * cap["fp32_certified"]["requests_per_s"]
     m = max(64, int(rate * SERVE_SECONDS))

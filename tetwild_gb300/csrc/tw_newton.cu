@@ -143,8 +143,7 @@ __device__ bool star_update(const StarView& S, const double* pos, double& energy
         int4 tv = __ldg(S.tets + i);
         int start = (tv.x == S.v) ? 0 : (tv.y == S.v) ? 1 : (tv.z == S.v) ? 2 : (tv.w == S.v) ? 3 : 0;
         gather_tet(S, tv, start, pos, T);
-        e += amips_energy(T);
-        amips_egh(T, J1, H1);
+        e += amips_egh(T, J1, H1);   // its E is amips_energy's, operation for operation
         for (int j = 0; j < 3; ++j) {
             J[j] += J1[j];
             H[3 * j + 0] += H1[3 * j + 0];
@@ -268,8 +267,7 @@ __device__ __forceinline__ int newton_group_star(const StarView& S, double* pos,
                           : (tv.w == S.v) ? 3 : 0;
                 double T[12];
                 gather_tet(S, tv, start, pos, T);
-                te = amips_energy(T);
-                amips_egh(T, tJ, tH);
+                te = amips_egh(T, tJ, tH);   // its E is amips_energy's, operation for operation
             }
             for (int t = 0; t < cnt; ++t) {
                 e += __shfl_sync(gm, te, t, G);
