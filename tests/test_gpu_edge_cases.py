@@ -75,3 +75,47 @@ def test_server_empty_requests(setup):
         t4, P_out = srv.submit_points(j, syn.envelope_points(V, F, 1000, eps, seed=2))
         srv.wait(t4)
         assert P_out.shape == (1000,)
+
+
+def test_errors_leave_the_context_usable(ctx, oracle, setup):
+    """Rejected calls report their error and the next call answers correctly: ids out of
+    range in every index-based entry point, a face beyond the per-row sample bound (the
+    kernel flags it before sampling), a query without a surface."""
+    V, F, eps, xyz, off, tets, ff, cen, kinds = setup
+    nv = len(xyz)
+    with tw.Context(0) as c:
+        with pytest.raises(tw.TetWildGpuError) as e:
+            c.envelope_points(np.zeros((4, 3)))
+        assert e.value.code == tw.TW_ERR_NO_SURFACE
+        c.set_params(eps * eps, eps / 2, 1, 8)
+        c.surface_upload(V, F)
+        c.mesh_upload(xyz)
+        bad = tets.copy()
+        bad[-1, 2] = nv + 7
+        calls = [
+            lambda: c.tet_quality(bad),
+            lambda: c.newton_stars(off, bad, cen),
+            lambda: c.smooth_stars(off, bad, cen, ff, kinds),
+            lambda: c.energy_stats(bad),
+            lambda: c.collapse_check(np.array([[0, nv + 3]], np.int32), np.zeros(1, np.uint8),
+                                     np.array([0, 1], np.int32), tets[:1], ff[:1]),
+        ]
+        for call in calls:
+            with pytest.raises(tw.TetWildGpuError) as e:
+                call()
+            assert e.value.code == tw.TW_ERR_ARG
+        # one face with edges of 1e4 at sampling distance eps/2: far beyond 4e6 samples a row
+        huge = np.array([[0.0, 0, 0, 1e4, 0, 0, 0, 1e4, 0]])
+        fine = np.hstack([V[F[:50, 0]], V[F[:50, 1]], V[F[:50, 2]]])
+        for prec in MODES:
+            c.set_precision(prec)
+            with pytest.raises(tw.TetWildGpuError) as e:
+                c.envelope_faces(np.vstack([fine, huge]))
+            assert e.value.code == tw.TW_ERR_ARG and "sample bound" in str(e.value)
+            assert np.array_equal(c.envelope_faces(fine),
+                                  oracle.surface(V, F).faces_out(fine, eps * eps, eps / 2))
+        got, st = c.smooth_stars(off, tets, cen, ff, kinds)
+        S = oracle.surface(V, F)
+        want, wst = oracle.smooth_stars(xyz, off, tets, cen, ff, kinds, surface=S, boundary=S,
+                                        eps2=eps * eps, sd=eps / 2, max_step=1, max_it=8)
+        assert np.array_equal(st.astype(np.int8), wst) and np.array_equal(got, want)
