@@ -307,6 +307,20 @@ TW_API int tw_energy_stats(tw_ctx* ctx, const int32_t* tets, int64_t n, const ui
 TW_API double tw_filter_energy(const int64_t* buckets, double filter_energy_thres,
                                int* is_clean_up);
 
+/* ---- dihedral-angle sweep ------------------------------------------------------------
+ * Replaces: LocalOperations::calTetQuality_AD over the live tets
+ * (LocalOperations.cpp:783-860, called by outputInfo :350-353) and
+ * outputInfo's statistics over them (:483-521) at the resident positions.
+ * locked[i] != 0 (NULL: none) excludes tet i from the statistics.
+ * out = {smallest min angle (10 when no tet counts), mean min angle, largest
+ * max angle, mean max angle} in radians, the means from double-double sums;
+ * counts = {min angle < 6, < 12, < 18 degrees, max angle > 162, > 168,
+ * > 174 degrees, tets counted}.  min_angle / max_angle (may be NULL): each
+ * tet's (min_d_angle, max_d_angle).  Angles use CUDA's acos (within 2 ulp of
+ * the host's).                                                             */
+TW_API int tw_dihedral_stats(tw_ctx* ctx, const int32_t* tets, int64_t n, const uint8_t* locked,
+                             double* out, int64_t* counts, double* min_angle, double* max_angle);
+
 /* ---- edge-collapse checks ------------------------------------------------------------
  * Replaces: the checks of EdgeCollapser::collapseAnEdge (EdgeCollapser.cpp:
  * 284-446, decl EdgeCollapser.h:31) with isCollapsable_epsilon (:727-775)

@@ -91,6 +91,8 @@ class Oracle:
             "two_collapse_check_batch": ([_P, _P, _P, _P, _P, _P, _I64, _P, _P, _D, _D, _I, _D,
                                           _P, _I], None),
             "two_energy_stats": ([_P, _P, _I64, _P, _D, _P, _P, _P, _P], None),
+            "two_dihedral_minmax": ([_P, _P, _P], None),
+            "two_dihedral_stats": ([_P, _P, _I64, _P, _P, _P, _P, _P], None),
             "two_filter_energy": ([_P, _D, _P], _D),
         }
         for name, (args, res) in sig.items():
@@ -201,6 +203,27 @@ class Oracle:
                                         1 if check_quality else 0, soft_energy, _p(out), nthreads)
         return out
 
+
+    def dihedral_minmax(self, T12):
+        """calTetQuality_AD of one tet (12 coordinates): (min, max) dihedral angle."""
+        t = _c(T12, np.float64).reshape(12)
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self.L.two_dihedral_minmax(_p(t), ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def dihedral_stats(self, xyz, tets, locked=None):
+        """outputInfo's dihedral sweep: (out[4] = min, avg min, max, avg max; counts[7];
+        per-tet mins; per-tet maxs)."""
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        L = None if locked is None else _c(locked, np.uint8)
+        n = T.shape[0]
+        out = np.zeros(4)
+        cnt = np.zeros(7, np.int64)
+        mins = np.empty(n)
+        maxs = np.empty(n)
+        self.L.two_dihedral_stats(_p(X), _p(T), n, _p(L), _p(out), _p(cnt), _p(mins), _p(maxs))
+        return out, cnt, mins, maxs
 
     def energy_stats(self, xyz, tets, locked=None, thres=10.0):
         """(avg, max, second max, buckets[11]) of getAvgMaxEnergy / getMaxEnergy /

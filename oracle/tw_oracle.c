@@ -1335,6 +1335,124 @@ void two_energy_stats(const double* xyz, const int32_t* tets, int64_t n, const u
     *second_max = mx2;
 }
 
+/* =========================================================================
+ * Dihedral angles (calTetQuality_AD, LocalOperations.cpp:783-860) and the
+ * outputInfo sweep over them (:483-521).  For face i (the other three
+ * vertices p, q, r in cyclic order from i+1): the plane's normal
+ * (a, b, c) = (p - r) x (q - r) and offset d = -(a r.x + b r.y + c r.z); a
+ * zero normal is a degenerate face.  Vertex s = v_i projects to
+ * s - lambda (a, b, c), lambda = (a s + d) / (a a + b b + c c); nv_i = s - proj
+ * and its squared length is the height.  A face whose projection equals s,
+ * or whose nv or height is 0, gives (0, pi).  nv is rescaled by its largest
+ * component when that is below 1e-5.  The six angles are
+ * acos(-nv_a . nv_b / (|nv_a| |nv_b|)) over the vertex pairs (0,1), (1,2),
+ * (0,2), (2,3), (0,3), (3,1), clamped to [0, pi] outside [-1, 1].
+ * ========================================================================= */
+#define TWO_PI 3.14159265358979323846   /* M_PI */
+
+void two_dihedral_minmax(const double T[12], double* min_angle, double* max_angle)
+{
+    double nv[4][3], len[4];
+    for (int i = 0; i < 4; ++i) {
+        const double* sv = T + 3 * i;
+        const double* p = T + 3 * ((i + 1) % 4);
+        const double* q = T + 3 * ((i + 2) % 4);
+        const double* r = T + 3 * ((i + 3) % 4);
+        const double rp[3] = {p[0] - r[0], p[1] - r[1], p[2] - r[2]};
+        const double rq[3] = {q[0] - r[0], q[1] - r[1], q[2] - r[2]};
+        const double a = rp[1] * rq[2] - rq[1] * rp[2];
+        const double b = rp[2] * rq[0] - rq[2] * rp[0];
+        const double c = rp[0] * rq[1] - rq[0] * rp[1];
+        if (a == 0.0 && b == 0.0 && c == 0.0) {
+            *min_angle = 0.0;
+            *max_angle = TWO_PI;
+            return;
+        }
+        const double d = ((-a * r[0]) - b * r[1]) - c * r[2];
+        const double num = ((a * sv[0] + b * sv[1]) + c * sv[2]) + d;
+        const double den = (a * a + b * b) + c * c;
+        const double lam = num / den;
+        const double pr[3] = {sv[0] - lam * a, sv[1] - lam * b, sv[2] - lam * c};
+        if (pr[0] == sv[0] && pr[1] == sv[1] && pr[2] == sv[2]) {
+            *min_angle = 0.0;
+            *max_angle = TWO_PI;
+            return;
+        }
+        double v[3] = {sv[0] - pr[0], sv[1] - pr[1], sv[2] - pr[2]};
+        const double h = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+        double m = fabs(v[0]);
+        if (fabs(v[1]) > m) m = fabs(v[1]);
+        if (fabs(v[2]) > m) m = fabs(v[2]);
+        if (m == 0.0 || h == 0.0) {
+            *min_angle = 0.0;
+            *max_angle = TWO_PI;
+            return;
+        }
+        if (m < 1e-5) {
+            v[0] = v[0] / m;
+            v[1] = v[1] / m;
+            v[2] = v[2] / m;
+            len[i] = sqrt(h / (m * m));
+        } else {
+            len[i] = sqrt(h);
+        }
+        nv[i][0] = v[0];
+        nv[i][1] = v[1];
+        nv[i][2] = v[2];
+    }
+    static const int pa[6] = {0, 1, 0, 2, 0, 3}, pb[6] = {1, 2, 2, 3, 3, 1};
+    double mn = 0.0, mx = 0.0;
+    for (int k = 0; k < 6; ++k) {
+        const double* u = nv[pa[k]];
+        const double* w = nv[pb[k]];
+        const double cs = ((-u[0]) * w[0] + (-u[1]) * w[1] + (-u[2]) * w[2]) /
+                          (len[pa[k]] * len[pb[k]]);
+        const double ang = cs > 1.0 ? 0.0 : cs < -1.0 ? TWO_PI : acos(cs);
+        if (k == 0 || ang < mn) mn = ang;
+        if (k == 0 || ang > mx) mx = ang;
+    }
+    *min_angle = mn;
+    *max_angle = mx;
+}
+
+void two_dihedral_stats(const double* xyz, const int32_t* tets, int64_t n, const uint8_t* locked,
+                        double out[4], int64_t counts[7], double* mins, double* maxs)
+{
+    static const double cmp[6] = {6 / 180.0 * TWO_PI, 12 / 180.0 * TWO_PI, 18 / 180.0 * TWO_PI,
+                                  162 / 180.0 * TWO_PI, 168 / 180.0 * TWO_PI, 174 / 180.0 * TWO_PI};
+    double mn_all = 10.0, mx_all = 0.0, sum_mn = 0.0, sum_mx = 0.0;
+    int64_t cnt = 0;
+    for (int k = 0; k < 7; ++k) counts[k] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double T[12];
+        for (int j = 0; j < 4; ++j) {
+            const double* src = xyz + 3 * (size_t)tets[4 * i + j];
+            T[3 * j] = src[0];
+            T[3 * j + 1] = src[1];
+            T[3 * j + 2] = src[2];
+        }
+        double a, b;
+        two_dihedral_minmax(T, &a, &b);
+        if (mins) mins[i] = a;
+        if (maxs) maxs[i] = b;
+        if (locked && locked[i]) continue;
+        cnt++;
+        if (a < mn_all) mn_all = a;
+        if (b > mx_all) mx_all = b;
+        sum_mn += a;
+        sum_mx += b;
+        for (int j = 0; j < 3; ++j) {
+            if (a < cmp[j]) counts[j]++;
+            if (b > cmp[j + 3]) counts[j + 3]++;
+        }
+    }
+    counts[6] = cnt;
+    out[0] = mn_all;
+    out[1] = sum_mn / (double)cnt;
+    out[2] = mx_all;
+    out[3] = sum_mx / (double)cnt;
+}
+
 /* getFilterEnergy's choice over the buckets (LocalOperations.cpp:674-692). */
 double two_filter_energy(const int64_t buckets[11], double thres, int* is_clean_up)
 {

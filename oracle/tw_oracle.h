@@ -112,6 +112,15 @@ int two_collapse_check(const double* xyz, const int32_t* tets, const uint8_t* ff
                        int check_quality, double soft_energy);
 
 /* ---- energy sweeps (LocalOperations.cpp:605-693) ------------------------- */
+/* calTetQuality_AD (LocalOperations.cpp:783-860): the smallest and largest
+ * dihedral angle of tet T, (0, pi) for a degenerate one. */
+void two_dihedral_minmax(const double T[12], double* min_angle, double* max_angle);
+/* outputInfo's dihedral sweep (LocalOperations.cpp:483-521) over tets not
+ * locked: out = {min, sum of mins / cnt, max, sum of maxes / cnt} (sums in tet
+ * order), counts = {min < 6, 12, 18 deg, max > 162, 168, 174 deg, cnt};
+ * per-tet angles when mins / maxs are non-NULL. */
+void two_dihedral_stats(const double* xyz, const int32_t* tets, int64_t n, const uint8_t* locked,
+                        double out[4], int64_t counts[7], double* mins, double* maxs);
 void two_energy_stats(const double* xyz, const int32_t* tets, int64_t n, const uint8_t* locked,
                       double filter_energy_thres, double* avg, double* max_e,
                       double* second_max, int64_t buckets[11]);

@@ -108,3 +108,30 @@ def test_energy_sweeps_vs_oracle(ctx, oracle):
             assert mx == mxo and m2 == m2o and np.array_equal(b, bo)
             assert abs(a - ao) <= 1e-12 * abs(ao)
             assert ctx.filter_energy(b, thres) == oracle.filter_energy(bo, thres)
+
+
+def test_dihedral_sweep_vs_oracle(ctx, oracle):
+    """calTetQuality_AD over the whole mesh and outputInfo's statistics: per-tet angles
+    within 4 ulp (CUDA's acos against the host's), degenerate tets (0, pi) exactly,
+    extremes within 4 ulp, means within 1e-12, threshold counts identical."""
+    m = syn.icosphere_stage1_mesh(seed=6)
+    xyz = m["xyz"].copy()
+    tets = m["tets"].copy()
+    rng = np.random.default_rng(9)
+    xyz += rng.normal(0.0, 0.05 * m["edge"], xyz.shape)     # slivers and caps
+    flat = rng.choice(len(tets), 20, replace=False)
+    tets[flat, 3] = tets[flat, 2]                             # repeated vertex: degenerate
+    locked = (rng.random(len(tets)) < 0.05).astype(np.uint8)
+    ctx.mesh_upload(xyz)
+    for lk in (None, locked):
+        out, cnt, mins, maxs = ctx.dihedral_stats(tets, lk, per_tet=True)
+        wout, wcnt, wmins, wmaxs = oracle.dihedral_stats(xyz, tets, lk)
+        assert np.array_equal(mins[flat], np.zeros(20)) and np.all(maxs[flat] == math.pi)
+        assert np.allclose(mins, wmins, rtol=4 * 2.0 ** -52, atol=1e-300)
+        assert np.allclose(maxs, wmaxs, rtol=4 * 2.0 ** -52, atol=1e-300)
+        assert np.array_equal(cnt, wcnt) and cnt[6] == (len(tets) - (lk.sum() if lk is not None else 0))
+        assert abs(out[0] - wout[0]) <= 4 * 2.0 ** -52 * wout[0] + 1e-300
+        assert abs(out[2] - wout[2]) <= 4 * 2.0 ** -52 * wout[2]
+        assert abs(out[1] - wout[1]) <= 1e-12 * wout[1] and abs(out[3] - wout[3]) <= 1e-12 * wout[3]
+    out, cnt, mins, maxs = ctx.dihedral_stats(tets[:0])
+    assert cnt[6] == 0 and out[0] == 10.0 and out[2] == 0.0 and mins is None

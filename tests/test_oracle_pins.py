@@ -426,3 +426,46 @@ def test_energy_sweeps_match_reference_live(oracle, reflib, sigma):
         assert f == rf and clean == rclean
         seen.add((f, clean))
     assert len(seen) >= 2
+
+
+def _dihedral_numpy(t):
+    """Independent dihedral angles of one tet: pi minus the angle between the outward
+    normals of the two faces meeting at each edge."""
+    v = t.reshape(4, 3)
+    n = []
+    for i in range(4):
+        o = [j for j in range(4) if j != i]
+        nn = np.cross(v[o[1]] - v[o[0]], v[o[2]] - v[o[0]])
+        if np.dot(nn, v[i] - v[o[0]]) > 0:
+            nn = -nn
+        n.append(nn / np.linalg.norm(nn))
+    ang = [math.pi - math.acos(max(-1.0, min(1.0, float(np.dot(n[a], n[b])))))
+           for a in range(4) for b in range(a + 1, 4)]
+    return min(ang), max(ang)
+
+
+def test_dihedral_known_answers(oracle):
+    """calTetQuality_AD (LocalOperations.cpp:783-860): regular and corner tets, degenerate
+    tets give (0, pi), tiny tets take the rescaled branch, and random tets agree with an
+    independent computation from face normals."""
+    reg = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], float).reshape(12)
+    a, b = oracle.dihedral_minmax(reg)
+    assert abs(a - math.acos(1 / 3)) < 1e-15 and abs(b - math.acos(1 / 3)) < 1e-15
+    corner = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float).reshape(12)
+    a, b = oracle.dihedral_minmax(corner)
+    assert abs(a - math.acos(1 / math.sqrt(3))) < 1e-15 and abs(b - math.pi / 2) < 1e-15
+    for bad in ([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]],      # flat
+                [[0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 0, 1]],      # repeated vertex
+                [[0, 0, 0], [1, 0, 0], [2, 0, 0], [0, 0, 1]]):     # collinear face
+        assert oracle.dihedral_minmax(np.array(bad, float).reshape(12)) == (0.0, math.pi)
+    rng = np.random.default_rng(77)
+    for k in range(300):
+        t = rng.normal(size=12)
+        if k % 3 == 0:
+            t *= 1e-7                      # every nv component below 1e-5: rescaled
+        a, b = oracle.dihedral_minmax(t)
+        wa, wb = _dihedral_numpy(t)
+        assert abs(a - wa) < 1e-9 and abs(b - wb) < 1e-9
+        perm = rng.permutation(4)
+        pa, pb = oracle.dihedral_minmax(t.reshape(4, 3)[perm].reshape(12))
+        assert abs(pa - a) < 1e-12 and abs(pb - b) < 1e-12

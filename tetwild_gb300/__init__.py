@@ -136,6 +136,7 @@ _SIGS = {
     "tw_smooth_stars": [_P, _P, _P, _P, _P, _P, _I32, _P, _P],
     "tw_collapse_check": [_P, _P, _P, _P, _P, _P, _I32, _I, _D, _P],
     "tw_energy_stats": [_P, _P, _I64, _P, _D, _P, _P, _P, _P],
+    "tw_dihedral_stats": [_P, _P, _I64, _P, _P, _P, _P, _P],
     "tw_filter_energy": [_P, _D, _P],
     "tw_smooth_stars_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P],
     "tw_smooth_autotune_device": [_P, _P, _P, _P, _P, _P, _I32, _I64, _P, _P, ctypes.POINTER(_I),
@@ -432,6 +433,20 @@ class Context:
                                              filter_energy_thres, ctypes.byref(a), ctypes.byref(m),
                                              ctypes.byref(m2), _ptr(b)))
         return a.value, m.value, m2.value, b
+
+    def dihedral_stats(self, tets, locked=None, per_tet=False):
+        """calTetQuality_AD over tets of the resident mesh and outputInfo's statistics:
+        (out[4] = min, mean min, max, mean max; counts[7]; per-tet mins, maxs or None)."""
+        T = _c(tets, np.int32).reshape(-1, 4)
+        L = None if locked is None else _c(locked, np.uint8)
+        n = T.shape[0]
+        out = np.zeros(4)
+        cnt = np.zeros(7, np.int64)
+        mins = np.empty(n) if per_tet else None
+        maxs = np.empty(n) if per_tet else None
+        self._check(self.lib.tw_dihedral_stats(self.h, _ptr(T), n, _ptr(L), _ptr(out), _ptr(cnt),
+                                               _ptr(mins), _ptr(maxs)))
+        return out, cnt, mins, maxs
 
     def filter_energy(self, buckets, filter_energy_thres=10.0):
         b = _c(buckets, np.int64)

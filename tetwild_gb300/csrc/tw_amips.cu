@@ -507,6 +507,181 @@ __global__ void k_energy_stats_sum(const DD* __restrict__ block_sum, int nblocks
 
 int energy_stats_blocks(int64_t n) { return grid_for(n > 0 ? n : 1, kStatsBlock, 4); }
 
+// ---------------------------------------------------------------------------
+// Dihedral angles (calTetQuality_AD, LocalOperations.cpp:783-860) and
+// outputInfo's sweep over them (:483-521).  Per face i (the other vertices
+// p, q, r from i+1 on): normal (a, b, c) = (p - r) x (q - r), offset
+// d = -(a r.x + b r.y + c r.z); vertex s = v_i projects to s - lambda (a, b, c)
+// with lambda = (a s + d) / |(a, b, c)|^2; nv_i = s - projection, rescaled by
+// its largest component below 1e-5.  A zero normal, a projection equal to s or
+// a zero nv gives (0, pi).  Angles acos(-nv_a . nv_b / (|nv_a| |nv_b|)) over
+// the pairs (0,1), (1,2), (0,2), (2,3), (0,3), (3,1).  Operation for operation
+// as the oracle; acos is CUDA's.
+// ---------------------------------------------------------------------------
+constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ void tet_dihedral_minmax(const double* T, double& mn, double& mx) {
+    double nv[4][3], len[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const double* sv = T + 3 * i;
+        const double* p = T + 3 * ((i + 1) % 4);
+        const double* q = T + 3 * ((i + 2) % 4);
+        const double* r = T + 3 * ((i + 3) % 4);
+        const double rp0 = p[0] - r[0], rp1 = p[1] - r[1], rp2 = p[2] - r[2];
+        const double rq0 = q[0] - r[0], rq1 = q[1] - r[1], rq2 = q[2] - r[2];
+        const double a = rp1 * rq2 - rq1 * rp2;
+        const double b = rp2 * rq0 - rq2 * rp0;
+        const double c = rp0 * rq1 - rq0 * rp1;
+        if (a == 0.0 && b == 0.0 && c == 0.0) {
+            mn = 0.0;
+            mx = kPi;
+            return;
+        }
+        const double d = ((-a * r[0]) - b * r[1]) - c * r[2];
+        const double num = ((a * sv[0] + b * sv[1]) + c * sv[2]) + d;
+        const double den = (a * a + b * b) + c * c;
+        const double lam = num / den;
+        const double pr0 = sv[0] - lam * a, pr1 = sv[1] - lam * b, pr2 = sv[2] - lam * c;
+        if (pr0 == sv[0] && pr1 == sv[1] && pr2 == sv[2]) {
+            mn = 0.0;
+            mx = kPi;
+            return;
+        }
+        double v0 = sv[0] - pr0, v1 = sv[1] - pr1, v2 = sv[2] - pr2;
+        const double h = (v0 * v0 + v1 * v1) + v2 * v2;
+        double m = fabs(v0);
+        if (fabs(v1) > m) m = fabs(v1);
+        if (fabs(v2) > m) m = fabs(v2);
+        if (m == 0.0 || h == 0.0) {
+            mn = 0.0;
+            mx = kPi;
+            return;
+        }
+        if (m < 1e-5) {
+            v0 = v0 / m;
+            v1 = v1 / m;
+            v2 = v2 / m;
+            len[i] = sqrt(h / (m * m));
+        } else {
+            len[i] = sqrt(h);
+        }
+        nv[i][0] = v0;
+        nv[i][1] = v1;
+        nv[i][2] = v2;
+    }
+    const int pa[6] = {0, 1, 0, 2, 0, 3}, pb[6] = {1, 2, 2, 3, 3, 1};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double* u = nv[pa[k]];
+        const double* w = nv[pb[k]];
+        const double cs =
+            ((-u[0]) * w[0] + (-u[1]) * w[1] + (-u[2]) * w[2]) / (len[pa[k]] * len[pb[k]]);
+        const double ang = cs > 1.0 ? 0.0 : cs < -1.0 ? kPi : acos(cs);
+        if (k == 0 || ang < mn) mn = ang;
+        if (k == 0 || ang > mx) mx = ang;
+    }
+}
+
+// acc: [0] min bits (initialised to 10.0's), [1] max bits, [2..7] threshold
+// counts, [8] unlocked count; block_sum: per block the DD sums of the mins
+// and of the maxes.
+__global__ void __launch_bounds__(kStatsBlock) k_dihedral_stats(
+    const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,
+    const double* __restrict__ vy, const double* __restrict__ vz,
+    const uint8_t* __restrict__ locked, double* __restrict__ mins, double* __restrict__ maxs,
+    DD* __restrict__ block_sum, unsigned long long* __restrict__ acc) {
+    __shared__ DD ssum[2][kStatsBlock / 32];
+    const double cmp[6] = {6 / 180.0 * kPi, 12 / 180.0 * kPi, 18 / 180.0 * kPi,
+                           162 / 180.0 * kPi, 168 / 180.0 * kPi, 174 / 180.0 * kPi};
+    DD smn{0.0, 0.0}, smx{0.0, 0.0};
+    unsigned long long bmn = (unsigned long long)__double_as_longlong(10.0), bmx = 0, cnt = 0;
+    unsigned long long c6[6] = {0, 0, 0, 0, 0, 0};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int4 tv = __ldg(tets + i);
+        const int id[4] = {tv.x, tv.y, tv.z, tv.w};
+        double t[12];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            t[3 * j] = __ldg(vx + id[j]);
+            t[3 * j + 1] = __ldg(vy + id[j]);
+            t[3 * j + 2] = __ldg(vz + id[j]);
+        }
+        double a = 0.0, b = 0.0;
+        tet_dihedral_minmax(t, a, b);
+        if (mins) mins[i] = a;
+        if (maxs) maxs[i] = b;
+        if (locked && __ldg(locked + i)) continue;
+        // angles are >= 0: their bit patterns order as the values
+        bmn = min(bmn, (unsigned long long)__double_as_longlong(a));
+        bmx = max(bmx, (unsigned long long)__double_as_longlong(b));
+        smn = dd_add(smn, DD{a, 0.0});
+        smx = dd_add(smx, DD{b, 0.0});
+        ++cnt;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            c6[j] += a < cmp[j] ? 1 : 0;
+            c6[j + 3] += b > cmp[j + 3] ? 1 : 0;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DD x{__shfl_down_sync(0xffffffffu, smn.hi, o), __shfl_down_sync(0xffffffffu, smn.lo, o)};
+        smn = dd_add(smn, x);
+        DD y{__shfl_down_sync(0xffffffffu, smx.hi, o), __shfl_down_sync(0xffffffffu, smx.lo, o)};
+        smx = dd_add(smx, y);
+        bmn = min(bmn, __shfl_down_sync(0xffffffffu, bmn, o));
+        bmx = max(bmx, __shfl_down_sync(0xffffffffu, bmx, o));
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) c6[j] += __shfl_down_sync(0xffffffffu, c6[j], o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ssum[0][threadIdx.x >> 5] = smn;
+        ssum[1][threadIdx.x >> 5] = smx;
+        atomicMin(acc + 0, bmn);
+        atomicMax(acc + 1, bmx);
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+            if (c6[j]) atomicAdd(acc + 2 + j, c6[j]);
+        if (cnt) atomicAdd(acc + 8, cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        DD a = ssum[0][0], b = ssum[1][0];
+        for (int w = 1; w < kStatsBlock / 32; ++w) {
+            a = dd_add(a, ssum[0][w]);
+            b = dd_add(b, ssum[1][w]);
+        }
+        block_sum[2 * blockIdx.x] = a;
+        block_sum[2 * blockIdx.x + 1] = b;
+    }
+}
+
+__global__ void k_dihedral_stats_sum(const DD* __restrict__ block_sum, int nblocks,
+                                     double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    DD a{0.0, 0.0}, b{0.0, 0.0};
+    for (int k = 0; k < nblocks; ++k) {
+        a = dd_add(a, block_sum[2 * k]);
+        b = dd_add(b, block_sum[2 * k + 1]);
+    }
+    out[0] = a.hi + a.lo;
+    out[1] = b.hi + b.lo;
+}
+
+void launch_dihedral_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                           const double* vz, const uint8_t* locked, double* mins, double* maxs,
+                           void* block_sum, unsigned long long* acc, double* sums_out,
+                           cudaStream_t s) {
+    const int blocks = energy_stats_blocks(n);
+    k_dihedral_stats<<<blocks, kStatsBlock, 0, s>>>(reinterpret_cast<const int4*>(tets), n, vx,
+                                                    vy, vz, locked, mins, maxs, (DD*)block_sum,
+                                                    acc);
+    k_dihedral_stats_sum<<<1, 32, 0, s>>>((const DD*)block_sum, blocks, sums_out);
+}
+
 void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                          const double* vz, const uint8_t* locked, double thres,
                          void* block_sum, unsigned long long* acc, double* sum_out,

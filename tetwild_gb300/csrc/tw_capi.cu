@@ -1038,6 +1038,67 @@ int tw_energy_stats(tw_ctx* c, const int32_t* tets, int64_t n, const uint8_t* lo
     return TW_OK;
 }
 
+int tw_dihedral_stats(tw_ctx* c, const int32_t* tets, int64_t n, const uint8_t* locked,
+                      double* out, int64_t* counts, double* min_angle, double* max_angle) {
+    if (!c || n < 0 || (n > 0 && !tets) || !out || !counts) return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    Guard g(c->device);
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const int nb = energy_stats_blocks(n);
+    const bool per = min_angle || max_angle;
+    const size_t bytes = align(16 * (size_t)n) + align((size_t)n) + align(32 * (size_t)nb) +
+                         align(9 * 8) + align(16) + (per ? 2 * align(8 * (size_t)n) : 0) + 256;
+    void* p;
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)n);
+    uint8_t* dl = (uint8_t*)q; q += align((size_t)n);
+    void* dbs = q; q += align(32 * (size_t)nb);
+    unsigned long long* dacc = (unsigned long long*)q; q += align(9 * 8);
+    double* dsum = (double*)q; q += align(16);
+    double* dmin = per ? (double*)q : nullptr; q += per ? align(8 * (size_t)n) : 0;
+    double* dmax = per ? (double*)q : nullptr;
+    int* bad = (int*)(c->counters + kCntBad);
+    unsigned long long init[9] = {0};
+    const double ten = 10.0;
+    std::memcpy(&init[0], &ten, 8);
+    cudaMemsetAsync(bad, 0, sizeof(int), c->stream);
+    cudaMemcpyAsync(dacc, init, sizeof init, cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(dsum, 0, 16, c->stream);
+    if (n > 0) {
+        cudaMemcpyAsync(dt, tets, 16 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+        if (locked) cudaMemcpyAsync(dl, locked, (size_t)n, cudaMemcpyHostToDevice, c->stream);
+        k_check_ids<<<(unsigned)((4 * n + 255) / 256), 256, 0, c->stream>>>(dt, 4 * n, c->nv, bad);
+    }
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_dihedral_stats");
+    if (st != TW_OK) return st;
+    if (hbad) return fail(c, TW_ERR_ARG, "tet vertex id out of range");
+    if (n > 0)
+        launch_dihedral_stats(dt, n, c->vx, c->vy, c->vz, locked ? dl : nullptr, dmin, dmax, dbs,
+                              dacc, dsum, c->stream);
+    unsigned long long hacc[9];
+    double hsum[2] = {0.0, 0.0};
+    cudaMemcpyAsync(hacc, dacc, sizeof hacc, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(hsum, dsum, 16, cudaMemcpyDeviceToHost, c->stream);
+    if (n > 0 && min_angle)
+        cudaMemcpyAsync(min_angle, dmin, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    if (n > 0 && max_angle)
+        cudaMemcpyAsync(max_angle, dmax, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_dihedral_stats");
+    if (st != TW_OK) return st;
+    const double cnt = (double)hacc[8];
+    out[0] = __longlong_as_double_host(hacc[0]);
+    out[1] = hsum[0] / cnt;
+    out[2] = __longlong_as_double_host(hacc[1]);
+    out[3] = hsum[1] / cnt;
+    for (int k = 0; k < 6; ++k) counts[k] = (int64_t)hacc[2 + k];
+    counts[6] = (int64_t)hacc[8];
+    return TW_OK;
+}
+
 double tw_filter_energy(const int64_t* b, double thres, int* is_clean_up) {
     int64_t t1[10], t2[10];
     for (int i = 0; i < 10; ++i) {

@@ -193,6 +193,14 @@ void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, co
 // 14 words zeroed by the caller (max bits, second-max bits, unlocked count,
 // 11 buckets); sum_out the unlocked energies' sum.
 int energy_stats_blocks(int64_t n);
+// Dihedral sweep: block_sum holds 2 x energy_stats_blocks(n) double-doubles;
+// acc 9 words set by the caller (min bits = 10.0's, max bits 0, 6 threshold
+// counts, unlocked count); sums_out the unlocked mins' and maxes' sums;
+// mins / maxs per tet (may be null).
+void launch_dihedral_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
+                           const double* vz, const uint8_t* locked, double* mins, double* maxs,
+                           void* block_sum, unsigned long long* acc, double* sums_out,
+                           cudaStream_t s);
 void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                          const double* vz, const uint8_t* locked, double thres,
                          void* block_sum, unsigned long long* acc, double* sum_out,
