@@ -119,3 +119,44 @@ def test_errors_leave_the_context_usable(ctx, oracle, setup):
         want, wst = oracle.smooth_stars(xyz, off, tets, cen, ff, kinds, surface=S, boundary=S,
                                         eps2=eps * eps, sd=eps / 2, max_step=1, max_it=8)
         assert np.array_equal(st.astype(np.int8), wst) and np.array_equal(got, want)
+
+
+def test_reference_named_mirror(ctx, oracle, setup):
+    """tetwild_gb300.LocalOperations / VertexSmoother: every method under its reference
+    name answers as the oracle does."""
+    V, F, eps, xyz, off, tets, ff, cen, kinds = setup
+    ctx.set_params(eps * eps, eps / 2, 15, 20)
+    ctx.surface_upload(V, F)
+    ctx.surface_upload(V, F, tw.TW_SURFACE_BOUNDARY)
+    ops = tw.LocalOperations(ctx, xyz)
+    T = np.ascontiguousarray(xyz[tets].reshape(-1, 12))
+    E, J, H, Fl = oracle.amips_batch_soa(T.T.copy(), quality=False)
+    assert np.array_equal(ops.comformalAMIPSEnergy_new(T), E)
+    assert np.array_equal(ops.comformalAMIPSJacobian_new(T), J.T)
+    assert np.array_equal(ops.comformalAMIPSHessian_new(T), H.T)
+    Eq, _, _, Fq = oracle.amips_batch_soa(T.T.copy(), quality=True)
+    assert np.array_equal(ops.calTetQualities(tets), Eq)
+    assert ops.isFlip(tets) == bool(Fq.any()) and ops.isTetFlip(tets[0]) == bool(Fq[0])
+    S = oracle.surface(V, F)
+    P = syn.envelope_points(V, F, 64, eps, seed=4)
+    want = S.points_out(P, eps * eps)
+    assert [ops.isPointOutEnvelop(p) for p in P] == [bool(w) for w in want]
+    assert [ops.isPointOutBoundaryEnvelop(p) for p in P[:8]] == [bool(w) for w in want[:8]]
+    tri = np.hstack([V[F[:6, 0]], V[F[:6, 1]], V[F[:6, 2]]])
+    wf = S.faces_out(tri, eps * eps, eps / 2)
+    assert [ops.isFaceOutEnvelop(t) for t in tri] == [bool(w) for w in wf]
+    a, m = ops.getAvgMaxEnergy(tets)
+    wa, wm, wm2, wb = oracle.energy_stats(xyz, tets)
+    assert m == wm and abs(a - wa) <= 1e-12 * abs(wa)
+    assert ops.getMaxEnergy(tets) == wm and ops.getSecondMaxEnergy(tets) == wm2
+    assert ops.getFilterEnergy(tets) == oracle.filter_energy(wb)
+    mins, maxs = ops.calTetQuality_AD(tets)
+    _, _, wmins, wmaxs = oracle.dihedral_stats(xyz, tets)
+    assert np.allclose(mins, wmins, rtol=4 * 2.0 ** -52) and np.allclose(maxs, wmaxs, rtol=4 * 2.0 ** -52)
+    vs = tw.VertexSmoother(ctx, xyz)
+    inner = np.nonzero(kinds == 0)[0]
+    so = np.concatenate([[0], np.cumsum(np.diff(off)[inner])]).astype(np.int32)
+    st = np.concatenate([tets[off[i]:off[i + 1]] for i in inner])
+    pos, moved = vs.NewtonsMethod(so, st, cen[inner])
+    wpos, wmoved = oracle.newton_stars(xyz, so, st, cen[inner])
+    assert np.array_equal(pos, wpos) and np.array_equal(moved, wmoved)

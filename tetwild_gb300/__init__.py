@@ -600,6 +600,29 @@ class LocalOperations:
     def isFaceOutEnvelop(self, tri) -> bool:
         return bool(self.ctx.envelope_faces(np.asarray(tri).reshape(1, 9))[0])
 
+    # full-mesh sweeps over the live tets (LocalOperations.cpp:605-693, :783-860);
+    # locked: isTetLocked_ui per tet
+    def getAvgMaxEnergy(self, tets, locked=None):
+        a, m, _, _ = self.ctx.energy_stats(tets, locked)
+        return a, m
+
+    def getMaxEnergy(self, tets, locked=None) -> float:
+        return self.ctx.energy_stats(tets, locked)[1]
+
+    def getSecondMaxEnergy(self, tets, locked=None) -> float:
+        return self.ctx.energy_stats(tets, locked)[2]
+
+    def getFilterEnergy(self, tets, filter_energy_thres=10.0):
+        """(filter energy, is_clean_up); is_clean_up is set only by the first branch, as in
+        the reference (False otherwise)."""
+        b = self.ctx.energy_stats(tets, None, filter_energy_thres)[3]
+        return self.ctx.filter_energy(b, filter_energy_thres)
+
+    def calTetQuality_AD(self, tets):
+        """(min_d_angle [n], max_d_angle [n]) of each tet, radians."""
+        _, _, mins, maxs = self.ctx.dihedral_stats(tets, None, per_tet=True)
+        return mins, maxs
+
 
 class Server:
     """The serving loop (tw_server_*): many jobs resident in HBM, their query batches joined
