@@ -203,3 +203,28 @@ def test_certified_amips_edge_cases(ctx):
     assert np.array_equal(fa, np.isfinite(b["E"]) & (b["E"] < 1e50))
     assert np.all(np.abs(b["E"][fa] - a["E"][fa]) <= E_TOL32 * a["E"][fa])
     assert np.array_equal(a["E"][~fa], b["E"][~fa])
+
+
+def test_certified_without_grid(ctx, oracle):
+    """A facet whose box spans more than 2^16 grid cells leaves the surface without a grid:
+    the certified point and face tests fall back to the tree walk (warp-shared candidates),
+    with the same decisions."""
+    Vs, Fs = syn.icosphere(3)
+    big = np.array([[-50.0, -50.0, 3.0], [50.0, -50.0, 3.0], [0.0, 50.0, 3.0]])
+    V = np.vstack([Vs, big])
+    F = np.vstack([Fs, np.array([[len(Vs), len(Vs) + 1, len(Vs) + 2]])]).astype(np.int32)
+    eps = 2e-3
+    rng = np.random.default_rng(31)
+    P = np.vstack([syn.envelope_points(Vs, Fs, 20000, eps, seed=32),
+                   np.c_[rng.uniform(-40, 40, (5000, 2)), 3.0 + rng.uniform(-2 * eps, 2 * eps, 5000)]])
+    ctx.set_params(eps * eps, eps / 2)
+    ctx.surface_upload(V, F)
+    a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P))
+    want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
+    assert np.array_equal(a, want) and np.array_equal(b, want)
+    assert 0 < want.sum() < len(P)
+    tri = np.hstack([Vs[Fs[:200, 0]], Vs[Fs[:200, 1]], Vs[Fs[:200, 2]]])
+    tri = tri + rng.uniform(-1.5 * eps, 1.5 * eps, (len(tri), 1))
+    fa, fb, _ = _both_modes(ctx, lambda: ctx.envelope_faces(tri))
+    fw = oracle.surface(V, F).faces_out(tri, eps * eps, eps / 2, nthreads=8)
+    assert np.array_equal(fa, fw) and np.array_equal(fb, fw)
