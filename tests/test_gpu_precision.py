@@ -73,12 +73,15 @@ def _soup(n, size, seed):
     return V, np.arange(3 * n, dtype=np.int32).reshape(n, 3)
 
 
-@pytest.mark.parametrize("cell", [0.05, 0.1, 0.2, 1.0])
-def test_certified_grid_keeps_every_facet_within_reach(ctx, oracle, cell):
+@pytest.mark.parametrize("cell,offset", [(0.05, 0.0), (0.1, 0.0), (0.2, 0.0), (1.0, 0.0),
+                                         (0.1, 1000.0)])
+def test_certified_grid_keeps_every_facet_within_reach(ctx, oracle, cell, offset):
     """Points just inside eps of a random point of a random facet (interior, edges and
     corners), in random directions: a facet dropped from a cell's list by the grid's
-    separating-axis culling would turn such a point out."""
+    separating-axis culling would turn such a point out.  The offset moves the soup far
+    from the origin, where binary32 rounding of the culling is largest."""
     V, F = _soup(3000, 0.05, seed=21)
+    V = V + offset
     eps = 2e-3
     rng = np.random.default_rng(22)
     n = 60000
