@@ -387,9 +387,11 @@ def run_ours(args):
         "clocks": cert["clocks"],
         "wall_s_timed": cert["wall"],
     }
-    if not args.no_batching:
+    # the star-batch and serving configurations are single-GPU workloads: under
+    # torchrun (N > 1) the line carries the scaled step only
+    if not args.no_batching and ws == 1:
         line["batching"] = run_batching(ctx, V, F, args, dev, ws)
-    if not args.no_serving:
+    if not args.no_serving and ws == 1:
         line["serving"] = run_serving(args, dev)
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle.oracle import default_threads
