@@ -758,8 +758,9 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     }
     const EnvTree T = env_tree_for(S, eps2);
     const EpsParams E = eps_params(eps2);
-    // at least 6 blocks of 128 threads per SM (85 registers): measured best of
-    // 1, 6 and 8 on the 10M-point workload (8 spills)
+    // the tree-walk kernels: at least 6 blocks of 128 threads per SM (85
+    // registers), measured best of 1, 6 and 8 on the 10M-point workload (8
+    // spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
     if (precision == TW_PRECISION_FP32_CERTIFIED && T.gslot) {
         // 768 resident threads per SM (85 registers) in every block shape
