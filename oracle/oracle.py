@@ -29,12 +29,18 @@ def build_oracle() -> Path:
     return ORACLE_SO
 
 
-def build_ref() -> Path | None:
-    """Slice (when the reference checkout is present) and compile oracle/_ref."""
+def _recipe():
+    """oracle/ref/build_ref.py, the recipe that slices and compiles the reference."""
     import importlib.util
     spec = importlib.util.spec_from_file_location("tw_build_ref", HERE / "ref" / "build_ref.py")
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
+    return mod
+
+
+def build_ref() -> Path | None:
+    """Slice (when the reference checkout is present) and compile oracle/_ref."""
+    mod = _recipe()
     mod.do_slice()
     return mod.do_compile()
 
@@ -318,7 +324,7 @@ class RefLib:
     @staticmethod
     def available() -> bool:
         return REF_SO.exists() or (HERE / "_ref" / "src" / "amips_slice.inc").exists() or \
-            Path(os.environ.get("TW_REFERENCE_ROOT", "/root/reference"), "src").is_dir()
+            (_recipe().reference_root() / "src").is_dir()
 
     def amips_batch_soa(self, T, nthreads=1, energy=True, jacobian=True, hessian=True):
         T = _c(T, np.float64)
