@@ -231,3 +231,30 @@ def test_certified_without_grid(ctx, oracle):
     fa, fb, _ = _both_modes(ctx, lambda: ctx.envelope_faces(tri))
     fw = oracle.surface(V, F).faces_out(tri, eps * eps, eps / 2, nthreads=8)
     assert np.array_equal(fa, fw) and np.array_equal(fb, fw)
+
+
+def test_full_size_step_decisions(ctx, oracle):
+    """The bench's step at its full size: all 10M point decisions around the 100k-facet
+    displaced sphere in both precision modes, and the flips and energy sentinels of all
+    4M certified AMIPS evaluations, against the oracle (energies within 1e-5 of FP64)."""
+    from oracle.oracle import default_threads
+
+    V, F = syn.displaced_sphere(seed=0)
+    eps = 1e-3
+    P = syn.envelope_points(V, F, 10_000_000, eps, seed=1)
+    ctx.set_params(eps * eps, eps)
+    ctx.surface_upload(V, F)
+    a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P))
+    want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=default_threads())
+    assert np.array_equal(a, want) and np.array_equal(b, want)
+    T = syn.energy_batch(4_000_000, seed=3)
+    ctx.set_precision(tw.TW_PRECISION_FP32_CERTIFIED)
+    try:
+        g = ctx.amips(T, tw.TW_ENERGY_QUALITY, True, False, False, True)
+    finally:
+        ctx.set_precision(tw.TW_PRECISION_FP64)
+    E, _, _, Fl = oracle.amips_batch_soa(T, quality=True, jacobian=False, hessian=False,
+                                         nthreads=default_threads())
+    assert np.array_equal(g["flip"], Fl) and np.array_equal(g["E"] >= 1e50, E >= 1e50)
+    fin = E < 1e50
+    assert np.max(np.abs(g["E"][fin] - E[fin]) / E[fin]) <= 1e-5
