@@ -175,3 +175,28 @@ def test_smooth_device_graph_replay(ctx, oracle, sphere):
         assert np.array_equal(d_st.cpu().numpy().astype(np.int8), wst)
         assert np.array_equal(d_out.cpu().numpy().reshape(-1, 3), want)
     g.close()
+
+
+def test_smooth_pass_full_size(ctx, oracle):
+    """The bench's star batch at full size: 200,000 stars (half on the 100k-facet
+    displaced sphere), Newton max_step 1 / max_it 8 — every status and position
+    identical to the oracle in both precision modes."""
+    from oracle.oracle import default_threads
+
+    V, F = syn.displaced_sphere(seed=0)
+    xyz, off, tets, ff, cen, kinds = syn.mixed_star_batch(V, F, 200_000, EPS, seed=11,
+                                                          surface_fraction=0.5)
+    S = oracle.surface(V, F)
+    want, wst = oracle.smooth_stars(xyz, off, tets, cen, ff, kinds, surface=S, boundary=S,
+                                    eps2=EPS * EPS, sd=EPS / 2, max_step=1, max_it=8,
+                                    nthreads=default_threads())
+    ctx.set_params(EPS * EPS, EPS / 2, 1, 8)
+    ctx.surface_upload(V, F)
+    ctx.mesh_upload(xyz)
+    for precision in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
+        ctx.set_precision(precision)
+        try:
+            out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
+        finally:
+            ctx.set_precision(tw.TW_PRECISION_FP64)
+        assert np.array_equal(st.astype(np.int8), wst) and np.array_equal(out, want)
