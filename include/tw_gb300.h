@@ -442,6 +442,12 @@ TW_API int tw_server_get_stats(tw_server* srv, tw_server_stats* out);
  * counts round-to-nearest double->float mismatches, failures[1] exact
  * float->double mismatches.  Both must be 0.                               */
 TW_API int tw_self_test(tw_ctx* ctx, uint64_t samples, uint64_t* failures);
+/* The bounded wait of the bulk-copy AMIPS kernel: a barrier no copy completes
+ * must give up after `limit` polls (1 .. 2^20) and one fed by a bulk copy must
+ * complete.  result = {1 when the first gave up, 1 when the second completed,
+ * clock cycles the first took, the bits of the first copied double (1.5)}.
+ * The kernel faults nothing and leaves no copy in flight.                    */
+TW_API int tw_self_test_wait(tw_ctx* ctx, int32_t limit, uint64_t* result);
 
 /* ---- measured pipe peaks (roofline denominators) ------------------------------
  * Times a dependent-FMA loop over the whole GPU and returns FP64 and FP32

@@ -11,6 +11,7 @@ every call raises.
 from __future__ import annotations
 
 import ctypes
+import struct
 from pathlib import Path
 
 import numpy as np
@@ -151,6 +152,7 @@ _SIGS = {
     "tw_host_free": [_P],
     "tw_probe_peaks": [_P, ctypes.POINTER(_D), ctypes.POINTER(_D)],
     "tw_self_test": [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
+    "tw_self_test_wait": [_P, _I32, ctypes.POINTER(ctypes.c_uint64)],
     "tw_server_create": [_I, _SZ, _I, ctypes.POINTER(_P)],
     "tw_server_destroy": [_P],
     "tw_server_last_error": [_P],
@@ -515,6 +517,13 @@ class Context:
         f = (ctypes.c_uint64 * 2)()
         self._check(self.lib.tw_self_test(self.h, samples, f))
         return int(f[0]), int(f[1])
+
+    def self_test_wait(self, limit: int = 1 << 14):
+        """The bulk kernel's bounded wait: {'timed_out', 'completed', 'cycles', 'copied'}."""
+        r = (ctypes.c_uint64 * 4)()
+        self._check(self.lib.tw_self_test_wait(self.h, limit, r))
+        return {"timed_out": bool(r[0]), "completed": bool(r[1]), "cycles": int(r[2]),
+                "copied": struct.unpack("<d", struct.pack("<Q", r[3]))[0]}
 
     def probe_peaks(self):
         a, b = _D(), _D()

@@ -199,8 +199,8 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 
 // true when the barrier's phase with this parity completed within the limit
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 20); ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = 1 << 20) {
+    for (int it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n"
@@ -216,6 +216,36 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
+// Self-test of the bounded wait (one thread): a barrier whose phase needs 16
+// bytes that no copy delivers must give up after `limit` polls, and one fed by
+// a 16-byte bulk copy must complete.  out = {1 when the first gave up, 1 when
+// the second completed, cycles the first took, the first copied word}.
+__global__ void k_selftest_wait(const double* __restrict__ src, int limit,
+                                unsigned long long* __restrict__ out) {
+    __shared__ __align__(16) double buf[2];
+    __shared__ __align__(8) uint64_t bar[2];
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(&bar[0], 16);   // no copy will complete this phase
+    const long long t0 = clock64();
+    const bool done0 = mbar_wait(&bar[0], 0, limit);
+    const long long t1 = clock64();
+    mbar_expect_tx(&bar[1], 16);
+    bulk_g2s(buf, src, 16, &bar[1]);
+    bool done1 = mbar_wait(&bar[1], 0);
+    if (!done1) done1 = mbar_wait(&bar[1], 0);   // no copy may outlive the kernel
+    out[0] = done0 ? 0ULL : 1ULL;
+    out[1] = done1 ? 1ULL : 0ULL;
+    out[2] = (unsigned long long)(t1 - t0);
+    out[3] = done1 ? (unsigned long long)__double_as_longlong(buf[0]) : 0ULL;
+}
+
+void launch_selftest_wait(const double* src, int limit, unsigned long long* out, cudaStream_t s) {
+    k_selftest_wait<<<1, 32, 0, s>>>(src, limit, out);
+}
+
 template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
 __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
     const double* __restrict__ T, int64_t n, double* __restrict__ E, double* __restrict__ J,
@@ -224,16 +254,21 @@ __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
     double(*stage)[12 * kBulkTile] = reinterpret_cast<double(*)[12 * kBulkTile]>(stage_mem);
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int abort_flag;
+    __shared__ int pend[kBulkStages];   // a copy issued into stage k and not yet consumed
     uint32_t ntet = 0, nfp64 = 0, nexact = 0;
     const int64_t full = n / kBulkTile;               // full tiles
     const int64_t ntiles = (n + kBulkTile - 1) / kBulkTile;
     if (threadIdx.x == 0) {
-        for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
+        for (int k = 0; k < kBulkStages; ++k) {
+            mbar_init(&bar[k], 1);
+            pend[k] = 0;
+        }
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     auto issue = [&](int64_t tile, int k) {
+        pend[k] = 1;
         mbar_expect_tx(&bar[k], 12 * kBulkTile * 8);
         for (int c = 0; c < 12; ++c)
             bulk_g2s(&stage[k][c * kBulkTile], T + (int64_t)c * n + tile * kBulkTile,
@@ -252,12 +287,20 @@ __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
         double t[12];
         if (tile < full) {
             if (!mbar_wait(&bar[k], phase[k])) atomicExch(&abort_flag, 1);
-            phase[k] ^= 1u;
             __syncthreads();
             if (abort_flag) {
-                if (threadIdx.x == 0) atomicOr(counters + kCntError, 32ULL);
+                // leave no copy writing into this block's shared memory: wait
+                // again, with the same limit, for every stage still pending
+                if (threadIdx.x == 0) {
+                    atomicOr(counters + kCntError, 32ULL);
+                    for (int s2 = 0; s2 < kBulkStages; ++s2)
+                        if (pend[s2]) mbar_wait(&bar[s2], phase[s2]);
+                }
+                __syncthreads();
                 break;
             }
+            phase[k] ^= 1u;
+            if (threadIdx.x == 0) pend[k] = 0;
 #pragma unroll
             for (int c = 0; c < 12; ++c) t[c] = stage[k][c * kBulkTile + threadIdx.x];
             __syncthreads();  // every thread has its coordinates: the stage may be refilled

@@ -1352,6 +1352,22 @@ int tw_self_test(tw_ctx* c, uint64_t samples, uint64_t* failures) {
     return sync_status(c, "tw_self_test");
 }
 
+int tw_self_test_wait(tw_ctx* c, int32_t limit, uint64_t* result) {
+    if (!c || !result || limit < 1 || limit > (1 << 20)) return TW_ERR_ARG;
+    Guard g(c->device);
+    void* p;
+    int st = ensure(c, 6, 256, &p);
+    if (st != TW_OK) return st;
+    const double src[2] = {1.5, 2.5};
+    double* dsrc = (double*)p;
+    unsigned long long* dout = (unsigned long long*)((char*)p + 128);
+    cudaMemcpyAsync(dsrc, src, sizeof src, cudaMemcpyHostToDevice, c->stream);
+    cudaMemsetAsync(dout, 0, 32, c->stream);
+    launch_selftest_wait(dsrc, limit, dout, c->stream);
+    cudaMemcpyAsync(result, dout, 32, cudaMemcpyDeviceToHost, c->stream);
+    return sync_status(c, "tw_self_test_wait");
+}
+
 int tw_probe_peaks(tw_ctx* c, double* fp64_tflops, double* fp32_tflops) {
     if (!c || !fp64_tflops || !fp32_tflops) return TW_ERR_ARG;
     Guard g(c->device);

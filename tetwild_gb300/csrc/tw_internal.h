@@ -193,6 +193,9 @@ void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, co
 // 14 words zeroed by the caller (max bits, second-max bits, unlocked count,
 // 11 buckets); sum_out the unlocked energies' sum.
 int energy_stats_blocks(int64_t n);
+// The bounded-wait self-test (tw_amips.cu): src 16 bytes, 16-byte aligned, on
+// the device; out 4 words on the device.
+void launch_selftest_wait(const double* src, int limit, unsigned long long* out, cudaStream_t s);
 // Dihedral sweep: block_sum holds 2 x energy_stats_blocks(n) double-doubles;
 // acc 9 words set by the caller (min bits = 10.0's, max bits 0, 6 threshold
 // counts, unlocked count); sums_out the unlocked mins' and maxes' sums;
