@@ -20,6 +20,12 @@ rational arithmetic (Python fractions) for the orientation signs:
                     far from it, and the closest points and squared
                     distances of the reference's
                     MeshFacetsAABBWithEps::nearest_facet (mesh_AABB.h:130)
+  energy_sweeps_ref.npz
+                    tets of three energy spreads (some inverted, some
+                    locked) and the reference's getAvgMaxEnergy /
+                    getMaxEnergy / getSecondMaxEnergy / getFilterEnergy
+                    results over their calTetQualities energies
+                    (LocalOperations.cpp:605-693) at three filter thresholds
 
 Run: python tests/golden/make_golden.py [fixture names without .npz]
 (all fixtures when no name is given)
@@ -36,7 +42,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
-from oracle.oracle import RefLib  # noqa: E402
+from oracle.oracle import Oracle, RefLib  # noqa: E402
 from tetwild_gb300 import synthetic as syn  # noqa: E402
 
 
@@ -120,14 +126,55 @@ def make_nearest(ref):
     np.savez_compressed(HERE / "nearest_ref.npz", V=V, F=F, P=P, Q=Q, D=D)
 
 
+SWEEP_SIGMAS = (0.1, 0.6, 2.0)
+SWEEP_THRES = (1.0, 3.0, 10.0)
+
+
+def make_sweeps(ref):
+    """The sweeps' input is the oracle's calTetQualities energies (AMIPS energy, or the 1e50
+    sentinel for an inverted tet), stored as E: they agree with the reference's
+    comformalAMIPSEnergy_new to its forward error (amips_ref.npz pins that), not bit for
+    bit, so the reference's sweeps run over exactly these values.  The results are the
+    reference's."""
+    o = Oracle()
+    n = 600
+    Ts, Ls, Es, R = [], [], [], []
+    for c, sigma in enumerate(SWEEP_SIGMAS):
+        rng = np.random.default_rng(300 + c)
+        T = syn.energy_batch(n, seed=310 + c, sigma_rel=sigma)
+        flip = rng.random(n) < 0.03
+        T[0:3, flip], T[3:6, flip] = T[3:6, flip].copy(), T[0:3, flip].copy()
+        locked = (rng.random(n) < 0.1).astype(np.uint8)
+        E = o.amips_batch_soa(T, quality=True, jacobian=False, hessian=False)[0]
+        Er = ref.amips_batch_soa(T, jacobian=False, hessian=False)[0]
+        live = E != 1e50
+        # a loose sanity bound: the per-tet forward-error bound (up to 1.2e-10 relative on
+        # these spreads, for tets of energy near 1e3) is what amips_ref.npz checks
+        assert (np.abs(E[live] / Er[live] - 1.0) < 1e-8).all() and (~live).any()
+        rows = []
+        for thres in SWEEP_THRES:
+            a, m, _, m2, f, clean = ref.energy_sweeps(E, None, locked, thres)
+            rows.append([a, m, m2, f, float(clean)])
+        Ts.append(T)
+        Ls.append(locked)
+        Es.append(E)
+        R.append(rows)
+    np.savez_compressed(HERE / "energy_sweeps_ref.npz", T=np.stack(Ts), locked=np.stack(Ls),
+                        E=np.stack(Es), sigmas=np.asarray(SWEEP_SIGMAS), thres=np.asarray(SWEEP_THRES),
+                        results=np.asarray(R))
+
+
 def main(names=None):
     rng = np.random.default_rng(2024)
     ref = RefLib()
     if names:
         if "nearest_ref" in names:
             make_nearest(ref)
+        if "energy_sweeps_ref" in names:
+            make_sweeps(ref)
         return
     make_nearest(ref)
+    make_sweeps(ref)
 
     T = amips_cases(rng)
     E, J, H = ref.amips_batch_soa(T.T.copy())

@@ -428,6 +428,30 @@ def test_energy_sweeps_match_reference_live(oracle, reflib, sigma):
     assert len(seen) >= 2
 
 
+def test_energy_sweeps_match_reference_golden(oracle):
+    """getAvgMaxEnergy / getMaxEnergy / getSecondMaxEnergy / getFilterEnergy
+    (LocalOperations.cpp:605-693): the oracle's one-pass sweep against the reference's
+    results stored in energy_sweeps_ref.npz, bit for bit, over the filter branches the
+    fixture's thresholds reach (inverted tets at the 1e50 sentinel, locked tets skipped)."""
+    g = golden("energy_sweeps_ref.npz")
+    n = g["T"].shape[2]
+    tets = np.arange(4 * n, dtype=np.int32).reshape(n, 4)
+    branches = set()
+    for c in range(len(g["sigmas"])):
+        T = g["T"][c]
+        # the sweep input the reference ran over
+        E = oracle.amips_batch_soa(T, quality=True, jacobian=False, hessian=False)[0]
+        assert np.array_equal(E, g["E"][c])
+        xyz = T.reshape(4, 3, n).transpose(2, 0, 1).reshape(-1, 3)
+        for k, thres in enumerate(g["thres"]):
+            a, m, m2, buckets = oracle.energy_stats(xyz, tets, g["locked"][c], float(thres))
+            f, clean = oracle.filter_energy(buckets, float(thres))
+            ra, rm, rm2, rf, rclean = g["results"][c, k]
+            assert (a, m, m2, f, clean) == (ra, rm, rm2, rf, bool(rclean))
+            branches.add((rf, bool(rclean)))
+    assert len(branches) >= 3
+
+
 def _dihedral_numpy(t):
     """Independent dihedral angles of one tet: pi minus the angle between the outward
     normals of the two faces meeting at each edge."""
