@@ -316,7 +316,7 @@ TW_API double tw_filter_energy(const int64_t* buckets, double filter_energy_thre
  * max angle, mean max angle} in radians, the means from double-double sums;
  * counts = {min angle < 6, < 12, < 18 degrees, max angle > 162, > 168,
  * > 174 degrees, tets counted}.  min_angle / max_angle (may be NULL): each
- * tet's (min_d_angle, max_d_angle).  Angles use CUDA's acos (within 2 ulp of
+ * tet's (min_d_angle, max_d_angle).  Angles use CUDA's acos (within 4 ulp of
  * the host's).                                                             */
 TW_API int tw_dihedral_stats(tw_ctx* ctx, const int32_t* tets, int64_t n, const uint8_t* locked,
                              double* out, int64_t* counts, double* min_angle, double* max_angle);
