@@ -99,3 +99,61 @@ def test_filter_energy_rule_matches_oracle(oracle):
             c = ctypes.c_int()
             e = lib.tw_filter_energy(b.ctypes.data, thres, ctypes.byref(c))
             assert (e, bool(c.value)) == oracle.filter_energy(b, thres)
+
+
+def _header_signatures():
+    """{name: (return kind, [parameter kinds])} from the TW_API declarations; a kind is
+    'p' (pointer), 'f8' (double), 'f4' (float) or 'iN' (an integer of N bytes)."""
+    text = re.sub(r"/\*.*?\*/", " ", HEADER.read_text(), flags=re.S)
+    ints = {"int": 4, "int32_t": 4, "uint32_t": 4, "int64_t": 8, "uint64_t": 8, "size_t": 8,
+            "uint8_t": 1, "char": 1}
+
+    def kind(decl):
+        decl = decl.strip()
+        if "*" in decl:
+            return "p"
+        words = [w for w in re.findall(r"\w+", decl) if w not in ("const", "unsigned")]
+        if words[0] == "double":
+            return "f8"
+        if words[0] == "float":
+            return "f4"
+        return f"i{ints[words[0]]}"
+
+    sigs = {}
+    for m in re.finditer(r"^TW_API\s+([^(]*?)\s*\b(tw_\w+)\s*\(([^)]*)\)\s*;", text, re.M):
+        ret, name, params = m.groups()
+        ps = [q for q in params.split(",") if q.strip() and q.strip() != "void"]
+        sigs[name] = ("p" if "*" in ret else kind(ret), [kind(q) for q in ps])
+    return sigs
+
+
+def _ctypes_kind(t):
+    if t is ctypes.c_void_p or t is ctypes.c_char_p or hasattr(t, "_type_") and \
+            isinstance(getattr(t, "_type_"), type):
+        return "p"
+    if t in (ctypes.c_double,):
+        return "f8"
+    if t in (ctypes.c_float,):
+        return "f4"
+    return f"i{ctypes.sizeof(t)}"
+
+
+def test_python_signatures_match_header():
+    """Every ctypes argument list (and return type) in the Python binding has the
+    parameter count, pointer-ness and integer/float widths of the header's
+    declaration, so no call passes a 4-byte int where the C side reads 8 bytes."""
+    import tetwild_gb300 as tw
+
+    sigs = _header_signatures()
+    assert sorted(sigs) == declared_symbols()
+    bad = []
+    for name, args in tw._SIGS.items():
+        ret, params = sigs[name]
+        got = [_ctypes_kind(a) for a in args]
+        if got != params:
+            bad.append((name, got, params))
+        want_ret = ("p" if name.endswith("last_error") else
+                    "f8" if name == "tw_filter_energy" else "i4")
+        if ret != want_ret:
+            bad.append((name, "return", ret, want_ret))
+    assert not bad, bad
