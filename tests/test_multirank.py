@@ -48,3 +48,18 @@ def test_two_ranks_barrier_and_max_over_ranks():
         assert p.exitcode == 0
     assert [r[1] for r in res] == [(2, 0, 0), (2, 1, 1)]
     assert all(r[2] == 11.0 for r in res)
+
+
+@pytest.mark.timeout(120)
+def test_reference_arm_runs_on_rank_zero_only():
+    """Under torchrun the reference arm's rank 0 alone times the CPU code and prints the line;
+    every other rank exits 0 at once without work or output."""
+    import subprocess
+
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2",
+               MASTER_ADDR="127.0.0.1", MASTER_PORT=str(_free_port()))
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--gpus",
+                        "2", "--steps", "1", "--warmup", "0"], env=env, cwd=str(ROOT),
+                       capture_output=True, text=True, timeout=100)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip() == ""
