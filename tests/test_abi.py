@@ -157,3 +157,26 @@ def test_python_signatures_match_header():
         if ret != want_ret:
             bad.append((name, "return", ret, want_ret))
     assert not bad, bad
+
+
+@pytest.mark.parametrize("compiler,std,ext", [("gcc", "-std=c99", "c"), ("g++", "-std=c++17", "cpp")])
+def test_header_compiles_for_c_and_cpp_hosts(tmp_path, compiler, std, ext):
+    """The header is valid C99 and C++17 on its own (a C, C++ or cgo host includes it as
+    is), and every declared symbol is a function with C linkage of that name."""
+    import shutil
+
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not installed")
+    syms = declared_symbols()
+    src = tmp_path / f"use_header.{ext}"
+    src.write_text('#include "tw_gb300.h"\n'
+                   "typedef void (*fn)(void);\n"
+                   "fn const table[] = {\n" +
+                   "".join(f"    (fn)&{s},\n" for s in syms) + "};\n")
+    r = subprocess.run([compiler, std, "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-I", str(HEADER.parent), "-c", str(src), "-o", str(tmp_path / "u.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run(["nm", "-u", str(tmp_path / "u.o")], capture_output=True, text=True,
+                         check=True).stdout
+    assert sorted(l.split()[-1] for l in out.splitlines() if "tw_" in l) == syms
