@@ -8,7 +8,7 @@
  * VertexSmoother, switched at compile time between the scalar code and the
  * ISPC kernel (TETWILD_WITH_ISPC, LocalOperations.h:21-23).  Each entry point
  * below names the reference routine it replaces; a TetWild build binds them
- * behind the same switch.
+ * behind a switch of the same kind (TETWILD_WITH_GB300).
  *
  * Conventions
  *  - Every call returns an int status: TW_OK (0), a negative error code, or
@@ -21,8 +21,11 @@
  *  - A context belongs to one device and one stream; distinct contexts may be
  *    used from distinct threads.
  *  - Coordinates are binary64.  Decisions (signs, in/out, accept/reject) are
- *    exact or bit-identical to the CPU oracle; energies, gradients and
- *    Hessians agree with the reference expressions to 1e-12 relative.
+ *    exact or bit-identical to the CPU oracle.  In the default energy form
+ *    (TW_ENERGY_FORM_REFERENCE) the binary64 energies, gradients and Hessians
+ *    perform the reference routines' own operations in their order, so they
+ *    agree with the reference's results to its rounding (within 1e-12
+ *    relative; a few ulp in practice, the only difference being pow).
  */
 #ifndef TW_GB300_H
 #define TW_GB300_H
@@ -61,6 +64,14 @@ extern "C" {
                                           binary64 recomputation inside the band:
                                           decisions identical to TW_PRECISION_FP64 */
 
+/* energy forms of the binary64 AMIPS evaluations (tw_set_energy_form) */
+#define TW_ENERGY_FORM_REFERENCE 0  /* the reference's generated operations, in its
+                                       order and with its 15-digit coefficients
+                                       (default: agrees with the reference)   */
+#define TW_ENERGY_FORM_CLOSED 1     /* closed form of the same function: within a
+                                       few ulp of the exact value, ~3x fewer
+                                       binary64 operations                     */
+
 /* surfaces */
 #define TW_SURFACE_INPUT 0       /* geo_sf_tree (MeshRefinement.cpp:209)      */
 #define TW_SURFACE_BOUNDARY 1    /* geo_b_tree  (MeshRefinement.cpp:213)      */
@@ -90,6 +101,12 @@ TW_API int tw_memory_used(const tw_ctx* ctx, size_t* bytes);
  * exceed eps; AMIPS: tets whose certified relative error bound exceeds
  * 1e-5), so every decision equals the binary64 one.                         */
 TW_API int tw_set_precision(tw_ctx* ctx, int mode);
+/* Energy form of every binary64 AMIPS evaluation of the context (the batch
+ * calls, tet qualities, energy sweeps, Newton steps, smoothing passes and
+ * collapse checks): TW_ENERGY_FORM_REFERENCE (default) or
+ * TW_ENERGY_FORM_CLOSED.  No counterpart in the reference, whose expressions
+ * are the reference form (LocalOperations.cpp:28-291).                      */
+TW_API int tw_set_energy_form(tw_ctx* ctx, int form);
 typedef struct tw_stats {
     uint64_t exact_orientations;   /* orientation signs that needed the exact path */
     uint64_t env_queries;          /* envelope points and face samples queried      */
@@ -121,9 +138,10 @@ TW_API int tw_amips_soa_device(tw_ctx* ctx, const double* T, int64_t n, int mode
  * entry point for callers that cannot let a library allocate device memory,
  * such as a host program whose allocator reserves all free HBM at start-up,
  * or one that must not stall its other streams on the device-wide
- * synchronisation of cudaFree.  Same inputs, outputs and results as
- * tw_amips_soa, for at most TW_NOALLOC_MAX_TETS tets per call (larger n
- * returns TW_ERR_TOO_LARGE); needs no context.  It calls no cudaMalloc or
+ * synchronisation of cudaFree.  Same inputs and outputs as tw_amips_soa, and
+ * the same results as tw_amips_soa on a context in TW_PRECISION_FP64 with the
+ * default energy form, for at most TW_NOALLOC_MAX_TETS tets per call (larger
+ * n returns TW_ERR_TOO_LARGE); needs no context.  It calls no cudaMalloc or
  * cudaFree: its scratch is a fixed device array of TW_NOALLOC_SCRATCH_BYTES
  * that every GPU loading this library holds until the process exits.  The
  * first call on a device looks up that array's address (make it before any

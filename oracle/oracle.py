@@ -15,6 +15,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "libtw_oracle.so"
+# the same source built with TW_RF_LIBM: the reference-form AMIPS routines take
+# libm's pow as the reference does (the bit-for-bit pin against oracle/_ref)
+ORACLE_LIBM_SO = HERE / "libtw_oracle_libm.so"
 REF_SO = HERE / "_ref" / "libtwref.so"
 
 _P = ctypes.c_void_p
@@ -58,14 +61,22 @@ def default_threads() -> int:
 
 
 class Oracle:
-    """The CPU restatement (oracle/tw_oracle.c)."""
+    """The CPU restatement (oracle/tw_oracle.c); libm=True loads its libm-pow
+    build (libtw_oracle_libm.so)."""
 
-    def __init__(self):
-        if not ORACLE_SO.exists():
+    def __init__(self, libm: bool = False):
+        so = ORACLE_LIBM_SO if libm else ORACLE_SO
+        if not so.exists():
             build_oracle()
-        L = ctypes.CDLL(str(ORACLE_SO))
+        L = ctypes.CDLL(str(so))
         sig = {
             "two_icbrt": ([_D], _D),
+            "two_set_energy_form": ([_I], None),
+            "two_get_energy_form": ([], _I),
+            "two_rf_pow_m13": ([_D], _D),
+            "two_amips_energy_rf": ([_P], _D),
+            "two_amips_jacobian_rf": ([_P, _P], None),
+            "two_amips_hessian_rf": ([_P, _P], None),
             "two_amips_energy": ([_P], _D),
             "two_amips_jacobian": ([_P, _P], None),
             "two_amips_hessian": ([_P, _P], None),
@@ -110,6 +121,13 @@ class Oracle:
     # scalar helpers
     def icbrt(self, x: float) -> float:
         return self.L.two_icbrt(x)
+
+    def set_energy_form(self, form: int):
+        """0: reference form (default), 1: closed form; process-wide."""
+        self.L.two_set_energy_form(form)
+
+    def energy_form(self) -> int:
+        return self.L.two_get_energy_form()
 
     def orient3d(self, p, q, r, s) -> int:
         a = [_c(v, np.float64) for v in (p, q, r, s)]

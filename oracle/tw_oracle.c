@@ -92,7 +92,10 @@ double two_icbrt(double x)
  * r = (D^2)^(-1/3):
  *   J = r (gN - (2/3)(N/D) g)
  *   H = 3 r I - (2/3)(r/D)(gN g^T + g gN^T) + (10/9)(N r/D^2) g g^T.
- * Agreement with the generated expressions: 1e-12 relative (tested).
+ * This closed form is the accurate one (within a few ulp of the exact
+ * function); the reference form below is the one that agrees with the
+ * reference's own rounding.  two_set_energy_form selects which one the
+ * unsuffixed routines (and every caller in this file) use.
  * ========================================================================= */
 #define TW_ISQ3 0.57735026918962576451   /* 1/sqrt(3) */
 #define TW_ISQ6 0.40824829046386301637   /* 1/sqrt(6) */
@@ -119,7 +122,7 @@ static inline void tw_cross(const double u[3], const double v[3], double w[3])
     w[2] = u[0] * v[1] - u[1] * v[0];
 }
 
-double two_amips_energy(const double T[12])
+double two_amips_energy_cf(const double T[12])
 {
     double a[3], b[3], c[3], bc[3];
     tw_frame(T, a, b, c);
@@ -149,7 +152,7 @@ static void tw_amips_grad_terms(const double* T, double* N_, double* D_, double*
     *r_ = two_icbrt(D * D);
 }
 
-void two_amips_jacobian(const double T[12], double J[3])
+void two_amips_jacobian_cf(const double T[12], double J[3])
 {
     double N, D, r, g[3], gN[3];
     tw_amips_grad_terms(T, &N, &D, &r, g, gN);
@@ -158,7 +161,7 @@ void two_amips_jacobian(const double T[12], double J[3])
     for (int k = 0; k < 3; ++k) J[k] = r * (gN[k] - t * g[k]);
 }
 
-void two_amips_hessian(const double T[12], double H[9])
+void two_amips_hessian_cf(const double T[12], double H[9])
 {
     double N, D, r, g[3], gN[3];
     tw_amips_grad_terms(T, &N, &D, &r, g, gN);
@@ -171,6 +174,235 @@ void two_amips_hessian(const double T[12], double H[9])
             double base = (i == j) ? r3 : 0.0;
             H[i * 3 + j] = (base - s1 * (gN[i] * g[j] + g[i] * gN[j])) + s2 * (g[i] * g[j]);
         }
+}
+
+/* =========================================================================
+ * Reference form of the AMIPS energy, gradient and Hessian.
+ *
+ * LocalOperations.cpp:28-81, :83-147 and :149-291 evaluate machine-generated
+ * expressions on the absolute coordinates with 15-digit coefficients.  For a
+ * small tet away from the origin their terms cancel by up to ~1e4, so the
+ * reference's result carries rounding of up to ~5e-12 relative; agreeing
+ * with it to 1e-12 takes the same IEEE operations in the same order.  The
+ * routines below perform them: each sum and product is grouped as the
+ * generated code groups it (left to right), with its coefficients (RF_*).
+ * IEEE addition and multiplication are commutative and negation is exact, so
+ * the operand order inside one operation and the placement of signs are free;
+ * only the grouping is kept.  Names: x0..z3 the coordinates of vertices 0..3;
+ * bx, by, bz and cx, cy, cz the two scaled frame rows, each routine grouping
+ * them as its generated code does; Lx0..Lz3 the per-coordinate linear forms
+ * of the numerator.
+ *
+ * pow(d, 2) is d*d (pow is exact to the rounding of d*d), and
+ * pow(s, -0.333333333333333) is rf_pow_m13: s^(-1/3) (two_icbrt) times
+ * s^RF_DELTA, RF_DELTA = -0.333333333333333 + 1/3 = 3.5157e-16, applied as
+ * the first-order factor 1 + RF_DELTA ln s (a correction below 2.6e-13 over
+ * the double range; ln s to ~4% keeps its own error below 1e-17 relative).
+ * Built with -DTW_RF_LIBM the two powers are libm's, which makes the three
+ * routines bit-identical to the reference's own (a CPU test checks it).
+ * ========================================================================= */
+#define RF_B1   0.577350269189626      /* 1/sqrt3, as the generated code spells it */
+#define RF_B2   1.15470053837925       /* 2/sqrt3 (not 2*RF_B1) */
+#define RF_C1   0.408248290463863      /* 1/sqrt6 */
+#define RF_C3   1.22474487139159       /* 3/sqrt6 */
+#define RF_S2   0.707106781186548      /* 1/sqrt2 */
+#define RF_2_3  0.666666666666667
+#define RF_4_3  1.33333333333333
+#define RF_4_9  0.444444444444444
+#define RF_10_9 1.11111111111111
+#define RF_TINY 1.85037170770859e-17   /* code-generation residue, kept (:267) */
+#define RF_EXP  -0.333333333333333
+#define RF_DELTA 3.515706244646329e-16 /* RF_EXP + 1/3 */
+#define RF_LN2  0.6931471805599453
+
+#ifdef TW_RF_LIBM
+#define RF_SQ(d) pow((d), 2)
+#define RF_POW_M13(s) pow((s), RF_EXP)
+#else
+#define RF_SQ(d) ((d) * (d))
+#define RF_POW_M13(s) two_rf_pow_m13(s)
+#endif
+
+double two_rf_pow_m13(double s)
+{
+    double r = two_icbrt(s);
+    if (!(r > 0.0) || r == INFINITY) return r;   /* NaN, s = inf, s = 0 */
+    uint64_t u = tw_bits(s);
+    int e = (int)((u >> 52) & 0x7ff);
+    double m = tw_from_bits((u & 0x000fffffffffffffULL) | (1023ULL << 52));   /* [1, 2) */
+    double ln = (double)(e - 1023) * RF_LN2 + (2.0 * (m - 1.0)) / (m + 1.0);
+    return r + r * (RF_DELTA * ln);
+}
+
+double two_amips_energy_rf(const double T[12])
+{
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double bx = (RF_B1 * x0 - RF_B2 * x1) + RF_B1 * x3;
+    const double cy = ((RF_C1 * y3 + RF_C1 * y0) + RF_C1 * y1) - RF_C3 * y2;
+    const double by = (RF_B1 * y3 + RF_B1 * y0) - RF_B2 * y1;
+    const double cx = ((RF_C1 * x0 - RF_C3 * x2) + RF_C1 * x1) + RF_C1 * x3;
+    const double cz = ((RF_C1 * z0 + RF_C1 * z1) - RF_C3 * z2) + RF_C1 * z3;
+    const double bz = (RF_B1 * z0 - RF_B2 * z1) + RF_B1 * z3;
+    const double hx = 0.5 * x2 + 0.5 * x1, hy = 0.5 * y1 + 0.5 * y2, hz = 0.5 * z1 + 0.5 * z2;
+    const double num =
+        z0 * ((0.5 * z3 - 1.5 * z0) + hz) + y3 * ((hy - 1.5 * y3) + 0.5 * y0) +
+        x2 * (((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3) +
+        z1 * (((0.5 * z0 - 1.5 * z1) + 0.5 * z2) + 0.5 * z3) +
+        z2 * (((0.5 * z0 + 0.5 * z1) - 1.5 * z2) + 0.5 * z3) + z3 * ((0.5 * z0 - 1.5 * z3) + hz) +
+        x0 * ((hx - 1.5 * x0) + 0.5 * x3) + x1 * (((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3) +
+        x3 * ((hx + 0.5 * x0) - 1.5 * x3) + y0 * ((0.5 * y3 + hy) - 1.5 * y0) +
+        y1 * (((0.5 * y3 + 0.5 * y0) - 1.5 * y1) + 0.5 * y2) +
+        y2 * (((0.5 * y3 + 0.5 * y0) + 0.5 * y1) - 1.5 * y2);
+    const double det = ((z0 - z3) * (cy * bx - by * cx) - (y0 - y3) * (cz * bx - cx * bz)) +
+                       (x0 - x3) * (by * cz - cy * bz);
+    return -num * RF_POW_M13(RF_SQ(det));
+}
+
+void two_amips_jacobian_rf(const double T[12], double J[3])
+{
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double dy = y0 - y3, dz = z0 - z3, dx = x0 - x3;
+    const double bx = (RF_B1 * x0 - RF_B2 * x1) + RF_B1 * x3;
+    const double by = (RF_B1 * y0 - RF_B2 * y1) + RF_B1 * y3;
+    const double bz = (RF_B1 * z0 - RF_B2 * z1) + RF_B1 * z3;
+    const double cx = ((RF_C1 * x0 - RF_C3 * x2) + RF_C1 * x1) + RF_C1 * x3;
+    const double cy = ((RF_C1 * y0 + RF_C1 * y1) - RF_C3 * y2) + RF_C1 * y3;
+    const double cz = ((RF_C1 * z1 - RF_C3 * z2) + RF_C1 * z3) + RF_C1 * z0;
+    const double czbx = cz * bx - bz * cx;
+    const double cybx = cy * bx, cxby = cx * by;
+    const double det = (czbx * dy - dz * (cybx - cxby)) - dx * (cz * by - bz * cy);
+    const double r = RF_POW_M13(RF_SQ(det));
+    const double sz = RF_S2 * z1 - RF_S2 * z2, sy = RF_S2 * y1 - RF_S2 * y2;
+    const double sx = RF_S2 * x1 - RF_S2 * x2;
+    const double hx = 0.5 * x2 + 0.5 * x1, hy = 0.5 * y1 + 0.5 * y2, hz = 0.5 * z1 + 0.5 * z2;
+    const double num =
+        y0 * ((0.5 * y3 - 1.5 * y0) + hy) + z1 * (((0.5 * z2 - 1.5 * z1) + 0.5 * z3) + 0.5 * z0) +
+        z2 * (((0.5 * z1 - 1.5 * z2) + 0.5 * z3) + 0.5 * z0) + z3 * ((hz - 1.5 * z3) + 0.5 * z0) +
+        y3 * ((0.5 * y0 - 1.5 * y3) + hy) + x2 * (((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3) +
+        y1 * (((0.5 * y0 + 0.5 * y3) - 1.5 * y1) + 0.5 * y2) +
+        y2 * (((0.5 * y0 + 0.5 * y3) + 0.5 * y1) - 1.5 * y2) + x0 * ((hx - 1.5 * x0) + 0.5 * x3) +
+        x1 * (((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3) + x3 * ((0.5 * x0 + hx) - 1.5 * x3) +
+        z0 * ((0.5 * z3 + hz) - 1.5 * z0);
+    const double w = (RF_2_3 * num) / det;
+    const double q0 = ((sz * (y3 - y0) - sy * (z3 - z0)) - bz * cy) + by * cz;
+    J[0] = -(r * ((((x2 - 3.0 * x0) + w * q0) + x1) + x3));
+    J[1] = r * ((((3.0 * y0 - y3) - y1) - y2) + w * ((czbx + dz * sx) - dx * sz));
+    J[2] = r * (((((-z1) - z2) - z3) + w * (((-(dy * sx)) - cybx) + cxby + dx * sy)) + 3.0 * z0);
+}
+
+void two_amips_hessian_rf(const double T[12], double H[9])
+{
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double dz = z0 - z3, dx = x0 - x3, dy = y0 - y3;
+    const double bx = (RF_B1 * x0 - RF_B2 * x1) + RF_B1 * x3;
+    const double by = (RF_B1 * y0 - RF_B2 * y1) + RF_B1 * y3;
+    const double bz = (RF_B1 * z0 - RF_B2 * z1) + RF_B1 * z3;
+    const double cx = ((RF_C1 * x0 + RF_C1 * x1) - RF_C3 * x2) + RF_C1 * x3;
+    const double cy = ((RF_C1 * y0 + RF_C1 * y1) - RF_C3 * y2) + RF_C1 * y3;
+    const double cz = ((RF_C1 * z0 + RF_C1 * z1) - RF_C3 * z2) + RF_C1 * z3;
+    const double bxcy = bx * cy, bycx = by * cx;
+    const double mx = dz * (bxcy - bycx);
+    const double bycz = by * cz, cybz = cy * bz;
+    const double myz = bycz - cybz;
+    const double my = dx * myz;
+    const double bxcz = bx * cz, cxbz = cx * bz;
+    const double mxz = bxcz - cxbz;
+    const double mz = dy * mxz;
+    const double det = (mx + my) - mz;
+    const double det2 = RF_SQ(det);
+    const double r = RF_POW_M13(det2);
+    const double lx = ((x2 - 3.0 * x0) + x1) + x3;
+    const double sy = RF_S2 * y1 - RF_S2 * y2;
+    const double dzsy = dz * sy;
+    const double sz = RF_S2 * z1 - RF_S2 * z2;
+    const double dysz = dy * sz;
+    const double u = (myz + dzsy) - dysz;
+    const double k43 = RF_4_3 / det;
+    const double idet2 = 1.0 / det2;
+    const double hx = 0.5 * x2 + 0.5 * x1;
+    const double Lx0 = (hx - 1.5 * x0) + 0.5 * x3;
+    const double Lx3 = (0.5 * x0 + hx) - 1.5 * x3;
+    const double Lx2 = ((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3;
+    const double Lx1 = ((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3;
+    const double hy = 0.5 * y1 + 0.5 * y2;
+    const double Ly0 = (0.5 * y3 - 1.5 * y0) + hy;
+    const double Ly3 = (0.5 * y0 - 1.5 * y3) + hy;
+    const double Ly2 = ((0.5 * y0 + 0.5 * y1) - 1.5 * y2) + 0.5 * y3;
+    const double Ly1 = ((0.5 * y0 - 1.5 * y1) + 0.5 * y2) + 0.5 * y3;
+    const double hz = 0.5 * z1 + 0.5 * z2;
+    const double Lz0 = (0.5 * z3 - 1.5 * z0) + hz;
+    const double Lz3 = (0.5 * z0 - 1.5 * z3) + hz;
+    const double Lz2 = ((0.5 * z0 + 0.5 * z3) + 0.5 * z1) - 1.5 * z2;
+    const double Lz1 = ((0.5 * z0 + 0.5 * z3) - 1.5 * z1) + 0.5 * z2;
+    const double num = z0 * Lz0 + y0 * Ly0 + y1 * Ly1 + y2 * Ly2 + y3 * Ly3 + z3 * Lz3 +
+                       x2 * Lx2 + z1 * Lz1 + z2 * Lz2 + x0 * Lx0 + x1 * Lx1 + Lx3 * x3;
+    const double k49n = (RF_4_9 * idet2) * num;
+    const double nd = idet2 * num;
+    const double ineg = 1.0 / (-det);
+    const double rneg = ineg * r;
+    const double sx = RF_S2 * x1 - RF_S2 * x2;
+    const double v1 = (((RF_2_3 * bx) * cz + (RF_2_3 * dz) * sx) - (RF_2_3 * cx) * bz) -
+                      (RF_2_3 * dx) * sz;
+    const double ly = ((y1 - 3.0 * y0) + y2) + y3;
+    const double ey = y3 - y0, ez = z3 - z0;
+    const double v2 = (((-RF_2_3 * sy) * ez + (RF_2_3 * sz) * ey) + (RF_2_3 * by) * cz) -
+                      (RF_2_3 * bz) * cy;
+    const double dzsx = dz * sx, dxsz = dx * sz;
+    const double p = (dzsx - dxsz) + mxz;
+    const double q = ((sz * ey - sy * ez) + by * cz) - bz * cy;
+    const double a1 = ((((RF_4_9 * p) * q) * num) * ineg + lx * v1) - ly * v2;
+    const double tiny = (RF_TINY * z0) * Lz0 + (RF_TINY * y0) * Ly0 + (RF_TINY * y1) * Ly1 +
+                        (RF_TINY * y2) * Ly2 + (RF_TINY * y3) * Ly3 + (RF_TINY * z3) * Lz3 +
+                        (RF_TINY * x2) * Lx2 + (RF_TINY * z1) * Lz1 + (RF_TINY * z2) * Lz2 +
+                        (RF_TINY * x0) * Lx0 + (RF_TINY * x1) * Lx1 + (RF_TINY * Lx3) * x3;
+    const double un = (u * num) * ineg;
+    const double v3 = (((RF_2_3 * by) * cx - (RF_2_3 * bx) * cy) + (RF_2_3 * dx) * sy) -
+                      (RF_2_3 * dy) * sx;
+    const double lz = ((z3 - 3.0 * z0) + z1) + z2;
+    const double t = ((bycx - bxcy) + dx * sy) - dy * sx;
+    const double tn = ((RF_4_9 * t) * num) * ineg;
+    const double a2 = (q * tn + v3 * lx) - lz * v2;
+    const double ex = x3 - x0;
+    const double w1 = (num * ineg) * (((ex * sz - sx * ez) + bx * cz) - cx * bz);
+    const double s = ((dxsz - dzsx) - bxcz) + cxbz;
+    const double a3 = ((-p) * tn + v3 * ly) + lz * v1;
+    const double w2 = (num * ineg) * (((ex * (-sy) + sx * ey) - bx * cy) + cx * by);
+    H[0] = r * ((((lx * u) * k43 - RF_SQ(u) * k49n) + ((RF_2_3 * u) * nd) * (((cybz - bycz) - dzsy) + dysz)) + 3.0);
+    H[1] = rneg * ((a1 - tiny * z1) + un * v1);
+    H[2] = rneg * (un * v3 + a2);
+    H[3] = rneg * (a1 + w1 * v2);
+    H[4] = r * ((((-RF_SQ(s)) * k49n + (s * k43) * ly) + (s * nd) * v1) + 3.0);
+    H[5] = rneg * (((-tiny) * x1 - v3 * w1) + a3);
+    H[6] = rneg * (((-tiny) * y1 + a2) + w2 * v2);
+    H[7] = rneg * (a3 - w2 * v1);
+    H[8] = r * ((((-lz) * t) * k43 - (RF_10_9 * RF_SQ(t)) * nd) + 3.0);
+}
+
+static int tw_energy_form = TWO_FORM_REFERENCE;
+
+void two_set_energy_form(int form) { tw_energy_form = form; }
+int two_get_energy_form(void) { return tw_energy_form; }
+
+double two_amips_energy(const double T[12])
+{
+    return tw_energy_form == TWO_FORM_CLOSED ? two_amips_energy_cf(T) : two_amips_energy_rf(T);
+}
+void two_amips_jacobian(const double T[12], double J[3])
+{
+    if (tw_energy_form == TWO_FORM_CLOSED)
+        two_amips_jacobian_cf(T, J);
+    else
+        two_amips_jacobian_rf(T, J);
+}
+void two_amips_hessian(const double T[12], double H[9])
+{
+    if (tw_energy_form == TWO_FORM_CLOSED)
+        two_amips_hessian_cf(T, H);
+    else
+        two_amips_hessian_rf(T, H);
 }
 
 /* =========================================================================

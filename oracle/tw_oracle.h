@@ -30,9 +30,24 @@ extern "C" {
 
 /* ---- AMIPS (LocalOperations.cpp:28-291) ---------------------------------- */
 double two_icbrt(double x);                                   /* x^(-1/3)      */
+/* The unsuffixed routines evaluate the selected form: TWO_FORM_REFERENCE
+ * (default) performs the reference's generated operations in its order and
+ * agrees with it to its rounding; TWO_FORM_CLOSED is the accurate closed
+ * form.  The selection is process-wide; set it before a batch call.         */
+#define TWO_FORM_REFERENCE 0
+#define TWO_FORM_CLOSED 1
+void   two_set_energy_form(int form);
+int    two_get_energy_form(void);
 double two_amips_energy(const double T[12]);                  /* :28-81        */
 void   two_amips_jacobian(const double T[12], double J[3]);   /* :83-147       */
 void   two_amips_hessian(const double T[12], double H[9]);    /* :149-291      */
+double two_amips_energy_rf(const double T[12]);
+void   two_amips_jacobian_rf(const double T[12], double J[3]);
+void   two_amips_hessian_rf(const double T[12], double H[9]);
+double two_amips_energy_cf(const double T[12]);
+void   two_amips_jacobian_cf(const double T[12], double J[3]);
+void   two_amips_hessian_cf(const double T[12], double H[9]);
+double two_rf_pow_m13(double s);                 /* s^-0.333333333333333 */
 
 /* ---- exact predicates (CGAL Epick orientation / collinear) --------------- */
 /* +1 POSITIVE, 0 COPLANAR, -1 NEGATIVE; CGAL convention:

@@ -131,12 +131,12 @@ SWEEP_THRES = (1.0, 3.0, 10.0)
 
 
 def make_sweeps(ref):
-    """The sweeps' input is the oracle's calTetQualities energies (AMIPS energy, or the 1e50
-    sentinel for an inverted tet), stored as E: they agree with the reference's
-    comformalAMIPSEnergy_new to its forward error (amips_ref.npz pins that), not bit for
-    bit, so the reference's sweeps run over exactly these values.  The results are the
-    reference's."""
-    o = Oracle()
+    """The sweeps' input is calTetQualities' energies (AMIPS energy, or the 1e50 sentinel for
+    an inverted tet), stored as E: the oracle's reference form built with libm's pow, which
+    is the reference's comformalAMIPSEnergy_new bit for bit (asserted below), with the
+    oracle's exact orientation for the sentinel.  The results are the reference's sweeps
+    over exactly these values."""
+    o = Oracle(libm=True)
     n = 600
     Ts, Ls, Es, R = [], [], [], []
     for c, sigma in enumerate(SWEEP_SIGMAS):
@@ -148,9 +148,7 @@ def make_sweeps(ref):
         E = o.amips_batch_soa(T, quality=True, jacobian=False, hessian=False)[0]
         Er = ref.amips_batch_soa(T, jacobian=False, hessian=False)[0]
         live = E != 1e50
-        # a loose sanity bound: the per-tet forward-error bound (up to 1.2e-10 relative on
-        # these spreads, for tets of energy near 1e3) is what amips_ref.npz checks
-        assert (np.abs(E[live] / Er[live] - 1.0) < 1e-8).all() and (~live).any()
+        assert np.array_equal(E[live], Er[live]) and (~live).any()
         rows = []
         for thres in SWEEP_THRES:
             a, m, _, m2, f, clean = ref.energy_sweeps(E, None, locked, thres)

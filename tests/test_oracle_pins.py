@@ -40,26 +40,60 @@ def test_icbrt_special_values(oracle):
 
 
 # ---------------------------------------------------------------- AMIPS ----
+# Two energy forms (two_set_energy_form): the reference form, the default,
+# performs the reference's generated operations (LocalOperations.cpp:28-291)
+# in its order and agrees with it to its rounding; the closed form evaluates
+# the same function accurately.  Tolerance of the reference form against the
+# reference's own routines: 1e-12 relative per entry of E, J and H.
+REL_TOL = 1e-12
+FORM_REFERENCE, FORM_CLOSED = 0, 1
+
+
 def _aos_to_soa(T):
     return np.ascontiguousarray(np.asarray(T).T)
 
 
+@pytest.fixture
+def closed_form(oracle):
+    oracle.set_energy_form(FORM_CLOSED)
+    yield oracle
+    oracle.set_energy_form(FORM_REFERENCE)
+
+
+def test_default_form_is_reference(oracle):
+    assert oracle.energy_form() == FORM_REFERENCE
+
+
+def _within(a, b, tol):
+    """Entry-wise |a - b| <= tol |b| (a zero reference entry must be matched exactly)."""
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b) <= tol * np.abs(b)
+
+
 def test_amips_known_answers(oracle):
-    t = (syn.REGULAR_TET * 0.37 + np.array([3.0, -2.0, 5.0])).reshape(12)
-    E, J, H, F = oracle.amips_batch_soa(_aos_to_soa([t]), quality=False)
-    assert abs(E[0] - 3.0) < 1e-14
-    assert np.abs(J[:, 0]).max() < 1e-12 / 0.37
-    # at the minimum the Hessian is symmetric positive definite
-    Hm = H[:, 0].reshape(3, 3)
-    assert np.array_equal(Hm, Hm.T)
-    assert np.linalg.eigvalsh(Hm).min() > 0
-    # either orientation gives 3 (README: range 3..inf)
-    t2 = t.reshape(4, 3)[[0, 2, 1, 3]].reshape(12)
-    E2, _, _, F2 = oracle.amips_batch_soa(_aos_to_soa([t2]), quality=False)
-    assert abs(E2[0] - 3.0) < 1e-14 and F2[0] == 1 and F[0] == 0
+    for form, tol in ((FORM_CLOSED, 1e-14), (FORM_REFERENCE, REL_TOL)):
+        oracle.set_energy_form(form)
+        try:
+            t = (syn.REGULAR_TET * 0.37 + np.array([3.0, -2.0, 5.0])).reshape(12)
+            E, J, H, F = oracle.amips_batch_soa(_aos_to_soa([t]), quality=False)
+            assert abs(E[0] - 3.0) < 3.0 * tol
+            assert np.abs(J[:, 0]).max() < 1e-10 / 0.37
+            # at the minimum the Hessian is symmetric positive definite (exactly
+            # symmetric in the closed form; the generated expressions of H[1] and
+            # H[3] round differently)
+            Hm = H[:, 0].reshape(3, 3)
+            assert np.all(_within(Hm, Hm.T, tol) | (np.abs(Hm - Hm.T) < tol * np.abs(Hm).max()))
+            assert np.linalg.eigvalsh((Hm + Hm.T) / 2).min() > 0
+            # either orientation gives 3 (README: range 3..inf)
+            t2 = t.reshape(4, 3)[[0, 2, 1, 3]].reshape(12)
+            E2, _, _, F2 = oracle.amips_batch_soa(_aos_to_soa([t2]), quality=False)
+            assert abs(E2[0] - 3.0) < 3.0 * tol and F2[0] == 1 and F[0] == 0
+        finally:
+            oracle.set_energy_form(FORM_REFERENCE)
 
 
-def test_amips_invariances(oracle):
+def test_amips_invariances(closed_form):
+    oracle = closed_form
     T = syn.energy_batch(2000, seed=3).T
     E0 = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)[0]
     Ts = T * 7.5
@@ -71,31 +105,96 @@ def test_amips_invariances(oracle):
     assert np.all(E0 >= 3.0 - 1e-12)
 
 
-def test_amips_derivatives_match_finite_differences(oracle):
-    T = syn.energy_batch(50, seed=4).T
-    E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)
-    h = 1e-7
-    for i in range(0, 50, 7):
-        for k in range(3):
-            tp, tm = T[i].copy(), T[i].copy()
-            tp[k] += h
-            tm[k] -= h
-            Ep, Jp, _, _ = oracle.amips_batch_soa(_aos_to_soa([tp]), quality=False)
-            Em, Jm, _, _ = oracle.amips_batch_soa(_aos_to_soa([tm]), quality=False)
-            fd = (Ep[0] - Em[0]) / (2 * h)
-            assert abs(fd - J[k, i]) < 1e-5 * max(1.0, abs(E[i]) / 0.01)
-            fdH = (Jp[:, 0] - Jm[:, 0]) / (2 * h)
-            Hrow = H[:, i].reshape(3, 3)[:, k]
-            assert np.max(np.abs(fdH - Hrow)) < 1e-4 * np.max(np.abs(Hrow))
+@pytest.mark.parametrize("form", [FORM_REFERENCE, FORM_CLOSED])
+def test_amips_derivatives_match_finite_differences(oracle, form):
+    oracle.set_energy_form(form)
+    try:
+        T = syn.energy_batch(50, seed=4).T
+        E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)
+        h = 1e-7
+        for i in range(0, 50, 7):
+            for k in range(3):
+                tp, tm = T[i].copy(), T[i].copy()
+                tp[k] += h
+                tm[k] -= h
+                Ep, Jp, _, _ = oracle.amips_batch_soa(_aos_to_soa([tp]), quality=False)
+                Em, Jm, _, _ = oracle.amips_batch_soa(_aos_to_soa([tm]), quality=False)
+                fd = (Ep[0] - Em[0]) / (2 * h)
+                assert abs(fd - J[k, i]) < 1e-5 * max(1.0, abs(E[i]) / 0.01)
+                fdH = (Jp[:, 0] - Jm[:, 0]) / (2 * h)
+                Hrow = H[:, i].reshape(3, 3)[:, k]
+                assert np.max(np.abs(fdH - Hrow)) < 1e-4 * np.max(np.abs(Hrow))
+    finally:
+        oracle.set_energy_form(FORM_REFERENCE)
 
 
-def _amips_tolerances(T):
-    """Reference-vs-restatement tolerance per tet.  The reference's generated
-    expressions round their coefficients to 15 digits (e.g. 1.15470053837925 is
-    not 2 * 0.577350269189626), which makes them depend on the absolute position
-    of the tet: an error of about 2e-15 * |x| / edge on each row of the map,
-    amplified by the conditioning edge^3 / |det| of the map.  The bound is
-    1e-12 relative for tets at the origin, growing with |x|/edge * conditioning."""
+def _amips_cases_live():
+    """The energy-batch distribution (regular tets of edge 0.01 in the unit
+    cube, vertices perturbed by 0.1 edge) and a near-flat batch."""
+    return np.hstack([syn.energy_batch(20000, seed=21),
+                      syn.energy_batch(3000, seed=22, sigma_rel=0.35)])
+
+
+def test_amips_reference_form_libm_bit_exact_golden():
+    """With libm's pow (the TW_RF_LIBM build) the reference form performs
+    exactly the reference's operations: bit-identical E, J and H on every
+    fixture tet (the fixtures were made by the reference's own routines)."""
+    from oracle.oracle import Oracle
+
+    o = Oracle(libm=True)
+    g = golden("amips_ref.npz")
+    E, J, H, _ = o.amips_batch_soa(_aos_to_soa(g["T"]), quality=False)
+    assert np.array_equal(E, g["E"])
+    assert np.array_equal(J.T, g["J"])
+    assert np.array_equal(H.T, g["H"])
+
+
+def test_amips_reference_form_libm_bit_exact_live(reflib):
+    from oracle.oracle import Oracle
+
+    o = Oracle(libm=True)
+    T = _amips_cases_live()
+    Er, Jr, Hr = reflib.amips_batch_soa(T, nthreads=4)
+    E, J, H, _ = o.amips_batch_soa(T, quality=False, nthreads=4)
+    assert np.array_equal(E, Er) and np.array_equal(J, Jr) and np.array_equal(H, Hr)
+
+
+def test_rf_pow_matches_libm(oracle):
+    """rf_pow_m13 (icbrt times the exponent correction) against libm's
+    pow(s, -0.333333333333333) over the double range: a few ulp."""
+    rng = np.random.default_rng(5)
+    xs = 10.0 ** rng.uniform(-300, 300, 20000)
+    got = np.array([oracle.L.two_rf_pow_m13(float(x)) for x in xs])
+    want = np.array([math.pow(float(x), -0.333333333333333) for x in xs])   # libm's pow
+    rel = np.abs(got - want) / want
+    assert rel.max() < 1e-15, rel.max()
+    assert oracle.L.two_rf_pow_m13(0.0) == math.inf and oracle.L.two_rf_pow_m13(math.inf) == 0.0
+
+
+def test_amips_matches_reference_golden(oracle):
+    g = golden("amips_ref.npz")
+    E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(g["T"]), quality=False)
+    assert np.all(_within(E, g["E"], REL_TOL))
+    assert np.all(_within(J.T, g["J"], REL_TOL))
+    assert np.all(_within(H.T, g["H"], REL_TOL))
+
+
+def test_amips_matches_reference_live(oracle, reflib):
+    T = _amips_cases_live()
+    Er, Jr, Hr = reflib.amips_batch_soa(T, nthreads=4)
+    E, J, H, _ = oracle.amips_batch_soa(T, quality=False, nthreads=4)
+    assert np.all(_within(E, Er, REL_TOL)), np.max(np.abs(E - Er) / np.abs(Er))
+    assert np.all(_within(J, Jr, REL_TOL))
+    assert np.all(_within(H, Hr, REL_TOL))
+
+
+def _closed_form_tolerances(T):
+    """Closed form against the reference: the reference's 15-digit
+    coefficients (1.15470053837925 is not 2 * 0.577350269189626) make its
+    result depend on the absolute position of the tet, and its terms on
+    absolute coordinates cancel: an error of about 2e-15 |x| / edge on each
+    row of the map, amplified by the conditioning edge^3 / |det| of the map.
+    1e-12 relative at the origin, growing with |x|/edge * conditioning."""
     P = T.reshape(-1, 4, 3)
     edge = np.linalg.norm(P[:, 0] - P[:, 3], axis=1)
     far = np.abs(P).max(axis=(1, 2)) / np.maximum(edge, 1e-300)
@@ -125,34 +224,41 @@ def _term_scales(T):
     return sJ, sH
 
 
-def test_amips_matches_reference_golden(oracle):
+def test_amips_closed_form_vs_reference(closed_form):
+    oracle = closed_form
     g = golden("amips_ref.npz")
     T = g["T"]
     E, J, H, _ = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)
     ok = np.isfinite(g["E"]) & (g["E"] < 1e8)
-    tol = _amips_tolerances(T)
+    tol = _closed_form_tolerances(T)
     relE = np.abs(E - g["E"]) / np.abs(g["E"])
     assert np.all(relE[ok] <= tol[ok]), relE[ok].max()
-    # J, H: relative to the magnitude of the terms they sum (forward-error scale)
     sJ, sH = _term_scales(T)
     errJ = np.abs(J.T - g["J"]).max(1) / sJ
     errH = np.abs(H.T - g["H"]).max(1) / sH
     assert np.all(errJ[ok] <= 10 * tol[ok]), errJ[ok].max()
     assert np.all(errH[ok] <= 10 * tol[ok]), errH[ok].max()
-    # origin-centred subset (the last 200 tets): 1e-12 relative outright
-    c = slice(len(T) - 200, len(T))
-    assert relE[c].max() <= 1e-12
-    assert errJ[c].max() <= 1e-12 and errH[c].max() <= 1e-12
 
 
-def test_amips_matches_reference_live(oracle, reflib):
-    T = syn.energy_batch(20000, seed=21)
-    Er, Jr, Hr = reflib.amips_batch_soa(T, nthreads=4)
-    E, J, H, _ = oracle.amips_batch_soa(T, quality=False, nthreads=4)
-    tol = _amips_tolerances(T.T)
-    ok = np.isfinite(Er) & (Er < 1e8)
-    rel = np.abs(E - Er) / np.abs(Er)
-    assert np.all(rel[ok] <= tol[ok])
+def test_amips_closed_form_accurate(closed_form):
+    """The closed form against a 60-digit evaluation of the same function."""
+    import mpmath
+
+    mpmath.mp.dps = 60
+    oracle = closed_form
+    T = syn.energy_batch(60, seed=23).T
+    E = oracle.amips_batch_soa(_aos_to_soa(T), quality=False)[0]
+    for i in range(T.shape[0]):
+        p = [[mpmath.mpf(float(x)) for x in T[i, 3 * j:3 * j + 3]] for j in range(4)]
+        s3, s6 = mpmath.sqrt(3), mpmath.sqrt(6)
+        a = [p[0][k] - p[3][k] for k in range(3)]
+        b = [(p[0][k] - 2 * p[1][k] + p[3][k]) / s3 for k in range(3)]
+        c = [(p[0][k] + p[1][k] + p[3][k] - 3 * p[2][k]) / s6 for k in range(3)]
+        N = sum(x * x for x in a + b + c)
+        D = (a[0] * (b[1] * c[2] - b[2] * c[1]) + a[1] * (b[2] * c[0] - b[0] * c[2]) +
+             a[2] * (b[0] * c[1] - b[1] * c[0]))
+        exact = N * (D * D) ** (mpmath.mpf(-1) / 3)
+        assert abs(float((E[i] - exact) / exact)) < 1e-14
 
 
 # ---------------------------------------------------------- orientation ----
@@ -432,7 +538,16 @@ def test_energy_sweeps_match_reference_golden(oracle):
     """getAvgMaxEnergy / getMaxEnergy / getSecondMaxEnergy / getFilterEnergy
     (LocalOperations.cpp:605-693): the oracle's one-pass sweep against the reference's
     results stored in energy_sweeps_ref.npz, bit for bit, over the filter branches the
-    fixture's thresholds reach (inverted tets at the 1e50 sentinel, locked tets skipped)."""
+    fixture's thresholds reach (inverted tets at the 1e50 sentinel, locked tets skipped).
+    The fixture's energies are the reference's own; the sweep runs on the oracle's libm
+    build, whose energies equal them bit for bit, and the default build's energies agree
+    with them to 1e-12."""
+    from oracle.oracle import Oracle
+
+    Ed = oracle.amips_batch_soa(golden("energy_sweeps_ref.npz")["T"][0], quality=True,
+                                jacobian=False, hessian=False)[0]
+    assert np.all(_within(Ed, golden("energy_sweeps_ref.npz")["E"][0], REL_TOL))
+    oracle = Oracle(libm=True)
     g = golden("energy_sweeps_ref.npz")
     n = g["T"].shape[2]
     tets = np.arange(4 * n, dtype=np.int32).reshape(n, 4)

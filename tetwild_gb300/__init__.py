@@ -80,6 +80,8 @@ _SZ = ctypes.c_size_t
 
 TW_PRECISION_FP64 = 0
 TW_PRECISION_FP32_CERTIFIED = 1
+TW_ENERGY_FORM_REFERENCE = 0
+TW_ENERGY_FORM_CLOSED = 1
 
 _STAT_FIELDS = ("exact_orientations", "env_queries", "env_facet_tests", "env_facet_fp64",
                 "amips_tets", "amips_fp64", "env_warp_fallbacks")
@@ -105,6 +107,7 @@ class TwServerStats(ctypes.Structure):
 
 _SIGS = {
     "tw_set_precision": [_P, _I],
+    "tw_set_energy_form": [_P, _I],
     "tw_get_stats": [_P, ctypes.POINTER(TwStats)],
     "tw_reset_stats": [_P],
     "tw_ctx_create": [_I, _SZ, ctypes.POINTER(_P)],
@@ -262,6 +265,11 @@ class Context:
     def set_precision(self, mode: int):
         """TW_PRECISION_FP64 or TW_PRECISION_FP32_CERTIFIED (same decisions)."""
         self._check(self.lib.tw_set_precision(self.h, mode))
+
+    def set_energy_form(self, form: int):
+        """TW_ENERGY_FORM_REFERENCE (default: the reference's own operations, in
+        its order) or TW_ENERGY_FORM_CLOSED (the accurate closed form)."""
+        self._check(self.lib.tw_set_energy_form(self.h, form))
 
     def stats(self) -> dict:
         s = TwStats()

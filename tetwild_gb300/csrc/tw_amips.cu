@@ -8,6 +8,7 @@
 // k_tet_quality_idx: calTetQualities over ids into the resident mesh
 // (LocalOperations.cpp:695-773): gathers the 4 vertices, orientation, energy
 // with the calTetQuality_AMIPS sentinel.
+#include <atomic>
 #include <cstdint>
 #include <utility>
 
@@ -22,7 +23,8 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
                                                    double* __restrict__ J,
                                                    double* __restrict__ H,
                                                    uint8_t* __restrict__ flip,
-                                                   unsigned long long* __restrict__ exact_count) {
+                                                   unsigned long long* __restrict__ exact_count,
+                                                   int form) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         double t[12];
@@ -37,9 +39,9 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
         double jv[3], hv[9];
         double e;
         if (WJ || WH) {
-            e = amips_egh(t, WJ ? jv : nullptr, WH ? hv : nullptr);
+            e = amips_egh_f(t, WJ ? jv : nullptr, WH ? hv : nullptr, form);
         } else {
-            e = amips_energy(t);
+            e = amips_energy_f(t, form);
         }
         if (WE) E[i] = QUAL ? quality_from(ori, e) : e;
         if (WF) flip[i] = (uint8_t)(ori != 1);
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
 // certified bounds of tw_device.cuh; a tet whose orientation the binary32
 // filter cannot certify takes the FP64 filter (then the exact path), and a tet
 // whose certified energy error exceeds 1e-5 relative is recomputed entirely
-// in FP64 (amips_egh).  Outputs are FP64 like k_amips_soa.
+// in FP64 (in the context's energy form).  Outputs are FP64 like k_amips_soa.
 constexpr float kAmipsTol32 = 1e-5f;
 
 // One tet of the certified kernel: coordinates t in, outputs at index i.
@@ -68,7 +70,7 @@ __device__ __forceinline__ void amips_cert_tet(const double* t, int64_t i, int64
                                                double* __restrict__ E, double* __restrict__ J,
                                                double* __restrict__ H,
                                                uint8_t* __restrict__ flip, uint32_t& ntet,
-                                               uint32_t& nfp64, uint32_t& nexact) {
+                                               uint32_t& nfp64, uint32_t& nexact, int form) {
     {
         float d1[3], d2[3], d3[3];
 #pragma unroll
@@ -100,9 +102,9 @@ __device__ __forceinline__ void amips_cert_tet(const double* t, int64_t i, int64
         } else {
             ++nfp64;
             if (WJ || WH)
-                e = amips_egh(t, WJ ? jv : nullptr, WH ? hv : nullptr);
+                e = amips_egh_f(t, WJ ? jv : nullptr, WH ? hv : nullptr, form);
             else
-                e = amips_energy(t);
+                e = amips_energy_f(t, form);
         }
         if (WE) {
             // a certified binary32 energy is finite and positive: only the
@@ -146,7 +148,8 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
                                                         double* __restrict__ J,
                                                         double* __restrict__ H,
                                                         uint8_t* __restrict__ flip,
-                                                        unsigned long long* __restrict__ counters) {
+                                                        unsigned long long* __restrict__ counters,
+                                                        int form) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     uint32_t ntet = 0, nfp64 = 0, nexact = 0;
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
         double t[12];
 #pragma unroll
         for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
-        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact);
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, form);
     }
     flush_amips_stats(ntet, nfp64, nexact, counters);
 }
@@ -249,7 +252,8 @@ void launch_selftest_wait(const double* src, int limit, unsigned long long* out,
 template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
 __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
     const double* __restrict__ T, int64_t n, double* __restrict__ E, double* __restrict__ J,
-    double* __restrict__ H, uint8_t* __restrict__ flip, unsigned long long* __restrict__ counters) {
+    double* __restrict__ H, uint8_t* __restrict__ flip, unsigned long long* __restrict__ counters,
+    int form) {
     extern __shared__ __align__(128) double stage_mem[];   // kBulkStages x 12 x kBulkTile
     double(*stage)[12 * kBulkTile] = reinterpret_cast<double(*)[12 * kBulkTile]>(stage_mem);
     __shared__ __align__(8) uint64_t bar[kBulkStages];
@@ -314,18 +318,37 @@ __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
 #pragma unroll
             for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
         }
-        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact);
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, form);
     }
     flush_amips_stats(ntet, nfp64, nexact, counters);
 }
 
+// Per-device caches (SM count; kernels whose shared-memory limit was raised),
+// indexed by the device ordinal and safe to fill from several threads: both
+// values are idempotent, so a race only repeats the query.
+constexpr int kMaxDevices = 64;
+static std::atomic<int> g_sm_count[kMaxDevices];
+static std::atomic<uint32_t> g_bulk_attr_set[kMaxDevices];
+
+static int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    return dev;
+}
+
 int grid_for(int64_t n, int block, int blocks_per_sm) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int dev = current_device();
+    int sms = g_sm_count[dev].load(std::memory_order_relaxed);
+    if (sms <= 0) {
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 0;
+        }
         if (sms <= 0) sms = 1;
+        else g_sm_count[dev].store(sms, std::memory_order_relaxed);
     }
     int64_t need = (n + block - 1) / block;
     int64_t cap = (int64_t)sms * blocks_per_sm;
@@ -334,7 +357,7 @@ int grid_for(int64_t n, int block, int blocks_per_sm) {
 }
 
 using AmipsKernel = void (*)(const double*, int64_t, double*, double*, double*, uint8_t*,
-                             unsigned long long*);
+                             unsigned long long*, int);
 
 template <int BITS>
 static AmipsKernel pick_amips() {
@@ -349,14 +372,14 @@ static AmipsKernel amips_table(int bits, std::integer_sequence<int, B...>) {
 }
 
 void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s) {
+                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s, int form) {
     if (n <= 0) return;
     int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
                ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
     AmipsKernel k = amips_table(bits, std::make_integer_sequence<int, 32>{});
     const int block = 256;
     int grid = grid_for(n, block, 8);
-    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, exact_count);
+    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, exact_count, form);
 }
 
 template <int BITS>
@@ -384,7 +407,7 @@ static AmipsKernel amips_bulk_table(int bits, std::integer_sequence<int, B...>) 
 }
 
 void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                           uint8_t* flip, unsigned long long* counters, cudaStream_t s) {
+                           uint8_t* flip, unsigned long long* counters, cudaStream_t s, int form) {
     if (n <= 0) return;
     int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
                ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
@@ -398,25 +421,28 @@ void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, doub
     if (device_mem && n % 2 == 0 && ((uintptr_t)T & 15) == 0 && n >= 64 * kBulkTile) {
         AmipsKernel k = amips_bulk_table(bits, std::make_integer_sequence<int, 32>{});
         const int smem = kBulkStages * 12 * kBulkTile * (int)sizeof(double);
-        static bool attr_set[32] = {};
-        if (!attr_set[bits]) {
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            attr_set[bits] = true;
+        // the shared-memory limit is a per-device attribute of the kernel
+        const int dev = current_device();
+        const uint32_t bit = 1u << bits;
+        if (!(g_bulk_attr_set[dev].load(std::memory_order_acquire) & bit)) {
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ==
+                cudaSuccess)
+                g_bulk_attr_set[dev].fetch_or(bit, std::memory_order_acq_rel);
         }
-        k<<<grid_for(n, kBulkTile, 2), kBulkTile, smem, s>>>(T, n, E, J, H, flip, counters);
+        k<<<grid_for(n, kBulkTile, 2), kBulkTile, smem, s>>>(T, n, E, J, H, flip, counters, form);
         return;
     }
     AmipsKernel k = amips_cert_table(bits, std::make_integer_sequence<int, 32>{});
     const int block = 256;
     int grid = grid_for(n, block, 8);
-    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, counters);
+    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, counters, form);
 }
 
 __global__ void __launch_bounds__(256) k_tet_quality_idx(
     const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,
     const double* __restrict__ vy, const double* __restrict__ vz,
     const uint8_t* __restrict__ rounded, double* __restrict__ E, uint8_t* __restrict__ flip,
-    uint8_t* __restrict__ needs_host, unsigned long long* __restrict__ counters) {
+    uint8_t* __restrict__ needs_host, unsigned long long* __restrict__ counters, int form) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         int4 tv = __ldg(tets + i);
@@ -433,7 +459,7 @@ __global__ void __launch_bounds__(256) k_tet_quality_idx(
         int ex = 0;
         int ori = orient3d(t, t + 3, t + 6, t + 9, &ex);
         if (ex) atomicAdd(counters, 1ULL);
-        if (E) E[i] = quality_from(ori, amips_energy(t));
+        if (E) E[i] = quality_from(ori, amips_energy_f(t, form));
         if (flip) flip[i] = (uint8_t)(ori != 1);
         if (needs_host) needs_host[i] = (uint8_t)(!all_rounded);
         if (!all_rounded) atomicAdd(counters + 1, 1ULL);
@@ -442,12 +468,13 @@ __global__ void __launch_bounds__(256) k_tet_quality_idx(
 
 void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                             const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
-                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s) {
+                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s,
+                            int form) {
     if (n <= 0) return;
     const int block = 256;
     k_tet_quality_idx<<<grid_for(n, block, 8), block, 0, s>>>(
         reinterpret_cast<const int4*>(tets), n, vx, vy, vz, rounded, E, flip, needs_host,
-        counters);
+        counters, form);
 }
 
 
@@ -478,7 +505,7 @@ __global__ void __launch_bounds__(kStatsBlock) k_energy_stats(
     const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,
     const double* __restrict__ vy, const double* __restrict__ vz,
     const uint8_t* __restrict__ locked, double thres_m1, DD* __restrict__ block_sum,
-    unsigned long long* __restrict__ acc) {
+    unsigned long long* __restrict__ acc, int form) {
     // acc: [0] max bits, [1] second-max bits, [2] unlocked count, [3..13] buckets
     __shared__ unsigned long long sb[11];
     __shared__ DD ssum[kStatsBlock / 32];
@@ -498,7 +525,7 @@ __global__ void __launch_bounds__(kStatsBlock) k_energy_stats(
             t[3 * j + 1] = __ldg(vy + id[j]);
             t[3 * j + 2] = __ldg(vz + id[j]);
         }
-        const double e = quality_from(orient3d(t, t + 3, t + 6, t + 9), amips_energy(t));
+        const double e = quality_from(orient3d(t, t + 3, t + 6, t + 9), amips_energy_f(t, form));
         int bk = -1;
         if (e > thres_m1 + 1e10) {
             bk = 10;
@@ -728,10 +755,11 @@ void launch_dihedral_stats(const int32_t* tets, int64_t n, const double* vx, con
 void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                          const double* vz, const uint8_t* locked, double thres,
                          void* block_sum, unsigned long long* acc, double* sum_out,
-                         cudaStream_t s) {
+                         cudaStream_t s, int form) {
     const int blocks = energy_stats_blocks(n);
     k_energy_stats<<<blocks, kStatsBlock, 0, s>>>(reinterpret_cast<const int4*>(tets), n, vx, vy,
-                                                  vz, locked, thres - 1, (DD*)block_sum, acc);
+                                                  vz, locked, thres - 1, (DD*)block_sum, acc,
+                                                  form);
     k_energy_stats_sum<<<1, 32, 0, s>>>((const DD*)block_sum, blocks, sum_out);
 }
 

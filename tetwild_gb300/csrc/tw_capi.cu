@@ -402,6 +402,14 @@ int tw_set_precision(tw_ctx* c, int mode) {
     return TW_OK;
 }
 
+int tw_set_energy_form(tw_ctx* c, int form) {
+    if (!c) return TW_ERR_ARG;
+    if (form != TW_ENERGY_FORM_REFERENCE && form != TW_ENERGY_FORM_CLOSED)
+        return fail(c, TW_ERR_ARG, "tw_set_energy_form: unknown form");
+    c->energy_form = form;
+    return TW_OK;
+}
+
 int tw_get_stats(tw_ctx* c, tw_stats* out) {
     if (!c || !out) return TW_ERR_ARG;
     Guard g(c->device);
@@ -439,9 +447,9 @@ int tw_amips_soa_device(tw_ctx* c, const double* T, int64_t n, int mode, double*
         return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
     Guard g(c->device);
     if (c->precision == TW_PRECISION_FP32_CERTIFIED)
-        launch_amips_soa_cert(T, n, mode, E, J, H, flip, c->counters, c->stream);
+        launch_amips_soa_cert(T, n, mode, E, J, H, flip, c->counters, c->stream, c->energy_form);
     else
-        launch_amips_soa(T, n, mode, E, J, H, flip, c->counters + kCntExactOrient, c->stream);
+        launch_amips_soa(T, n, mode, E, J, H, flip, c->counters + kCntExactOrient, c->stream, c->energy_form);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_amips_soa_device");
     return TW_OK;
@@ -464,11 +472,11 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
         if (dT && (!E || dE) && (!J || dJ) && (!H || dH) && (!flip || dF)) {
             if (c->precision == TW_PRECISION_FP32_CERTIFIED)
                 launch_amips_soa_cert((const double*)dT, n, mode, (double*)dE, (double*)dJ,
-                                      (double*)dH, (uint8_t*)dF, c->counters, c->stream);
+                                      (double*)dH, (uint8_t*)dF, c->counters, c->stream, c->energy_form);
             else
                 launch_amips_soa((const double*)dT, n, mode, (double*)dE, (double*)dJ,
                                  (double*)dH, (uint8_t*)dF, c->counters + kCntExactOrient,
-                                 c->stream);
+                                 c->stream, c->energy_form);
             return sync_status(c, "tw_amips_soa");
         }
     }
@@ -497,10 +505,10 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
             cudaMemcpyAsync(dT[k] + comp * len, T + comp * n + i0, 8 * (size_t)len,
                             cudaMemcpyHostToDevice, s);
         if (c->precision == TW_PRECISION_FP32_CERTIFIED)
-            launch_amips_soa_cert(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s);
+            launch_amips_soa_cert(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s, c->energy_form);
         else
             launch_amips_soa(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k],
-                             c->counters + kCntExactOrient, s);
+                             c->counters + kCntExactOrient, s, c->energy_form);
         if (E) cudaMemcpyAsync(E + i0, dE[k], 8 * (size_t)len, cudaMemcpyDeviceToHost, s);
         if (J)
             for (int comp = 0; comp < 3; ++comp)
@@ -584,7 +592,7 @@ int tw_tet_quality_device(tw_ctx* c, const int32_t* tets, int64_t n, double* ene
     if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
     Guard g(c->device);
     launch_tet_quality_idx(tets, n, c->vx, c->vy, c->vz, c->rounded, energy, flip, needs_host,
-                           c->counters, c->stream);
+                           c->counters, c->stream, c->energy_form);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_tet_quality_device");
     return TW_OK;
@@ -616,7 +624,7 @@ int tw_tet_quality(tw_ctx* c, const int32_t* tets, int64_t n, double* energy, ui
     if (st != TW_OK) return st;
     if (hbad) return fail(c, TW_ERR_ARG, "tet vertex id out of range");
     launch_tet_quality_idx(dt, n, c->vx, c->vy, c->vz, c->rounded, energy ? dE : nullptr,
-                           flip ? dF : nullptr, dN, c->counters, c->stream);
+                           flip ? dF : nullptr, dN, c->counters, c->stream, c->energy_form);
     unsigned long long unrounded = 0;
     cudaMemcpyAsync(&unrounded, c->counters + 1, sizeof(unrounded), cudaMemcpyDeviceToHost,
                     c->stream);
@@ -807,7 +815,7 @@ int tw_newton_stars(tw_ctx* c, const int32_t* star_off, const int32_t* tets, con
     if (st != TW_OK) return st;
     if (hbad) return fail(c, TW_ERR_ARG, "star vertex id out of range");
     launch_newton_stars_shape(c->newton_shape, c->vx, c->vy, c->vz, doff, dt, dc, nstars,
-                              c->newton_max_step, c->newton_max_it, dout, dm, c->stream);
+                              c->newton_max_step, c->newton_max_it, dout, dm, c->stream, c->energy_form);
     cudaMemcpyAsync(out, dout, 24 * (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(moved, dm, (size_t)nstars, cudaMemcpyDeviceToHost, c->stream);
     return sync_status(c, "tw_newton_stars");
@@ -880,7 +888,7 @@ void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uin
                    const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
                    double* out, uint8_t* status, const SmoothScratch& S) {
     launch_smooth_stage1(c->newton_shape, c->vx, c->vy, c->vz, off, tets, cen, kinds, nstars,
-                         c->newton_max_step, c->newton_max_it, out, S.pnew, status, c->stream);
+                         c->newton_max_step, c->newton_max_it, out, S.pnew, status, c->stream, c->energy_form);
     if (!any_surface) return;
     cudaMemsetAsync(S.face_count, 0, sizeof(unsigned long long), c->stream);
     launch_smooth_project(c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], c->eps2, kinds,
@@ -888,7 +896,7 @@ void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uin
                           status, S.pnew, c->counters, c->stream);
     launch_smooth_stage2(c->newton_shape, c->vx, c->vy, c->vz, off, tets, ff, cen, nstars, S.pnew,
                          status, S.faces, S.face_count, S.face_cap, S.face_base, S.face_cnt,
-                         c->counters, c->stream);
+                         c->counters, c->stream, c->energy_form);
     launch_env_faces_dev(c->surf[TW_SURFACE_INPUT], S.faces, S.face_count, S.face_cap, c->eps2,
                          c->sampling_dist, S.face_out, c->precision, c->counters, c->stream);
     launch_smooth_finalize(nstars, S.face_base, S.face_cnt, S.face_out, S.pnew, out, status,
@@ -1022,7 +1030,7 @@ int tw_energy_stats(tw_ctx* c, const int32_t* tets, int64_t n, const uint8_t* lo
     if (hbad) return fail(c, TW_ERR_ARG, "tet vertex id out of range");
     if (n > 0)
         launch_energy_stats(dt, n, c->vx, c->vy, c->vz, locked ? dl : nullptr, thres, dbs, dacc,
-                            dsum, c->stream);
+                            dsum, c->stream, c->energy_form);
     unsigned long long hacc[14];
     double hsum = 0.0;
     cudaMemcpyAsync(hacc, dacc, sizeof hacc, cudaMemcpyDeviceToHost, c->stream);
@@ -1180,7 +1188,7 @@ int tw_collapse_check(tw_ctx* c, const int32_t* v12, const uint8_t* flags, const
                            c->stream);
     launch_collapse_stage(c->newton_shape, c->vx, c->vy, c->vz, doff, dt, dff, dv, dfl, ddeg, n,
                           check_quality, soft_energy, dst, S.faces, S.face_count, S.face_cap,
-                          S.face_base, S.face_cnt, c->counters, c->stream);
+                          S.face_base, S.face_cnt, c->counters, c->stream, c->energy_form);
     if (any_surface)
         launch_env_faces_dev(c->surf[TW_SURFACE_INPUT], S.faces, S.face_count, S.face_cap,
                              c->eps2, c->sampling_dist, S.face_out, c->precision, c->counters,
@@ -1198,7 +1206,7 @@ int tw_newton_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* te
     if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
     Guard g(c->device);
     launch_newton_stars_shape(c->newton_shape, c->vx, c->vy, c->vz, star_off, tets, centers,
-                              nstars, c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+                              nstars, c->newton_max_step, c->newton_max_it, out, moved, c->stream, c->energy_form);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_newton_stars_device");
     return TW_OK;
@@ -1257,7 +1265,7 @@ int tw_newton_autotune_device(tw_ctx* c, const int32_t* star_off, const int32_t*
     Guard g(c->device);
     return autotune_shapes(c, "tw_newton_autotune_device", best_shape, ms_per_shape, [&](int sh) {
         launch_newton_stars_shape(sh, c->vx, c->vy, c->vz, star_off, tets, centers, nstars,
-                                  c->newton_max_step, c->newton_max_it, out, moved, c->stream);
+                                  c->newton_max_step, c->newton_max_it, out, moved, c->stream, c->energy_form);
     });
 }
 

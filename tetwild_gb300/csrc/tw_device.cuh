@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include "../../include/tw_gb300.h"
+
 namespace tw {
 
 constexpr double kMaxEnergy = 1e50;                    // State.h:29
@@ -151,6 +153,209 @@ __device__ __forceinline__ double amips_egh(const double* T, double* J, double* 
         }
     }
     return E;
+}
+
+// ---------------------------------------------------------------------------
+// Reference form of the AMIPS energy, gradient and Hessian
+// (LocalOperations.cpp:28-81, :83-147, :149-291).  The reference evaluates
+// machine-generated expressions on the absolute coordinates with 15-digit
+// coefficients; for a small tet away from the origin their terms cancel by up
+// to ~1e4, so its results carry rounding of up to ~5e-12 relative, and
+// agreeing with it to 1e-12 takes the same IEEE operations in the same order.
+// These routines perform them: every sum and product is grouped as the
+// generated code groups it (left to right), with its coefficients (kRf*).
+// Addition and multiplication are commutative and negation is exact, so only
+// the grouping is kept.  x0..z3: the vertices' coordinates; bx..bz, cx..cz:
+// the scaled frame rows, grouped per routine as its generated code does;
+// Lx0..Lz3: the numerator's per-coordinate linear forms.  pow(d, 2) is d*d
+// and pow(s, -0.333333333333333) is rf_pow_m13.  The CPU oracle performs the
+// same operations; its libm build is bit-identical to the reference.
+// ---------------------------------------------------------------------------
+constexpr double kRfB1 = 0.577350269189626;   // 1/sqrt3 as the generated code spells it
+constexpr double kRfB2 = 1.15470053837925;    // 2/sqrt3 (not 2 kRfB1)
+constexpr double kRfC1 = 0.408248290463863;   // 1/sqrt6
+constexpr double kRfC3 = 1.22474487139159;    // 3/sqrt6
+constexpr double kRfS2 = 0.707106781186548;   // 1/sqrt2
+constexpr double kRf2_3 = 0.666666666666667;
+constexpr double kRf4_3 = 1.33333333333333;
+constexpr double kRf4_9 = 0.444444444444444;
+constexpr double kRf10_9 = 1.11111111111111;
+constexpr double kRfTiny = 1.85037170770859e-17;  // code-generation residue (:267), kept
+constexpr double kRfDelta = 3.515706244646329e-16;  // -0.333333333333333 + 1/3
+constexpr double kRfLn2 = 0.6931471805599453;
+
+// s^(-0.333333333333333): s^(-1/3) (icbrt) times the first-order factor
+// 1 + kRfDelta ln s (a correction below 2.6e-13 over the double range; ln s
+// to ~4% from the exponent and one atanh term keeps its error below 1e-17).
+__device__ __forceinline__ double rf_pow_m13(double s) {
+    const double r = icbrt(s);
+    if (!(r > 0.0) || isinf(r)) return r;
+    const unsigned long long u = (unsigned long long)__double_as_longlong(s);
+    const int e = (int)((u >> 52) & 0x7ff);
+    const double m = __longlong_as_double(
+        (long long)((u & 0x000fffffffffffffULL) | (1023ULL << 52)));
+    const double ln = (double)(e - 1023) * kRfLn2 + (2.0 * (m - 1.0)) / (m + 1.0);
+    return r + r * (kRfDelta * ln);
+}
+
+__device__ __forceinline__ double amips_rf_energy(const double* T) {
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double bx = (kRfB1 * x0 - kRfB2 * x1) + kRfB1 * x3;
+    const double cy = ((kRfC1 * y3 + kRfC1 * y0) + kRfC1 * y1) - kRfC3 * y2;
+    const double by = (kRfB1 * y3 + kRfB1 * y0) - kRfB2 * y1;
+    const double cx = ((kRfC1 * x0 - kRfC3 * x2) + kRfC1 * x1) + kRfC1 * x3;
+    const double cz = ((kRfC1 * z0 + kRfC1 * z1) - kRfC3 * z2) + kRfC1 * z3;
+    const double bz = (kRfB1 * z0 - kRfB2 * z1) + kRfB1 * z3;
+    const double hx = 0.5 * x2 + 0.5 * x1, hy = 0.5 * y1 + 0.5 * y2, hz = 0.5 * z1 + 0.5 * z2;
+    const double num =
+        z0 * ((0.5 * z3 - 1.5 * z0) + hz) + y3 * ((hy - 1.5 * y3) + 0.5 * y0) +
+        x2 * (((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3) +
+        z1 * (((0.5 * z0 - 1.5 * z1) + 0.5 * z2) + 0.5 * z3) +
+        z2 * (((0.5 * z0 + 0.5 * z1) - 1.5 * z2) + 0.5 * z3) + z3 * ((0.5 * z0 - 1.5 * z3) + hz) +
+        x0 * ((hx - 1.5 * x0) + 0.5 * x3) + x1 * (((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3) +
+        x3 * ((hx + 0.5 * x0) - 1.5 * x3) + y0 * ((0.5 * y3 + hy) - 1.5 * y0) +
+        y1 * (((0.5 * y3 + 0.5 * y0) - 1.5 * y1) + 0.5 * y2) +
+        y2 * (((0.5 * y3 + 0.5 * y0) + 0.5 * y1) - 1.5 * y2);
+    const double det = ((z0 - z3) * (cy * bx - by * cx) - (y0 - y3) * (cz * bx - cx * bz)) +
+                       (x0 - x3) * (by * cz - cy * bz);
+    return -num * rf_pow_m13((det * det));
+}
+
+__device__ __forceinline__ void amips_rf_jacobian(const double* T, double* J) {
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double dy = y0 - y3, dz = z0 - z3, dx = x0 - x3;
+    const double bx = (kRfB1 * x0 - kRfB2 * x1) + kRfB1 * x3;
+    const double by = (kRfB1 * y0 - kRfB2 * y1) + kRfB1 * y3;
+    const double bz = (kRfB1 * z0 - kRfB2 * z1) + kRfB1 * z3;
+    const double cx = ((kRfC1 * x0 - kRfC3 * x2) + kRfC1 * x1) + kRfC1 * x3;
+    const double cy = ((kRfC1 * y0 + kRfC1 * y1) - kRfC3 * y2) + kRfC1 * y3;
+    const double cz = ((kRfC1 * z1 - kRfC3 * z2) + kRfC1 * z3) + kRfC1 * z0;
+    const double czbx = cz * bx - bz * cx;
+    const double cybx = cy * bx, cxby = cx * by;
+    const double det = (czbx * dy - dz * (cybx - cxby)) - dx * (cz * by - bz * cy);
+    const double r = rf_pow_m13((det * det));
+    const double sz = kRfS2 * z1 - kRfS2 * z2, sy = kRfS2 * y1 - kRfS2 * y2;
+    const double sx = kRfS2 * x1 - kRfS2 * x2;
+    const double hx = 0.5 * x2 + 0.5 * x1, hy = 0.5 * y1 + 0.5 * y2, hz = 0.5 * z1 + 0.5 * z2;
+    const double num =
+        y0 * ((0.5 * y3 - 1.5 * y0) + hy) + z1 * (((0.5 * z2 - 1.5 * z1) + 0.5 * z3) + 0.5 * z0) +
+        z2 * (((0.5 * z1 - 1.5 * z2) + 0.5 * z3) + 0.5 * z0) + z3 * ((hz - 1.5 * z3) + 0.5 * z0) +
+        y3 * ((0.5 * y0 - 1.5 * y3) + hy) + x2 * (((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3) +
+        y1 * (((0.5 * y0 + 0.5 * y3) - 1.5 * y1) + 0.5 * y2) +
+        y2 * (((0.5 * y0 + 0.5 * y3) + 0.5 * y1) - 1.5 * y2) + x0 * ((hx - 1.5 * x0) + 0.5 * x3) +
+        x1 * (((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3) + x3 * ((0.5 * x0 + hx) - 1.5 * x3) +
+        z0 * ((0.5 * z3 + hz) - 1.5 * z0);
+    const double w = (kRf2_3 * num) / det;
+    const double q0 = ((sz * (y3 - y0) - sy * (z3 - z0)) - bz * cy) + by * cz;
+    J[0] = -(r * ((((x2 - 3.0 * x0) + w * q0) + x1) + x3));
+    J[1] = r * ((((3.0 * y0 - y3) - y1) - y2) + w * ((czbx + dz * sx) - dx * sz));
+    J[2] = r * (((((-z1) - z2) - z3) + w * (((-(dy * sx)) - cybx) + cxby + dx * sy)) + 3.0 * z0);
+}
+
+__device__ __forceinline__ void amips_rf_hessian(const double* T, double* H) {
+    const double x0 = T[0], y0 = T[1], z0 = T[2], x1 = T[3], y1 = T[4], z1 = T[5];
+    const double x2 = T[6], y2 = T[7], z2 = T[8], x3 = T[9], y3 = T[10], z3 = T[11];
+    const double dz = z0 - z3, dx = x0 - x3, dy = y0 - y3;
+    const double bx = (kRfB1 * x0 - kRfB2 * x1) + kRfB1 * x3;
+    const double by = (kRfB1 * y0 - kRfB2 * y1) + kRfB1 * y3;
+    const double bz = (kRfB1 * z0 - kRfB2 * z1) + kRfB1 * z3;
+    const double cx = ((kRfC1 * x0 + kRfC1 * x1) - kRfC3 * x2) + kRfC1 * x3;
+    const double cy = ((kRfC1 * y0 + kRfC1 * y1) - kRfC3 * y2) + kRfC1 * y3;
+    const double cz = ((kRfC1 * z0 + kRfC1 * z1) - kRfC3 * z2) + kRfC1 * z3;
+    const double bxcy = bx * cy, bycx = by * cx;
+    const double mx = dz * (bxcy - bycx);
+    const double bycz = by * cz, cybz = cy * bz;
+    const double myz = bycz - cybz;
+    const double my = dx * myz;
+    const double bxcz = bx * cz, cxbz = cx * bz;
+    const double mxz = bxcz - cxbz;
+    const double mz = dy * mxz;
+    const double det = (mx + my) - mz;
+    const double det2 = (det * det);
+    const double r = rf_pow_m13(det2);
+    const double lx = ((x2 - 3.0 * x0) + x1) + x3;
+    const double sy = kRfS2 * y1 - kRfS2 * y2;
+    const double dzsy = dz * sy;
+    const double sz = kRfS2 * z1 - kRfS2 * z2;
+    const double dysz = dy * sz;
+    const double u = (myz + dzsy) - dysz;
+    const double k43 = kRf4_3 / det;
+    const double idet2 = 1.0 / det2;
+    const double hx = 0.5 * x2 + 0.5 * x1;
+    const double Lx0 = (hx - 1.5 * x0) + 0.5 * x3;
+    const double Lx3 = (0.5 * x0 + hx) - 1.5 * x3;
+    const double Lx2 = ((0.5 * x0 - 1.5 * x2) + 0.5 * x1) + 0.5 * x3;
+    const double Lx1 = ((0.5 * x2 + 0.5 * x0) - 1.5 * x1) + 0.5 * x3;
+    const double hy = 0.5 * y1 + 0.5 * y2;
+    const double Ly0 = (0.5 * y3 - 1.5 * y0) + hy;
+    const double Ly3 = (0.5 * y0 - 1.5 * y3) + hy;
+    const double Ly2 = ((0.5 * y0 + 0.5 * y1) - 1.5 * y2) + 0.5 * y3;
+    const double Ly1 = ((0.5 * y0 - 1.5 * y1) + 0.5 * y2) + 0.5 * y3;
+    const double hz = 0.5 * z1 + 0.5 * z2;
+    const double Lz0 = (0.5 * z3 - 1.5 * z0) + hz;
+    const double Lz3 = (0.5 * z0 - 1.5 * z3) + hz;
+    const double Lz2 = ((0.5 * z0 + 0.5 * z3) + 0.5 * z1) - 1.5 * z2;
+    const double Lz1 = ((0.5 * z0 + 0.5 * z3) - 1.5 * z1) + 0.5 * z2;
+    const double num = z0 * Lz0 + y0 * Ly0 + y1 * Ly1 + y2 * Ly2 + y3 * Ly3 + z3 * Lz3 +
+                       x2 * Lx2 + z1 * Lz1 + z2 * Lz2 + x0 * Lx0 + x1 * Lx1 + Lx3 * x3;
+    const double k49n = (kRf4_9 * idet2) * num;
+    const double nd = idet2 * num;
+    const double ineg = 1.0 / (-det);
+    const double rneg = ineg * r;
+    const double sx = kRfS2 * x1 - kRfS2 * x2;
+    const double v1 = (((kRf2_3 * bx) * cz + (kRf2_3 * dz) * sx) - (kRf2_3 * cx) * bz) -
+                      (kRf2_3 * dx) * sz;
+    const double ly = ((y1 - 3.0 * y0) + y2) + y3;
+    const double ey = y3 - y0, ez = z3 - z0;
+    const double v2 = (((-kRf2_3 * sy) * ez + (kRf2_3 * sz) * ey) + (kRf2_3 * by) * cz) -
+                      (kRf2_3 * bz) * cy;
+    const double dzsx = dz * sx, dxsz = dx * sz;
+    const double p = (dzsx - dxsz) + mxz;
+    const double q = ((sz * ey - sy * ez) + by * cz) - bz * cy;
+    const double a1 = ((((kRf4_9 * p) * q) * num) * ineg + lx * v1) - ly * v2;
+    const double tiny = (kRfTiny * z0) * Lz0 + (kRfTiny * y0) * Ly0 + (kRfTiny * y1) * Ly1 +
+                        (kRfTiny * y2) * Ly2 + (kRfTiny * y3) * Ly3 + (kRfTiny * z3) * Lz3 +
+                        (kRfTiny * x2) * Lx2 + (kRfTiny * z1) * Lz1 + (kRfTiny * z2) * Lz2 +
+                        (kRfTiny * x0) * Lx0 + (kRfTiny * x1) * Lx1 + (kRfTiny * Lx3) * x3;
+    const double un = (u * num) * ineg;
+    const double v3 = (((kRf2_3 * by) * cx - (kRf2_3 * bx) * cy) + (kRf2_3 * dx) * sy) -
+                      (kRf2_3 * dy) * sx;
+    const double lz = ((z3 - 3.0 * z0) + z1) + z2;
+    const double t = ((bycx - bxcy) + dx * sy) - dy * sx;
+    const double tn = ((kRf4_9 * t) * num) * ineg;
+    const double a2 = (q * tn + v3 * lx) - lz * v2;
+    const double ex = x3 - x0;
+    const double w1 = (num * ineg) * (((ex * sz - sx * ez) + bx * cz) - cx * bz);
+    const double s = ((dxsz - dzsx) - bxcz) + cxbz;
+    const double a3 = ((-p) * tn + v3 * ly) + lz * v1;
+    const double w2 = (num * ineg) * (((ex * (-sy) + sx * ey) - bx * cy) + cx * by);
+    H[0] = r * ((((lx * u) * k43 - (u * u) * k49n) + ((kRf2_3 * u) * nd) * (((cybz - bycz) - dzsy) + dysz)) + 3.0);
+    H[1] = rneg * ((a1 - tiny * z1) + un * v1);
+    H[2] = rneg * (un * v3 + a2);
+    H[3] = rneg * (a1 + w1 * v2);
+    H[4] = r * ((((-(s * s)) * k49n + (s * k43) * ly) + (s * nd) * v1) + 3.0);
+    H[5] = rneg * (((-tiny) * x1 - v3 * w1) + a3);
+    H[6] = rneg * (((-tiny) * y1 + a2) + w2 * v2);
+    H[7] = rneg * (a3 - w2 * v1);
+    H[8] = r * ((((-lz) * t) * k43 - (kRf10_9 * (t * t)) * nd) + 3.0);
+}
+
+// Energy form of the FP64 evaluations (TW_ENERGY_FORM_*): the reference form
+// (the default: agrees with the reference to its rounding) or the closed form.
+__device__ __forceinline__ double amips_energy_f(const double* T, int form) {
+    return form == TW_ENERGY_FORM_CLOSED ? amips_energy(T) : amips_rf_energy(T);
+}
+// E, and J / H when non-null, in the selected form.  In the reference form
+// they come from the three separate routines, as NewtonsUpdate calls them
+// (VertexSmoother.cpp:654-672).
+__device__ __forceinline__ double amips_egh_f(const double* T, double* J, double* H, int form) {
+    if (form == TW_ENERGY_FORM_CLOSED) return amips_egh(T, J, H);
+    const double e = amips_rf_energy(T);
+    if (J) amips_rf_jacobian(T, J);
+    if (H) amips_rf_hessian(T, H);
+    return e;
 }
 
 // ---------------------------------------------------------------------------

@@ -131,6 +131,7 @@ struct tw_ctx {
     int32_t nv = 0;
     size_t mesh_bytes = 0;
     int precision = TW_PRECISION_FP64;
+    int energy_form = TW_ENERGY_FORM_REFERENCE;   // tw_set_energy_form
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
     double grid_cell = 0.2;   // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
     // launch timing of the point-envelope test kernel (TW_TUNE_TIME_KERNELS):
@@ -180,14 +181,19 @@ void dev_free(tw_ctx* c, void* p, size_t bytes);
 int grid_for(int64_t n, int block, int blocks_per_sm);
 
 // ---- launchers (tw_amips.cu) ----
+// form: TW_ENERGY_FORM_* of the binary64 AMIPS evaluations (every launcher
+// below that evaluates energies takes it last, the reference form by default).
 void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s);
+                      uint8_t* flip, unsigned long long* exact_count, cudaStream_t s,
+                      int form = TW_ENERGY_FORM_REFERENCE);
 // certified binary32 variant; counters is the context's counter array
 void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                           uint8_t* flip, unsigned long long* counters, cudaStream_t s);
+                           uint8_t* flip, unsigned long long* counters, cudaStream_t s,
+                           int form = TW_ENERGY_FORM_REFERENCE);
 void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                             const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
-                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s);
+                            uint8_t* needs_host, unsigned long long* counters, cudaStream_t s,
+                            int form = TW_ENERGY_FORM_REFERENCE);
 
 // Energy sweeps: block_sum holds energy_stats_blocks(n) double-doubles; acc
 // 14 words zeroed by the caller (max bits, second-max bits, unlocked count,
@@ -207,7 +213,7 @@ void launch_dihedral_stats(const int32_t* tets, int64_t n, const double* vx, con
 void launch_energy_stats(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                          const double* vz, const uint8_t* locked, double thres,
                          void* block_sum, unsigned long long* acc, double* sum_out,
-                         cudaStream_t s);
+                         cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
 
 // ---- launchers (tw_lbvh.cu) ----
 int build_surface(tw_ctx* c, Surface& S, const double* dV, int32_t nv, const int32_t* dF,
@@ -255,7 +261,7 @@ void launch_smooth_project(const Surface& Sin, const Surface& Sb, double eps2,
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,
                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                          int32_t nstars, int max_step, int max_it, double* out, uint8_t* moved,
-                         cudaStream_t s);
+                         cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
 // shape in [0, newton_num_shapes()): lanes per star and block size (see
 // kNewtonShapes); every shape gives bit-identical results.
 int newton_num_shapes();
@@ -263,7 +269,8 @@ void newton_shape_info(int shape, int* group, int* block);
 void launch_newton_stars_shape(int shape, const double* vx, const double* vy, const double* vz,
                                const int32_t* star_off, const int32_t* tets,
                                const int32_t* centers, int32_t nstars, int max_step, int max_it,
-                               double* out, uint8_t* moved, cudaStream_t s);
+                               double* out, uint8_t* moved, cudaStream_t s,
+                               int form = TW_ENERGY_FORM_REFERENCE);
 
 // Smoothing pass (tw_newton.cu): stage 1 = validity + NewtonsMethod (interior
 // stars finish here, surface stars become kSmoothPendingProject with their
@@ -274,13 +281,15 @@ void launch_newton_stars_shape(int shape, const double* vx, const double* vy, co
 void launch_smooth_stage1(int shape, const double* vx, const double* vy, const double* vz,
                           const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                           const uint8_t* kinds, int32_t nstars, int max_step, int max_it,
-                          double* out, double* pnew, uint8_t* status, cudaStream_t s);
+                          double* out, double* pnew, uint8_t* status, cudaStream_t s,
+                          int form = TW_ENERGY_FORM_REFERENCE);
 void launch_smooth_stage2(int shape, const double* vx, const double* vy, const double* vz,
                           const int32_t* star_off, const int32_t* tets, const uint8_t* face_flags,
                           const int32_t* centers, int32_t nstars, const double* pnew,
                           uint8_t* status, double* faces, unsigned long long* face_count,
                           int64_t face_cap, int32_t* face_base, int32_t* face_cnt,
-                          unsigned long long* counters, cudaStream_t s);
+                          unsigned long long* counters, cudaStream_t s,
+                          int form = TW_ENERGY_FORM_REFERENCE);
 void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
                             const uint8_t* face_out, const double* pnew, double* out,
                             uint8_t* status, cudaStream_t s);
@@ -316,7 +325,7 @@ void launch_collapse_stage(int shape, const double* vx, const double* vy, const 
                            int32_t n, int check_quality, double soft_energy, uint8_t* status,
                            double* faces, unsigned long long* face_count, int64_t face_cap,
                            int32_t* face_base, int32_t* face_cnt, unsigned long long* counters,
-                           cudaStream_t s);
+                           cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
 void launch_collapse_finalize(int32_t n, const int32_t* face_base, const int32_t* face_cnt,
                               const uint8_t* face_out, uint8_t* status, cudaStream_t s);
 

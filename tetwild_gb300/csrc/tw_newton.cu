@@ -95,6 +95,7 @@ struct StarView {
     const int4* tets;
     int32_t nt;
     int32_t v;
+    int form;   // TW_ENERGY_FORM_* of the binary64 AMIPS evaluations
 };
 
 __device__ __forceinline__ void gather_tet(const StarView& S, int4 tv, int start, const double* pos,
@@ -128,7 +129,7 @@ __device__ double star_new_energy(const StarView& S, const double* pos) {
     double s = 0.0, T[12];
     for (int32_t i = 0; i < S.nt; ++i) {
         gather_tet(S, __ldg(S.tets + i), 0, pos, T);
-        s += amips_energy(T);
+        s += amips_energy_f(T, S.form);
     }
     if (isinf(s) || isnan(s) || s <= 0.0 || s > kMaxEnergy) s = kMaxEnergy;
     return s;
@@ -143,7 +144,7 @@ __device__ bool star_update(const StarView& S, const double* pos, double& energy
         int4 tv = __ldg(S.tets + i);
         int start = (tv.x == S.v) ? 0 : (tv.y == S.v) ? 1 : (tv.z == S.v) ? 2 : (tv.w == S.v) ? 3 : 0;
         gather_tet(S, tv, start, pos, T);
-        e += amips_egh(T, J1, H1);   // its E is amips_energy's, operation for operation
+        e += amips_egh_f(T, J1, H1, S.form);   // its E is amips_energy_f's, operation for operation
         for (int j = 0; j < 3; ++j) {
             J[j] += J1[j];
             H[3 * j + 0] += H1[3 * j + 0];
@@ -170,11 +171,11 @@ __global__ void __launch_bounds__(128) k_newton_stars(const double* __restrict__
                                                       const int32_t* __restrict__ centers,
                                                       int32_t nstars, int max_step, int max_it,
                                                       double* __restrict__ out,
-                                                      uint8_t* __restrict__ moved) {
+                                                      uint8_t* __restrict__ moved, int form) {
     int32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid >= nstars) return;
     int32_t b = star_off[sid], e = star_off[sid + 1];
-    StarView S{vx, vy, vz, tets + b, e - b, centers[sid]};
+    StarView S{vx, vy, vz, tets + b, e - b, centers[sid], form};
     double pos[3] = {vx[S.v], vy[S.v], vz[S.v]};
     int is_moved = 0;
     double old_energy = 0.0, new_energy = 0.0, J[3], H[9];
@@ -267,7 +268,7 @@ __device__ __forceinline__ int newton_group_star(const StarView& S, double* pos,
                           : (tv.w == S.v) ? 3 : 0;
                 double T[12];
                 gather_tet(S, tv, start, pos, T);
-                te = amips_egh(T, tJ, tH);   // its E is amips_energy's, operation for operation
+                te = amips_egh_f(T, tJ, tH, S.form);   // its E is amips_energy_f's
             }
             for (int t = 0; t < cnt; ++t) {
                 e += __shfl_sync(gm, te, t, G);
@@ -320,7 +321,7 @@ __device__ __forceinline__ int newton_group_star(const StarView& S, double* pos,
                 if (gl < cnt) {
                     double T[12];
                     gather_tet(S, __ldg(S.tets + c0 + gl), 0, pos, T);
-                    te = amips_energy(T);
+                    te = amips_energy_f(T, S.form);
                 }
                 for (int t = 0; t < cnt; ++t) sum += __shfl_sync(gm, te, t, G);
             }
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(256) k_newton_group(const double* __restrict__
                                                       const int32_t* __restrict__ centers,
                                                       int32_t nstars, int max_step, int max_it,
                                                       double* __restrict__ out,
-                                                      uint8_t* __restrict__ moved) {
+                                                      uint8_t* __restrict__ moved, int form) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(256) k_newton_group(const double* __restrict__
     const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
     for (int64_t sid = gid; sid < nstars; sid += ngroups) {
         const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
-        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid], form};
         double pos[3] = {vx[S.v], vy[S.v], vz[S.v]};
         const int is_moved = newton_group_star<G>(S, pos, max_step, max_it, gl, gm);
         if (gl == 0) {
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(256) k_smooth_stage1(
     const int32_t* __restrict__ star_off, const int4* __restrict__ tets,
     const int32_t* __restrict__ centers, const uint8_t* __restrict__ kinds, int32_t nstars,
     int max_step, int max_it, double* __restrict__ out, double* __restrict__ pnew,
-    uint8_t* __restrict__ status) {
+    uint8_t* __restrict__ status, int form) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(256) k_smooth_stage1(
     const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
     for (int64_t sid = gid; sid < nstars; sid += ngroups) {
         const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
-        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid], form};
         const double p0[3] = {vx[S.v], vy[S.v], vz[S.v]};
         double pos[3] = {p0[0], p0[1], p0[2]};
         const uint8_t kind = kinds ? kinds[sid] : (uint8_t)TW_STAR_INTERIOR;
@@ -447,8 +448,8 @@ __device__ __forceinline__ void face_key(int4 tv, int j, int32_t* k) {
 }
 
 // calTetQuality_AMIPS for a tet already known to be POSITIVE.
-__device__ __forceinline__ double positive_tet_quality(const double* T) {
-    return quality_from(1, amips_energy(T));
+__device__ __forceinline__ double positive_tet_quality(const double* T, int form) {
+    return quality_from(1, amips_energy_f(T, form));
 }
 
 // True when face j of the star's tet c0 is a surface face through the
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(256) k_smooth_stage2(
     const double* __restrict__ pnew, uint8_t* __restrict__ status, double* __restrict__ faces,
     unsigned long long* __restrict__ face_count, int64_t face_cap,
     int32_t* __restrict__ face_base, int32_t* __restrict__ face_cnt,
-    unsigned long long* __restrict__ counters) {
+    unsigned long long* __restrict__ counters, int form) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);
@@ -490,7 +491,7 @@ __global__ void __launch_bounds__(256) k_smooth_stage2(
     for (int64_t sid = gid; sid < nstars; sid += ngroups) {
         if (status[sid] != kSmoothPendingProject) continue;  // uniform within the group
         const int32_t b = star_off[sid], nt = star_off[sid + 1] - b;
-        StarView S{vx, vy, vz, tets + b, nt, centers[sid]};
+        StarView S{vx, vy, vz, tets + b, nt, centers[sid], form};
         const double p0[3] = {vx[S.v], vy[S.v], vz[S.v]};
         const double p[3] = {pnew[3 * sid], pnew[3 * sid + 1], pnew[3 * sid + 2]};
         // isFlip at the projected position (:374-378)
@@ -504,9 +505,9 @@ __global__ void __launch_bounds__(256) k_smooth_stage2(
             double T[12];
             int4 tv = tet_at(S, c0);
             gather_tet(S, tv, 0, p0, T);
-            old_max = fmax(old_max, positive_tet_quality(T));
+            old_max = fmax(old_max, positive_tet_quality(T, S.form));
             gather_tet(S, tv, 0, p, T);
-            new_max = fmax(new_max, positive_tet_quality(T));
+            new_max = fmax(new_max, positive_tet_quality(T, S.form));
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) {
@@ -594,7 +595,7 @@ __global__ void __launch_bounds__(256) k_collapse_stage(
     int check_quality, double soft_energy, uint8_t* __restrict__ status,
     double* __restrict__ faces, unsigned long long* __restrict__ face_count, int64_t face_cap,
     int32_t* __restrict__ face_base, int32_t* __restrict__ face_cnt,
-    unsigned long long* __restrict__ counters) {
+    unsigned long long* __restrict__ counters, int form) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const unsigned gm = group_mask<G>(lane);
@@ -604,7 +605,7 @@ __global__ void __launch_bounds__(256) k_collapse_stage(
         if (status[e] != kCollapsePending) continue;  // uniform within the group
         const int32_t b = off[e], nt = off[e + 1] - b;
         const int32_t v1 = v12[2 * e], v2 = v12[2 * e + 1];
-        StarView S{vx, vy, vz, tets + b, nt, v1};
+        StarView S{vx, vy, vz, tets + b, nt, v1, form};
         const double p1[3] = {vx[v1], vy[v1], vz[v1]};
         const double p2[3] = {vx[v2], vy[v2], vz[v2]};
         const uint8_t fl = flags[e];
@@ -630,10 +631,10 @@ __global__ void __launch_bounds__(256) k_collapse_stage(
                 double T[12];
                 gather_tet(S, tv, 0, p1, T);
                 old_max = fmax(old_max, quality_from(orient3d(T, T + 3, T + 6, T + 9),
-                                                     amips_energy(T)));
+                                                     amips_energy_f(T, S.form)));
                 if (tet_has(tv, v2)) continue;
                 gather_tet(S, tv, 0, p2, T);
-                new_max = fmax(new_max, positive_tet_quality(T));
+                new_max = fmax(new_max, positive_tet_quality(T, S.form));
             }
 #pragma unroll
             for (int o = G / 2; o > 0; o >>= 1) {
@@ -772,7 +773,7 @@ void newton_shape_info(int shape, int* group, int* block) {
 void launch_newton_stars_shape(int shape, const double* vx, const double* vy, const double* vz,
                                const int32_t* star_off, const int32_t* tets,
                                const int32_t* centers, int32_t nstars, int max_step, int max_it,
-                               double* out, uint8_t* moved, cudaStream_t s) {
+                               double* out, uint8_t* moved, cudaStream_t s, int form) {
     if (nstars <= 0) return;
     if (shape < 0 || shape >= newton_num_shapes()) shape = 5;
     const NewtonShape sh = kNewtonShapes[shape];
@@ -780,20 +781,20 @@ void launch_newton_stars_shape(int shape, const double* vx, const double* vy, co
     if (sh.group == 1) {
         int grid = (nstars + sh.block - 1) / sh.block;
         k_newton_stars<<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
-                                                 max_step, max_it, out, moved);
+                                                 max_step, max_it, out, moved, form);
         return;
     }
     const int64_t threads = (int64_t)nstars * sh.group;
     const int grid = grid_for(threads, sh.block, 2048 / sh.block);
     if (sh.group == 8)
         k_newton_group<8><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
-                                                    max_step, max_it, out, moved);
+                                                    max_step, max_it, out, moved, form);
     else if (sh.group == 16)
         k_newton_group<16><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
-                                                     max_step, max_it, out, moved);
+                                                     max_step, max_it, out, moved, form);
     else
         k_newton_group<32><<<grid, sh.block, 0, s>>>(vx, vy, vz, star_off, t4, centers, nstars,
-                                                     max_step, max_it, out, moved);
+                                                     max_step, max_it, out, moved, form);
 }
 
 // Smoothing kernels use the Newton shape's group size; shape 0 (one thread
@@ -809,7 +810,8 @@ static int smooth_group(int shape, int* block) {
 void launch_smooth_stage1(int shape, const double* vx, const double* vy, const double* vz,
                           const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                           const uint8_t* kinds, int32_t nstars, int max_step, int max_it,
-                          double* out, double* pnew, uint8_t* status, cudaStream_t s) {
+                          double* out, double* pnew, uint8_t* status, cudaStream_t s,
+                          int form) {
     if (nstars <= 0) return;
     int block;
     const int G = smooth_group(shape, &block);
@@ -817,13 +819,13 @@ void launch_smooth_stage1(int shape, const double* vx, const double* vy, const d
     const int4* t4 = reinterpret_cast<const int4*>(tets);
     if (G == 8)
         k_smooth_stage1<8><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
-                                                  max_step, max_it, out, pnew, status);
+                                                  max_step, max_it, out, pnew, status, form);
     else if (G == 16)
         k_smooth_stage1<16><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
-                                                   max_step, max_it, out, pnew, status);
+                                                   max_step, max_it, out, pnew, status, form);
     else
         k_smooth_stage1<32><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, centers, kinds, nstars,
-                                                   max_step, max_it, out, pnew, status);
+                                                   max_step, max_it, out, pnew, status, form);
 }
 
 void launch_smooth_stage2(int shape, const double* vx, const double* vy, const double* vz,
@@ -831,7 +833,7 @@ void launch_smooth_stage2(int shape, const double* vx, const double* vy, const d
                           const int32_t* centers, int32_t nstars, const double* pnew,
                           uint8_t* status, double* faces, unsigned long long* face_count,
                           int64_t face_cap, int32_t* face_base, int32_t* face_cnt,
-                          unsigned long long* counters, cudaStream_t s) {
+                          unsigned long long* counters, cudaStream_t s, int form) {
     if (nstars <= 0) return;
     int block;
     const int G = smooth_group(shape, &block);
@@ -840,15 +842,15 @@ void launch_smooth_stage2(int shape, const double* vx, const double* vy, const d
     if (G == 8)
         k_smooth_stage2<8><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
                                                   nstars, pnew, status, faces, face_count, face_cap,
-                                                  face_base, face_cnt, counters);
+                                                  face_base, face_cnt, counters, form);
     else if (G == 16)
         k_smooth_stage2<16><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
                                                    nstars, pnew, status, faces, face_count, face_cap,
-                                                   face_base, face_cnt, counters);
+                                                   face_base, face_cnt, counters, form);
     else
         k_smooth_stage2<32><<<grid, block, 0, s>>>(vx, vy, vz, star_off, t4, face_flags, centers,
                                                    nstars, pnew, status, faces, face_count, face_cap,
-                                                   face_base, face_cnt, counters);
+                                                   face_base, face_cnt, counters, form);
 }
 
 void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
@@ -866,7 +868,7 @@ void launch_collapse_stage(int shape, const double* vx, const double* vy, const 
                            int32_t n, int check_quality, double soft_energy, uint8_t* status,
                            double* faces, unsigned long long* face_count, int64_t face_cap,
                            int32_t* face_base, int32_t* face_cnt, unsigned long long* counters,
-                           cudaStream_t s) {
+                           cudaStream_t s, int form) {
     if (n <= 0) return;
     int block;
     const int G = smooth_group(shape, &block);
@@ -874,7 +876,7 @@ void launch_collapse_stage(int shape, const double* vx, const double* vy, const 
     const int4* t4 = reinterpret_cast<const int4*>(tets);
 #define TW_COLLAPSE_ARGS                                                                      \
     vx, vy, vz, off, t4, face_flags, v12, flags, degenerate, n, check_quality, soft_energy, status, \
-        faces, face_count, face_cap, face_base, face_cnt, counters
+        faces, face_count, face_cap, face_base, face_cnt, counters, form
     if (G == 8)
         k_collapse_stage<8><<<grid, block, 0, s>>>(TW_COLLAPSE_ARGS);
     else if (G == 16)
@@ -894,9 +896,9 @@ void launch_collapse_finalize(int32_t n, const int32_t* face_base, const int32_t
 void launch_newton_stars(const double* vx, const double* vy, const double* vz,
                          const int32_t* star_off, const int32_t* tets, const int32_t* centers,
                          int32_t nstars, int max_step, int max_it, double* out, uint8_t* moved,
-                         cudaStream_t s) {
+                         cudaStream_t s, int form) {
     launch_newton_stars_shape(5, vx, vy, vz, star_off, tets, centers, nstars, max_step, max_it, out,
-                              moved, s);
+                              moved, s, form);
 }
 
 }  // namespace tw

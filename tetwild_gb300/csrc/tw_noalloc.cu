@@ -18,7 +18,10 @@
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and keeps it; make
-// that first call before capturing the stream into a graph.  Every call on a
+// that first call before any stream capture.  Results are those of
+// tw_amips_soa on a context in TW_PRECISION_FP64 with the default (reference)
+// energy form.  An error that earlier work of the caller left pending is
+// consumed on entry; every copy and the launch are checked as they are queued.  Every call on a
 // device shares the one array and leaves the last call's contents in it:
 // calls whose work overlaps on the GPU (from several host threads, or on
 // several streams) race on it, so serialise them.
@@ -90,21 +93,35 @@ extern "C" TW_API int tw_amips_soa_noalloc(const double* T, int64_t n, int mode,
     double* dH = H ? reinterpret_cast<double*>(base + kOffH) : nullptr;
     uint8_t* dF = flip ? reinterpret_cast<uint8_t*>(base + kOffF) : nullptr;
     auto* counter = reinterpret_cast<unsigned long long*>(base + kOffC);
+    // An error left pending by earlier work of the caller is not this call's:
+    // consume it so that the checks below see only this call's own errors.
+    cudaGetLastError();
+    // Each step is checked as it is queued; on the first failure nothing more
+    // is queued, the stream is drained (so no queued copy outlives the call)
+    // and the call fails.
+    cudaError_t e = cudaSuccess;
+    auto step = [&](cudaError_t r) {
+        if (e == cudaSuccess && r != cudaSuccess) e = r;
+        return e == cudaSuccess;
+    };
     // The counter keeps the previous call's value: it must start at zero.
-    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
-    for (int c = 0; c < 12; ++c)
-        cudaMemcpyAsync(dT + c * n, T + c * n, 8 * (size_t)n, cudaMemcpyHostToDevice, s);
-    tw::launch_amips_soa(dT, n, mode, dE, dJ, dH, dF, counter, s);
-    if (E) cudaMemcpyAsync(E, dE, 8 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    if (J)
-        for (int c = 0; c < 3; ++c)
-            cudaMemcpyAsync(J + c * n, dJ + c * n, 8 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    if (H)
-        for (int c = 0; c < 9; ++c)
-            cudaMemcpyAsync(H + c * n, dH + c * n, 8 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    if (flip) cudaMemcpyAsync(flip, dF, (size_t)n, cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaGetLastError();
+    step(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s));
+    for (int c = 0; c < 12 && e == cudaSuccess; ++c)
+        step(cudaMemcpyAsync(dT + c * n, T + c * n, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+    if (e == cudaSuccess) {
+        tw::launch_amips_soa(dT, n, mode, dE, dJ, dH, dF, counter, s);
+        step(cudaGetLastError());
+    }
+    if (E && e == cudaSuccess)
+        step(cudaMemcpyAsync(E, dE, 8 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    for (int c = 0; J && c < 3 && e == cudaSuccess; ++c)
+        step(cudaMemcpyAsync(J + c * n, dJ + c * n, 8 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    for (int c = 0; H && c < 9 && e == cudaSuccess; ++c)
+        step(cudaMemcpyAsync(H + c * n, dH + c * n, 8 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (flip && e == cudaSuccess)
+        step(cudaMemcpyAsync(flip, dF, (size_t)n, cudaMemcpyDeviceToHost, s));
+    const cudaError_t es = cudaStreamSynchronize(s);
+    step(es);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return TW_ERR_CUDA;

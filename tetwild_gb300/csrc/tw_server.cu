@@ -240,10 +240,10 @@ int launch_amips(const BatchParams& P, Lane& L, std::vector<Req*>& B) {
         double* H = r.out2 ? dH : nullptr;
         uint8_t* F = r.out3 ? dF : nullptr;
         if (P.precision == TW_PRECISION_FP32_CERTIFIED)
-            launch_amips_soa_cert(dT, (int64_t)n, mode, E, J, H, F, c->counters, c->stream);
+            launch_amips_soa_cert(dT, (int64_t)n, mode, E, J, H, F, c->counters, c->stream, c->energy_form);
         else
             launch_amips_soa(dT, (int64_t)n, mode, E, J, H, F, c->counters + kCntExactOrient,
-                             c->stream);
+                             c->stream, c->energy_form);
         if (E) cudaMemcpyAsync(r.out0, dE, 8 * n, cudaMemcpyDeviceToHost, c->stream);
         if (J) cudaMemcpyAsync(r.out1, dJ, 24 * n, cudaMemcpyDeviceToHost, c->stream);
         if (H) cudaMemcpyAsync(r.out2, dH, 72 * n, cudaMemcpyDeviceToHost, c->stream);
