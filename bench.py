@@ -65,6 +65,86 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event (throttle) reasons read through NVML (the driver's
+    libnvidia-ml, by ctypes) every 2 ms during the timed region: a timed region of
+    tens of milliseconds still gets a record of several samples.  Reads only."""
+
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+    PERIOD_S = 0.002
+
+    def __init__(self, device: int, lib=None):
+        import ctypes
+
+        self.device = device
+        self.samples = []   # (sm_mhz, reasons bitmask)
+        self.sm_max = None
+        self.ok = False
+        self._stop = threading.Event()
+        if device < 0:
+            return
+        try:
+            L = lib or ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return
+        self.L = L
+        self.h = ctypes.c_void_p()
+        if L.nvmlInit_v2() != 0:
+            return
+        if L.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device), ctypes.byref(self.h)) != 0:
+            L.nvmlShutdown()
+            return
+        self._reasons = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(L, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        mx = ctypes.c_uint()
+        if L.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0:   # NVML_CLOCK_SM
+            self.sm_max = float(mx.value)
+        self.ok = self._reasons is not None
+
+    def _run(self):
+        import ctypes
+
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if (self.L.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(clk)) == 0 and
+                    self._reasons(self.h, ctypes.byref(rs)) == 0):
+                self.samples.append((float(clk.value), int(rs.value)))
+            time.sleep(self.PERIOD_S)
+
+    def __enter__(self):
+        if self.ok:
+            self.t = threading.Thread(target=self._run, daemon=True)
+            self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        if self.ok:
+            self._stop.set()
+            self.t.join(timeout=2)
+            self.L.nvmlShutdown()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.sm_max, "reasons": [], "samples": 0,
+                    "source": "nvml"}
+        reasons = set()
+        for _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(c for c, _ in self.samples),
+                "sm_max_mhz": self.sm_max, "reasons": sorted(reasons),
+                "samples": len(self.samples), "source": "nvml, every 2 ms"}
+
+
+def clock_sampler(device: int):
+    """NVML sampling when the driver library is loadable, else nvidia-smi."""
+    s = NvmlClockSampler(device)
+    return s if s.ok else ClockSampler(device)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -141,13 +221,15 @@ def make_inputs(seed=0):
     return T, V, F, P
 
 
-def cpu_baseline(T, V, F, P, nthreads):
+def cpu_baseline(T, V, F, P, nthreads, frac=1):
     """The reference's own CPU code when oracle/_ref is built, else the oracle port,
-    on a bounded sample (CPU_SAMPLE_TETS tets + CPU_SAMPLE_POINTS points)."""
+    on a bounded sample (CPU_SAMPLE_TETS tets + CPU_SAMPLE_POINTS points, divided by
+    frac)."""
     from oracle.oracle import Oracle, RefLib
 
-    Ts = np.ascontiguousarray(T[:, :CPU_SAMPLE_TETS])
-    Ps = np.ascontiguousarray(P[:CPU_SAMPLE_POINTS])
+    nt, npts = CPU_SAMPLE_TETS // frac, CPU_SAMPLE_POINTS // frac
+    Ts = np.ascontiguousarray(T[:, :nt])
+    Ps = np.ascontiguousarray(P[:npts])
     kind = "port"
     try:
         ref = RefLib()
@@ -162,16 +244,16 @@ def cpu_baseline(T, V, F, P, nthreads):
         o.amips_batch_soa(Ts, quality=True, nthreads=nthreads, jacobian=False, hessian=False)
         S.points_out(Ps, EPS * EPS, nthreads=nthreads)
         dt = time.perf_counter() - t0
-        sample = (f"{CPU_SAMPLE_TETS} tets (reference comformalAMIPS E/J/H + oracle exact orientation) "
-                  f"+ {CPU_SAMPLE_POINTS} points (reference isPointOutEnvelop over MeshFacetsAABBWithEps)")
+        sample = (f"{nt} tets (reference comformalAMIPS E/J/H + oracle exact orientation) "
+                  f"+ {npts} points (reference isPointOutEnvelop over MeshFacetsAABBWithEps)")
     else:
         S = o.surface(V, F)
         t0 = time.perf_counter()
         o.amips_batch_soa(Ts, quality=True, nthreads=nthreads)
         S.points_out(Ps, EPS * EPS, nthreads=nthreads)
         dt = time.perf_counter() - t0
-        sample = f"{CPU_SAMPLE_TETS} tets E/J/H + {CPU_SAMPLE_POINTS} points (oracle port)"
-    q = CPU_SAMPLE_TETS + CPU_SAMPLE_POINTS
+        sample = f"{nt} tets E/J/H + {npts} points (oracle port)"
+    q = nt + npts
     return {"value": q / dt, "unit": UNIT, "cores": nthreads, "kind": kind, "sample": sample,
             "seconds": dt}
 
@@ -288,7 +370,7 @@ def run_ours(args):
         ctx.set_tuning(ctx.TUNE_TIME_KERNELS, 1)   # events around the point-test kernel itself
         barrier(ws)
         torch.cuda.synchronize()
-        with ClockSampler(dev if clocks else -1) as clk:
+        with clock_sampler(dev if clocks else -1) as clk:
             t0 = time.perf_counter()
             for k in range(args.steps):
                 step(evs[k])
@@ -318,8 +400,13 @@ def run_ours(args):
     ctx.set_precision(tw.TW_PRECISION_FP32_CERTIFIED)
     value = cert["value"]
 
-    # e2e: the same step (certified mode) through the C-ABI with pinned host buffers
-    e2e = None if args.no_e2e else run_e2e(ctx, T, P, args, ws)
+    # e2e: the same step through the C-ABI with pinned host buffers, in both modes
+    e2e = e2e_fp64 = None
+    if not args.no_e2e:
+        ctx.set_precision(tw.TW_PRECISION_FP64)
+        e2e_fp64 = run_e2e(ctx, T, P, args, ws, steps=max(3, min(args.steps, 5)))
+        ctx.set_precision(tw.TW_PRECISION_FP32_CERTIFIED)
+        e2e = run_e2e(ctx, T, P, args, ws)
 
     hbm_peak, peak_kind = measured_peaks()
     ma, me = cert["t_amips"], cert["t_env"]
@@ -342,13 +429,20 @@ def run_ours(args):
                    "peak": hbm_peak, "unit": "GB/s", "frac": am_ach / hbm_peak,
                    "traffic": am_tr["bytes_per_unit"] * N_TETS if am_tr else None,
                    "algorithmic_bytes_per_unit": BYTES_PER_TET}]
-    flops_per_tet = 260.0   # FP64 operations per tet (orientation filter + E/J/H), static count
+    # FP64 instructions per tet of the plain kernel in the default (reference) energy
+    # form: 466 distinct operations of E/J/H after common-subexpression elimination
+    # (227 mul, 142 add, 90 sub, 4 div, 3 pow), ~20 per pow (icbrt's two binary64
+    # Newton steps and the exponent correction) and ~30 for the orientation filter;
+    # every one is a separate instruction (no FP contraction), so the pipe's peak is
+    # half its FMA flop rate
+    flops_per_tet = 556.0
     fp64_achieved = flops_per_tet * N_TETS / (plain["t_amips"] * 1e-3) / 1e12
     cst = cert["stats"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": cert["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32-certified+fp64-recheck",
+        "data": "synthetic",
         "config": {"workload": "isolated query batches: energy 4M tets (orientation + AMIPS "
                                "E/J/H) + envelope 10M points vs a 100k-tri displaced sphere, "
                                "eps=1e-3; certified FP32 mode (decisions identical to FP64)",
@@ -360,12 +454,19 @@ def run_ours(args):
         "kernels_ms": {"amips_step": ma, "envelope_step": me,
                        "envelope_point_kernel": cert["t_env_kernel"]},
         "decision_mismatches": cert["mism"],
-        "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_per_step"],
+        "plain_fp64": {"dtype": "f64 (reference energy form)", "value": plain["value"],
+                       "ms_per_step": plain["ms_per_step"],
                        "kernels_ms": {"amips_step": plain["t_amips"],
-                                      "envelope_step": plain["t_env"]},
+                                      "envelope_step": plain["t_env"],
+                                      "envelope_point_kernel": plain["t_env_kernel"]},
                        "decision_mismatches": plain["mism"],
                        "p99_ms": float(np.percentile(plain["step_ms"], 99)),
-                       "speedup_of_value": value / plain["value"]},
+                       "e2e": e2e_fp64,
+                       "speedup_of_value": value / plain["value"],
+                       "speedup_of_e2e": (e2e["value"] / e2e_fp64["value"]
+                                          if e2e and e2e_fp64 else None),
+                       "algorithm": "the same Morton sort and culled grid as the certified "
+                                    "mode, every facet test in FP64"},
         "precision": {"env_facet_tests": cst["env_facet_tests"],
                       "env_facet_fp64": cst["env_facet_fp64"],
                       "env_recheck_fraction": cst["env_facet_fp64"] / max(1, cst["env_facet_tests"]),
@@ -377,13 +478,19 @@ def run_ours(args):
                      "traffic": traffic_bytes, "peak_source": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes_per_unit": dom["per_unit"]},
         "roofline_other": roof_other,
-        "fp64_pipe": {"kernel": "k_amips_soa (plain FP64)", "achieved_tflops": fp64_achieved,
-                      "peak_tflops_measured": fp64_tflops, "frac": fp64_achieved / fp64_tflops,
-                      "flops_per_tet": flops_per_tet, "fp32_peak_tflops_measured": fp32_tflops},
+        "fp64_pipe": {"kernel": "k_amips_soa (plain FP64, reference energy form)",
+                      "achieved_tops": fp64_achieved,
+                      "peak_tops_measured": fp64_tflops / 2,
+                      "frac": fp64_achieved / (fp64_tflops / 2),
+                      "ops_per_tet": flops_per_tet, "fma_peak_tflops_measured": fp64_tflops,
+                      "fp32_peak_tflops_measured": fp32_tflops,
+                      "note": "binary64 instructions/s against the measured FMA issue rate "
+                              "(half the FMA flop rate): no FP contraction, one op each"},
         "e2e": e2e,
-        "gpu_launches": 4 * args.steps,
-        "gpu_launches_note": "per step: k_amips_soa_cert(_bulk), k_point_bins, k_point_place, "
-                             "k_env_points_grid (+ a memset and a CUB scan of the bin counts)",
+        "gpu_launches": 5 * args.steps,
+        "gpu_launches_note": "per step: k_amips_soa_cert_bulk, k_amips_recheck, k_point_bins, "
+                             "k_point_place, k_env_points_grid (+ two memsets and a CUB scan of "
+                             "the bin counts)",
         "clocks": cert["clocks"],
         "wall_s_timed": cert["wall"],
     }
@@ -398,6 +505,10 @@ def run_ours(args):
 
         line["cpu_baseline"] = cpu_baseline(T, V, F, P, default_threads())
         line["cpu_baseline"].pop("seconds", None)
+        # the reference's own setting (it has no threads): one thread on a bounded
+        # sample (1/16 of the step)
+        line["cpu_baseline_1thread"] = cpu_baseline(T, V, F, P, 1, frac=16)
+        line["cpu_baseline_1thread"].pop("seconds", None)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -769,9 +880,12 @@ def check_sample(T, P, V, F, dE, dFl, dO, n=20000):
             "energy_bit_identical_fraction": float((gE == E).mean())}
 
 
-def run_e2e(ctx, T, P, args, ws):
+def run_e2e(ctx, T, P, args, ws, steps=None):
+    """The step through the C-ABI host calls (tw_amips_soa, tw_envelope_points) with
+    pinned host buffers, in the context's current precision mode."""
     import tetwild_gb300 as tw
 
+    steps = steps or args.steps
     hT = tw.PinnedArray(T.shape, np.float64)
     hT.array[...] = T
     hP = tw.PinnedArray(P.shape, np.float64)
@@ -792,20 +906,20 @@ def run_e2e(ctx, T, P, args, ws):
                                     oO.array.ctypes.data)
         assert st == 0, st
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, min(args.warmup, 3))):
         step()
     barrier(ws)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     dt = time.perf_counter() - t0
     dt = max_over_ranks(dt, ws)
     for a in (hT, hP, oE, oJ, oH, oF, oO):
         a.free()
-    q = (N_TETS + N_POINTS) * args.steps * ws
+    q = (N_TETS + N_POINTS) * steps * ws
     return {"value": q / dt, "unit": UNIT, "h2d_bytes_per_step": 96 * N_TETS + 24 * N_POINTS,
             "d2h_bytes_per_step": (8 + 24 + 72 + 1) * N_TETS + N_POINTS,
-            "ms_per_step": 1e3 * dt / args.steps}
+            "ms_per_step": 1e3 * dt / steps, "steps": steps}
 
 
 def main():

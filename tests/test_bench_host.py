@@ -59,3 +59,63 @@ def test_clock_record_without_nvidia_smi(tmp_path, monkeypatch):
     with bench.ClockSampler(0) as clk:
         pass
     assert clk.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+class _FakeNvml:
+    """Stands in for libnvidia-ml: a fixed sequence of (SM clock, reasons) readings."""
+
+    def __init__(self, readings, sm_max=2070):
+        self.readings = list(readings)
+        self.sm_max = sm_max
+        self.k = 0
+        self.shutdown = False
+
+    def nvmlInit_v2(self):
+        return 0
+
+    def nvmlShutdown(self):
+        self.shutdown = True
+        return 0
+
+    def nvmlDeviceGetHandleByIndex_v2(self, index, handle):
+        return 0
+
+    def nvmlDeviceGetMaxClockInfo(self, h, kind, out):
+        out._obj.value = self.sm_max
+        return 0
+
+    def nvmlDeviceGetClockInfo(self, h, kind, out):
+        if self.k >= len(self.readings):
+            return 999                      # no more readings: the sample is skipped
+        out._obj.value = self.readings[self.k][0]
+        return 0
+
+    def nvmlDeviceGetCurrentClocksEventReasons(self, h, out):
+        if self.k >= len(self.readings):
+            return 999
+        out._obj.value = self.readings[self.k][1]
+        self.k += 1
+        return 0
+
+
+def test_nvml_clock_record(monkeypatch):
+    """The NVML sampler (every 2 ms): median SM clock, max clock, and the reason bits
+    that were set during the timed region."""
+    import bench
+
+    fake = _FakeNvml([(2070, 0x0), (1995, 0x4), (2040, 0x0), (1500, 0x40)])
+    with bench.NvmlClockSampler(0, lib=fake) as clk:
+        t = time.monotonic()
+        while fake.k < 4 and time.monotonic() - t < 10:
+            time.sleep(0.005)
+    s = clk.summary()
+    assert s["samples"] == 4 and s["sm_mhz"] == 2017.5 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    assert fake.shutdown
+
+
+def test_nvml_clock_record_without_gpu():
+    import bench
+
+    s = bench.NvmlClockSampler(-1)
+    assert not s.ok and s.summary()["samples"] == 0

@@ -62,6 +62,11 @@ __global__ void __launch_bounds__(256) k_amips_soa(const double* __restrict__ T,
 // filter cannot certify takes the FP64 filter (then the exact path), and a tet
 // whose certified energy error exceeds 1e-5 relative is recomputed entirely
 // in FP64 (in the context's energy form).  Outputs are FP64 like k_amips_soa.
+// The FP64 recomputation (about 3e-6 of the tets) is a separate pass: the
+// binary32 kernels append the index of each such tet to a list and write its
+// flip; k_amips_recheck then evaluates the listed tets in FP64 and writes
+// their E / J / H, so the binary32 kernels carry none of the registers of the
+// binary64 evaluation.
 constexpr float kAmipsTol32 = 1e-5f;
 
 // One tet of the certified kernel: coordinates t in, outputs at index i.
@@ -70,7 +75,9 @@ __device__ __forceinline__ void amips_cert_tet(const double* t, int64_t i, int64
                                                double* __restrict__ E, double* __restrict__ J,
                                                double* __restrict__ H,
                                                uint8_t* __restrict__ flip, uint32_t& ntet,
-                                               uint32_t& nfp64, uint32_t& nexact, int form) {
+                                               uint32_t& nfp64, uint32_t& nexact,
+                                               int32_t* __restrict__ recheck,
+                                               unsigned long long* __restrict__ nrecheck) {
     {
         float d1[3], d2[3], d3[3];
 #pragma unroll
@@ -90,38 +97,23 @@ __device__ __forceinline__ void amips_cert_tet(const double* t, int64_t i, int64
         }
         ++ntet;
         Amips32 R = amips_egh32<WJ, WH>(d1, d2, d3, kAmipsTol32);
-        double e, jv[3], hv[9];
-        if (R.ok) {
-            e = f2d_exact(R.E);
-            if (WJ)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) jv[c] = f2d_exact(R.J[c]);
-            if (WH)
-#pragma unroll
-                for (int c = 0; c < 9; ++c) hv[c] = f2d_exact(R.H[c]);
-        } else {
-            ++nfp64;
-            if (WJ || WH)
-                e = amips_egh_f(t, WJ ? jv : nullptr, WH ? hv : nullptr, form);
-            else
-                e = amips_energy_f(t, form);
-        }
-        if (WE) {
-            // a certified binary32 energy is finite and positive: only the
-            // orientation part of the sentinel rule can apply
-            if (R.ok)
-                E[i] = (QUAL && ori != 1) ? kMaxEnergy : e;
-            else
-                E[i] = QUAL ? quality_from(ori, e) : e;
-        }
         if (WF) flip[i] = (uint8_t)(ori != 1);
+        if (!R.ok) {
+            // E / J / H of this tet come from k_amips_recheck
+            ++nfp64;
+            recheck[atomicAdd(nrecheck, 1ULL)] = (int32_t)i;
+            return;
+        }
+        // a certified binary32 energy is finite and positive: only the
+        // orientation part of the sentinel rule can apply
+        if (WE) E[i] = (QUAL && ori != 1) ? kMaxEnergy : f2d_exact(R.E);
         if (WJ) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = f2d_exact(R.J[c]);
         }
         if (WH) {
 #pragma unroll
-            for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+            for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = f2d_exact(R.H[c]);
         }
     }
 }
@@ -142,6 +134,29 @@ __device__ __forceinline__ void flush_amips_stats(uint32_t ntet, uint32_t nfp64,
     }
 }
 
+// FP64 pass over the tets the binary32 kernels listed (in any order): E (with
+// the calTetQuality_AMIPS sentinel in quality mode), J and H in the context's
+// energy form.  The list length is read on the device.
+__global__ void __launch_bounds__(128) k_amips_recheck(
+    const double* __restrict__ T, int64_t n, const int32_t* __restrict__ recheck,
+    const unsigned long long* __restrict__ nrecheck, double* __restrict__ E,
+    double* __restrict__ J, double* __restrict__ H, int qual, int form) {
+    const int64_t m = (int64_t)*nrecheck;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += stride) {
+        const int64_t i = recheck[k];
+        double t[12], jv[3], hv[9];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) t[c] = T[(int64_t)c * n + i];
+        const double e = amips_egh_f(t, J ? jv : nullptr, H ? hv : nullptr, form);
+        if (E) E[i] = qual ? quality_from(orient3d(t, t + 3, t + 6, t + 9), e) : e;
+        if (J)
+            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+        if (H)
+            for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+    }
+}
+
 template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
 __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict__ T, int64_t n,
                                                         double* __restrict__ E,
@@ -149,7 +164,8 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
                                                         double* __restrict__ H,
                                                         uint8_t* __restrict__ flip,
                                                         unsigned long long* __restrict__ counters,
-                                                        int form) {
+                                                        int32_t* __restrict__ recheck,
+                                                        unsigned long long* __restrict__ nrecheck) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     uint32_t ntet = 0, nfp64 = 0, nexact = 0;
@@ -160,7 +176,8 @@ __global__ void __launch_bounds__(256) k_amips_soa_cert(const double* __restrict
         double t[12];
 #pragma unroll
         for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
-        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, form);
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, recheck,
+                                             nrecheck);
     }
     flush_amips_stats(ntet, nfp64, nexact, counters);
 }
@@ -253,7 +270,7 @@ template <bool WE, bool WJ, bool WH, bool WF, bool QUAL>
 __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
     const double* __restrict__ T, int64_t n, double* __restrict__ E, double* __restrict__ J,
     double* __restrict__ H, uint8_t* __restrict__ flip, unsigned long long* __restrict__ counters,
-    int form) {
+    int32_t* __restrict__ recheck, unsigned long long* __restrict__ nrecheck) {
     extern __shared__ __align__(128) double stage_mem[];   // kBulkStages x 12 x kBulkTile
     double(*stage)[12 * kBulkTile] = reinterpret_cast<double(*)[12 * kBulkTile]>(stage_mem);
     __shared__ __align__(8) uint64_t bar[kBulkStages];
@@ -318,7 +335,8 @@ __global__ void __launch_bounds__(kBulkTile, 2) k_amips_soa_cert_bulk(
 #pragma unroll
             for (int c = 0; c < 12; ++c) t[c] = __ldg(T + (int64_t)c * n + i);
         }
-        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, form);
+        amips_cert_tet<WE, WJ, WH, WF, QUAL>(t, i, n, E, J, H, flip, ntet, nfp64, nexact, recheck,
+                                             nrecheck);
     }
     flush_amips_stats(ntet, nfp64, nexact, counters);
 }
@@ -358,6 +376,8 @@ int grid_for(int64_t n, int block, int blocks_per_sm) {
 
 using AmipsKernel = void (*)(const double*, int64_t, double*, double*, double*, uint8_t*,
                              unsigned long long*, int);
+using AmipsCertKernel = void (*)(const double*, int64_t, double*, double*, double*, uint8_t*,
+                                 unsigned long long*, int32_t*, unsigned long long*);
 
 template <int BITS>
 static AmipsKernel pick_amips() {
@@ -383,32 +403,38 @@ void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J
 }
 
 template <int BITS>
-static AmipsKernel pick_amips_cert() {
+static AmipsCertKernel pick_amips_cert() {
     return k_amips_soa_cert<(BITS & 1) != 0, (BITS & 2) != 0, (BITS & 4) != 0, (BITS & 8) != 0,
                             (BITS & 16) != 0>;
 }
 
 template <int... B>
-static AmipsKernel amips_cert_table(int bits, std::integer_sequence<int, B...>) {
-    static const AmipsKernel table[] = {pick_amips_cert<B>()...};
+static AmipsCertKernel amips_cert_table(int bits, std::integer_sequence<int, B...>) {
+    static const AmipsCertKernel table[] = {pick_amips_cert<B>()...};
     return table[bits];
 }
 
 template <int BITS>
-static AmipsKernel pick_amips_bulk() {
+static AmipsCertKernel pick_amips_bulk() {
     return k_amips_soa_cert_bulk<(BITS & 1) != 0, (BITS & 2) != 0, (BITS & 4) != 0,
                                  (BITS & 8) != 0, (BITS & 16) != 0>;
 }
 
 template <int... B>
-static AmipsKernel amips_bulk_table(int bits, std::integer_sequence<int, B...>) {
-    static const AmipsKernel table[] = {pick_amips_bulk<B>()...};
+static AmipsCertKernel amips_bulk_table(int bits, std::integer_sequence<int, B...>) {
+    static const AmipsCertKernel table[] = {pick_amips_bulk<B>()...};
     return table[bits];
 }
 
 void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                           uint8_t* flip, unsigned long long* counters, cudaStream_t s, int form) {
+                           uint8_t* flip, unsigned long long* counters, void* recheck_scratch,
+                           cudaStream_t s, int form) {
     if (n <= 0) return;
+    // recheck list: a count (zeroed here) and n indices
+    auto* nrecheck = static_cast<unsigned long long*>(recheck_scratch);
+    int32_t* recheck = reinterpret_cast<int32_t*>(static_cast<char*>(recheck_scratch) + 256);
+    cudaMemsetAsync(nrecheck, 0, sizeof(unsigned long long), s);
+    const bool qual = (mode == TW_ENERGY_QUALITY && E);
     int bits = (E ? 1 : 0) | (J ? 2 : 0) | (H ? 4 : 0) | (flip ? 8 : 0) |
                ((mode == TW_ENERGY_QUALITY && E) ? 16 : 0);
     // bulk staging needs every row segment 16-byte aligned and is worth it
@@ -419,7 +445,7 @@ void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, doub
                             a.type == cudaMemoryTypeDevice;
     if (!device_mem) cudaGetLastError();
     if (device_mem && n % 2 == 0 && ((uintptr_t)T & 15) == 0 && n >= 64 * kBulkTile) {
-        AmipsKernel k = amips_bulk_table(bits, std::make_integer_sequence<int, 32>{});
+        AmipsCertKernel k = amips_bulk_table(bits, std::make_integer_sequence<int, 32>{});
         const int smem = kBulkStages * 12 * kBulkTile * (int)sizeof(double);
         // the shared-memory limit is a per-device attribute of the kernel
         const int dev = current_device();
@@ -429,14 +455,20 @@ void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, doub
                 cudaSuccess)
                 g_bulk_attr_set[dev].fetch_or(bit, std::memory_order_acq_rel);
         }
-        k<<<grid_for(n, kBulkTile, 2), kBulkTile, smem, s>>>(T, n, E, J, H, flip, counters, form);
-        return;
+        k<<<grid_for(n, kBulkTile, 2), kBulkTile, smem, s>>>(T, n, E, J, H, flip, counters,
+                                                             recheck, nrecheck);
+    } else {
+        AmipsCertKernel k = amips_cert_table(bits, std::make_integer_sequence<int, 32>{});
+        const int block = 256;
+        k<<<grid_for(n, block, 8), block, 0, s>>>(T, n, E, J, H, flip, counters, recheck,
+                                                   nrecheck);
     }
-    AmipsKernel k = amips_cert_table(bits, std::make_integer_sequence<int, 32>{});
-    const int block = 256;
-    int grid = grid_for(n, block, 8);
-    k<<<grid, block, 0, s>>>(T, n, E, J, H, flip, counters, form);
+    if (E || J || H)
+        k_amips_recheck<<<grid_for(n, 128, 1), 128, 0, s>>>(T, n, recheck, nrecheck, E, J, H,
+                                                            qual ? 1 : 0, form);
 }
+
+size_t amips_recheck_scratch_bytes(int64_t n) { return 256 + 4 * (size_t)(n > 0 ? n : 0); }
 
 __global__ void __launch_bounds__(256) k_tet_quality_idx(
     const int4* __restrict__ tets, int64_t n, const double* __restrict__ vx,

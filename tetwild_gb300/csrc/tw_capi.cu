@@ -176,6 +176,13 @@ __global__ void k_check_ids(const int32_t* __restrict__ ids, int64_t n, int32_t 
     if (v < 0 || v >= lim) atomicExch(bad, 1);
 }
 
+int amips_recheck_scratch(tw_ctx* c, int64_t n, int parts, char** out) {
+    void* p = nullptr;
+    int st = ensure(c, 9, (size_t)parts * amips_recheck_scratch_bytes(n), &p);
+    *out = static_cast<char*>(p);
+    return st;
+}
+
 }  // namespace tw
 
 using namespace tw;
@@ -446,10 +453,16 @@ int tw_amips_soa_device(tw_ctx* c, const double* T, int64_t n, int mode, double*
     if (mode != TW_ENERGY_RAW && mode != TW_ENERGY_QUALITY)
         return fail(c, TW_ERR_ARG, "tw_amips: unknown mode");
     Guard g(c->device);
-    if (c->precision == TW_PRECISION_FP32_CERTIFIED)
-        launch_amips_soa_cert(T, n, mode, E, J, H, flip, c->counters, c->stream, c->energy_form);
-    else
-        launch_amips_soa(T, n, mode, E, J, H, flip, c->counters + kCntExactOrient, c->stream, c->energy_form);
+    if (c->precision == TW_PRECISION_FP32_CERTIFIED) {
+        char* rs = nullptr;
+        int st = amips_recheck_scratch(c, n, 1, &rs);
+        if (st != TW_OK) return st;
+        launch_amips_soa_cert(T, n, mode, E, J, H, flip, c->counters, rs, c->stream,
+                              c->energy_form);
+    } else {
+        launch_amips_soa(T, n, mode, E, J, H, flip, c->counters + kCntExactOrient, c->stream,
+                         c->energy_form);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "tw_amips_soa_device");
     return TW_OK;
@@ -470,10 +483,14 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
         const void* dH = pinned_device_ptr(H);
         const void* dF = pinned_device_ptr(flip);
         if (dT && (!E || dE) && (!J || dJ) && (!H || dH) && (!flip || dF)) {
-            if (c->precision == TW_PRECISION_FP32_CERTIFIED)
+            if (c->precision == TW_PRECISION_FP32_CERTIFIED) {
+                char* rs = nullptr;
+                int st = amips_recheck_scratch(c, n, 1, &rs);
+                if (st != TW_OK) return st;
                 launch_amips_soa_cert((const double*)dT, n, mode, (double*)dE, (double*)dJ,
-                                      (double*)dH, (uint8_t*)dF, c->counters, c->stream, c->energy_form);
-            else
+                                      (double*)dH, (uint8_t*)dF, c->counters, rs, c->stream,
+                                      c->energy_form);
+            } else
                 launch_amips_soa((const double*)dT, n, mode, (double*)dE, (double*)dJ,
                                  (double*)dH, (uint8_t*)dF, c->counters + kCntExactOrient,
                                  c->stream, c->energy_form);
@@ -496,6 +513,11 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
         dH[k] = H ? (double*)q : nullptr; q += H ? 72 * (size_t)C : 0;
         dF[k] = flip ? (uint8_t*)q : nullptr;
     }
+    char* rs = nullptr;
+    if (c->precision == TW_PRECISION_FP32_CERTIFIED) {
+        int st = amips_recheck_scratch(c, C, kNumPipe, &rs);
+        if (st != TW_OK) return st;
+    }
     int64_t chunk = 0;
     for (int64_t i0 = 0; i0 < n; i0 += C, ++chunk) {
         const int k = (int)(chunk % kNumPipe);
@@ -505,7 +527,8 @@ int tw_amips_soa(tw_ctx* c, const double* T, int64_t n, int mode, double* E, dou
             cudaMemcpyAsync(dT[k] + comp * len, T + comp * n + i0, 8 * (size_t)len,
                             cudaMemcpyHostToDevice, s);
         if (c->precision == TW_PRECISION_FP32_CERTIFIED)
-            launch_amips_soa_cert(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters, s, c->energy_form);
+            launch_amips_soa_cert(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k], c->counters,
+                                  rs + k * amips_recheck_scratch_bytes(C), s, c->energy_form);
         else
             launch_amips_soa(dT[k], len, mode, dE[k], dJ[k], dH[k], dF[k],
                              c->counters + kCntExactOrient, s, c->energy_form);

@@ -359,10 +359,15 @@ __global__ void __launch_bounds__(128, MINB) k_env_points_warp(const double* __r
 }
 
 // ---------------------------------------------------------------------------
-// Certified test through the uniform grid: the leaves listed in the point's
-// own cell (see EnvGrid) are every leaf within its culling radius, so the
-// point is in iff one of them tests in.  No tree walk; the lanes of a warp
-// loop over their own lists in step.
+// Test through the uniform grid: the leaves listed in the point's own cell
+// (see EnvGrid) are every leaf within its culling radius, so the point is in
+// iff one of them tests in.  No tree walk; the lanes of a warp loop over
+// their own lists in step.  Both precision modes use it: CERT tests each leaf
+// with the certified binary32 bounds (FP64 in the band), !CERT tests each
+// leaf in FP64.  A leaf whose FP64 distance tests <= eps2 lies within
+// eps (1 + 2^-50) + O(2^-52 M) of the point, well inside the culling radius
+// R = eps (1 + 2^-18) + 2^-17 M the cell lists cover, so both decide exactly
+// as the FP64 tree walk (some facet with computed d^2 <= eps2).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void grid_cell_range(const EnvTree& T, const CertQuery& q,
                                                 uint32_t& b, uint32_t& e) {
@@ -392,7 +397,15 @@ __device__ __forceinline__ void grid_cell_range(const EnvTree& T, const CertQuer
     }
 }
 
+__device__ __forceinline__ bool fp64_leaf_within(const double* __restrict__ tri, int32_t lf,
+                                                 const V3& p, double eps2, TravStats& st) {
+    ++st.facets;
+    ++st.fp64;
+    return leaf_sqdist(tri, lf, p) <= eps2;
+}
+
 // in iff a leaf of the point's cell tests in; every lane of the warp calls it
+template <bool CERT>
 __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams& E, bool valid,
                                               const V3& p, const CertQuery& q, TravStats& st) {
     uint32_t b = 0, e = 0;
@@ -403,7 +416,8 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
     int32_t lf = b < e ? __ldg(T.glist + b) : 0;
     for (uint32_t k = b; k < e; ++k) {
         const int32_t next = k + 1 < e ? __ldg(T.glist + k + 1) : 0;
-        if (cert_leaf_within(T.cull, T.tri, lf, p, q, E.eps2, st)) {
+        if (CERT ? cert_leaf_within(T.cull, T.tri, lf, p, q, E.eps2, st)
+                 : fp64_leaf_within(T.tri, lf, p, E.eps2, st)) {
             in = true;
             break;
         }
@@ -415,7 +429,7 @@ __device__ __forceinline__ bool grid_point_in(const EnvTree& T, const EpsParams&
 // Block b's warps take 32-point groups b*W .. b*W+W-1 together (W warps per
 // block), then stride by the grid: in Morton order the warps of a block test
 // neighbouring cells at the same time and share their facet records in L1.
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, bool CERT>
 __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_grid(const double* __restrict__ P,
                                                            const int32_t* __restrict__ order,
                                                            int64_t n, EnvTree T, EpsParams E,
@@ -434,7 +448,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_grid(const double* _
             const int64_t j = order ? (int64_t)__ldcs(order + i) : i;
             const V3 p{__ldcs(P + 3 * j), __ldcs(P + 3 * j + 1), __ldcs(P + 3 * j + 2)};
             const CertQuery q = cert_query(p, E, T.scale_hi);
-            __stcs(out + j, (uint8_t)!grid_point_in(T, E, true, p, q, st));
+            __stcs(out + j, (uint8_t)!grid_point_in<CERT>(T, E, true, p, q, st));
             ++nq;
         }
     }
@@ -762,25 +776,29 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     // registers), measured best of 1, 6 and 8 on the 10M-point workload (8
     // spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (precision == TW_PRECISION_FP32_CERTIFIED && T.gslot) {
+    if (T.gslot && precision == TW_PRECISION_FP32_CERTIFIED) {
         // 768 resident threads per SM (85 registers) in every block shape
         switch (point_block) {
         case 256:
-            k_env_points_grid<256, 3><<<grid_for(n, 256, 8), 256, 0, s>>>(P, order, n, T, E, out,
-                                                                        counters);
+            k_env_points_grid<256, 3, true><<<grid_for(n, 256, 8), 256, 0, s>>>(P, order, n, T,
+                                                                               E, out, counters);
             break;
         case 128:
-            k_env_points_grid<128, 6><<<grid_for(n, 128, 16), 128, 0, s>>>(P, order, n, T, E, out,
-                                                                         counters);
+            k_env_points_grid<128, 6, true><<<grid_for(n, 128, 16), 128, 0, s>>>(P, order, n, T,
+                                                                                E, out, counters);
             break;
         case 768:
-            k_env_points_grid<768, 1><<<grid_for(n, 768, 3), 768, 0, s>>>(P, order, n, T, E, out,
-                                                                        counters);
+            k_env_points_grid<768, 1, true><<<grid_for(n, 768, 3), 768, 0, s>>>(P, order, n, T,
+                                                                               E, out, counters);
             break;
         default:   // 384: measured best of the four on 10M points (1.11 vs 1.15 ms at 128)
-            k_env_points_grid<384, 2><<<grid_for(n, 384, 6), 384, 0, s>>>(P, order, n, T, E, out,
-                                                                        counters);
+            k_env_points_grid<384, 2, true><<<grid_for(n, 384, 6), 384, 0, s>>>(P, order, n, T,
+                                                                               E, out, counters);
         }
+    } else if (T.gslot) {
+        // FP64 through the same sort and grid
+        k_env_points_grid<384, 2, false><<<grid_for(n, 384, 6), 384, 0, s>>>(P, order, n, T, E,
+                                                                            out, counters);
     }
     else if (precision == TW_PRECISION_FP32_CERTIFIED && order)
         k_env_points_warp<6><<<grid_for(n, block, 16), block, 0, s>>>(P, order, n, T, E, out,
@@ -1024,10 +1042,10 @@ __device__ __forceinline__ uint8_t env_face_samples(const SampleHeader& h, const
         }
         // out iff the lane's sample (have) is out; called by the whole warp
         auto lane_out = [&](bool have, const V3& p) -> bool {
-            if (FP32 && F.T.gslot) {
+            if (F.T.gslot) {
                 CertQuery q;
                 if (have) q = cert_query(p, F.E, F.T.scale_hi);
-                return have && !grid_point_in(F.T, F.E, have, p, q, st);
+                return have && !grid_point_in<FP32>(F.T, F.E, have, p, q, st);
             }
             if (cnt < 0) {
                 bool o = false;
@@ -1326,9 +1344,9 @@ __global__ void __launch_bounds__(128) k_env_points_segs(const double* __restric
             const EnvTree T = g.T;
             const EpsParams E = g.E;
             V3 p{__ldg(P + 3 * i), __ldg(P + 3 * i + 1), __ldg(P + 3 * i + 2)};
-            if (FP32 && T.gslot) {
+            if (T.gslot) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
-                out[i] = (uint8_t)!grid_point_in(T, E, true, p, q, st);
+                out[i] = (uint8_t)!grid_point_in<FP32>(T, E, true, p, q, st);
             } else {
                 int32_t f = query_point<FP32>(T, p, E, st);
                 if (f == kTraversalError) atomicOr(counters + kCntError, 1ULL);
@@ -1775,9 +1793,9 @@ __global__ void k_collapse_points(EnvTree Tin, EnvTree Tb, EpsParams E,
                 break;
             }
             int32_t f;
-            if (FP32 && T.gslot) {
+            if (T.gslot) {
                 const CertQuery q = cert_query(p, E, T.scale_hi);
-                f = grid_point_in(T, E, true, p, q, st) ? 0 : -1;
+                f = grid_point_in<FP32>(T, E, true, p, q, st) ? 0 : -1;
             } else {
                 f = query_point<FP32>(T, p, E, st);
             }

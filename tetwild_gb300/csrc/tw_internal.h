@@ -186,10 +186,17 @@ int grid_for(int64_t n, int block, int blocks_per_sm);
 void launch_amips_soa(const double* T, int64_t n, int mode, double* E, double* J, double* H,
                       uint8_t* flip, unsigned long long* exact_count, cudaStream_t s,
                       int form = TW_ENERGY_FORM_REFERENCE);
-// certified binary32 variant; counters is the context's counter array
+// certified binary32 variant; counters is the context's counter array;
+// recheck_scratch: amips_recheck_scratch_bytes(n) device bytes (256-byte
+// aligned) for the list of tets recomputed in FP64 (none may share it while
+// the launch runs)
 void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, double* J, double* H,
-                           uint8_t* flip, unsigned long long* counters, cudaStream_t s,
-                           int form = TW_ENERGY_FORM_REFERENCE);
+                           uint8_t* flip, unsigned long long* counters, void* recheck_scratch,
+                           cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
+size_t amips_recheck_scratch_bytes(int64_t n);
+// the context's recheck scratch (slot 9) for `parts` concurrent launches of
+// up to n tets each; part k starts at *out + k * amips_recheck_scratch_bytes(n)
+int amips_recheck_scratch(tw_ctx* c, int64_t n, int parts, char** out);
 void launch_tet_quality_idx(const int32_t* tets, int64_t n, const double* vx, const double* vy,
                             const double* vz, const uint8_t* rounded, double* E, uint8_t* flip,
                             uint8_t* needs_host, unsigned long long* counters, cudaStream_t s,

@@ -222,6 +222,14 @@ int launch_amips(const BatchParams& P, Lane& L, std::vector<Req*>& B) {
     void* p;
     int st = ensure(c, 0, bytes, &p);
     if (st != TW_OK) return st;
+    // the requests of a batch run one after another on the lane's stream, so
+    // they share the lane's recheck list (sized for the largest)
+    char* rs = nullptr;
+    if (P.precision == TW_PRECISION_FP32_CERTIFIED) {
+        int64_t max_n = 0;
+        for (Req* rq : B) max_n = std::max<int64_t>(max_n, rq->r.n);
+        if ((st = amips_recheck_scratch(c, max_n, 1, &rs)) != TW_OK) return st;
+    }
     char* q = (char*)p;
     for (Req* rq : B) {
         const tw_request& r = rq->r;
@@ -240,7 +248,8 @@ int launch_amips(const BatchParams& P, Lane& L, std::vector<Req*>& B) {
         double* H = r.out2 ? dH : nullptr;
         uint8_t* F = r.out3 ? dF : nullptr;
         if (P.precision == TW_PRECISION_FP32_CERTIFIED)
-            launch_amips_soa_cert(dT, (int64_t)n, mode, E, J, H, F, c->counters, c->stream, c->energy_form);
+            launch_amips_soa_cert(dT, (int64_t)n, mode, E, J, H, F, c->counters, rs, c->stream,
+                                  c->energy_form);
         else
             launch_amips_soa(dT, (int64_t)n, mode, E, J, H, F, c->counters + kCntExactOrient,
                              c->stream, c->energy_form);
