@@ -39,6 +39,32 @@ def test_certified_points_displaced_sphere(ctx, oracle):
     assert st["env_facet_fp64"] < 0.6 * st["env_facet_tests"]
 
 
+def test_point_kernel_shapes_same_decisions(ctx, oracle):
+    """Every launch shape of the grid point test (blocks of 128, 256, 384, 768) in both
+    precision modes, ragged tails included (n not a multiple of 32), a batch below the
+    sort threshold and a single point: the oracle's decisions."""
+    V, F = syn.displaced_sphere(seed=4)
+    eps = 1e-3
+    P = syn.envelope_points(V, F, 300_007, eps, seed=14)
+    ctx.set_params(eps * eps, eps)
+    ctx.surface_upload(V, F)
+    want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
+    try:
+        for shape in (128, 256, 384, 768):
+            ctx.set_tuning(ctx.TUNE_POINT_BLOCK, shape)
+            a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P))
+            assert np.array_equal(a, want), shape
+            assert np.array_equal(b, want), shape
+            # a batch below the sort threshold (input order) and a one-point batch
+            small = P[:1000]
+            a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(small))
+            assert np.array_equal(a, want[:1000]) and np.array_equal(b, want[:1000])
+            a, b, _ = _both_modes(ctx, lambda: ctx.envelope_points(P[:1]))
+            assert a[0] == want[0] and b[0] == want[0]
+    finally:
+        ctx.set_tuning(ctx.TUNE_POINT_BLOCK, 384)
+
+
 @pytest.mark.parametrize("offset", [0.0, 1000.0])
 def test_certified_points_at_threshold(ctx, oracle, offset):
     V = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.0]]) + offset
