@@ -297,6 +297,10 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
  *   (128, 256, 384 default, or 768; 768 resident threads per SM in each): the
  *   warps of a block test neighbouring sorted points together.  Results never
  *   depend on it.
+ * TW_TUNE_SMOOTH_FUSED: 1 (default) runs a smoothing pass (tw_smooth_stars*)
+ *   as one persistent kernel; 0 as five stage kernels (validity and Newton,
+ *   projection, flip / quality / face list, face samples, decisions).
+ *   Results never depend on it.
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.
@@ -305,6 +309,7 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 #define TW_TUNE_SORT_POINTS 1
 #define TW_TUNE_TIME_KERNELS 2
 #define TW_TUNE_POINT_BLOCK 3
+#define TW_TUNE_SMOOTH_FUSED 4
 TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
 TW_API int tw_kernel_times(tw_ctx* ctx, float* ms, int max, int* count);
 

@@ -68,8 +68,11 @@ def _oracle_pass(oracle, sphere, batch, max_step, max_it, boundary=None):
                                nthreads=8)
 
 
+@pytest.mark.parametrize("fused", [1, 0])
 @pytest.mark.parametrize("precision", [tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED])
-def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision):
+def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision, fused):
+    """One pass over 3000 mixed stars, as one persistent kernel (fused=1) and as the
+    five stage kernels (fused=0): every status and position bit for bit."""
     batch = _mixed(sphere, 3000, seed=5)
     xyz, off, tets, ff, cen, kinds = batch
     want, wst = _oracle_pass(oracle, sphere, batch, 1, 8)
@@ -79,12 +82,53 @@ def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision):
     ctx.surface_upload(*sphere)
     ctx.mesh_upload(xyz)
     ctx.set_precision(precision)
+    ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
     try:
         out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
     finally:
         ctx.set_precision(tw.TW_PRECISION_FP64)
+        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
     assert np.array_equal(st.astype(np.int8), wst)
     assert np.array_equal(out, want)
+
+
+def _large_stars(sphere):
+    """Eight surface stars of 400 tets with every face flagged a surface face: 600 faces
+    through each centre, more than one listing window of the fused kernel (288).  Four
+    stars of radius 2e-4 (inside the envelope: two pass every face), four of 4e-3."""
+    V, F = sphere
+    cp = V[np.random.default_rng(9).choice(len(V), 8, replace=False)]
+    parts = [syn.star_batch(4, seed=9 + k, mean_tets=400, lo=400, hi=400, radius=r,
+                            centres=cp[4 * k:4 * k + 4], jitter_rel=0.01)
+             for k, r in enumerate((2e-4, 4e-3))]
+    nv0 = len(parts[0][0])
+    xyz = np.vstack([parts[0][0], parts[1][0]])
+    off = np.concatenate([parts[0][1], parts[1][1][1:] + parts[0][1][-1]]).astype(np.int32)
+    tets = np.vstack([parts[0][2], parts[1][2] + nv0]).astype(np.int32)
+    cen = np.concatenate([parts[0][3], parts[1][3] + nv0]).astype(np.int32)
+    ff = np.full(len(tets), 15, np.uint8)
+    return xyz, off, tets, ff, cen, np.ones(len(cen), np.uint8)
+
+
+def test_smooth_pass_large_stars(ctx, oracle, sphere):
+    batch = _large_stars(sphere)
+    xyz, off, tets, ff, cen, kinds = batch
+    want, wst = _oracle_pass(oracle, sphere, batch, 1, 8)
+    assert (wst == 2).sum() >= 1 and (wst == 5).sum() >= 1, wst
+    ctx.set_params(EPS * EPS, EPS / 2, 1, 8)
+    ctx.surface_upload(*sphere)
+    ctx.mesh_upload(xyz)
+    try:
+        for fused in (1, 0):
+            ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
+            for precision in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
+                ctx.set_precision(precision)
+                out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
+                assert np.array_equal(st.astype(np.int8), wst), (fused, precision)
+                assert np.array_equal(out, want), (fused, precision)
+    finally:
+        ctx.set_precision(tw.TW_PRECISION_FP64)
+        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
 
 
 def test_smooth_pass_every_launch_shape(ctx, oracle, sphere):
@@ -95,13 +139,16 @@ def test_smooth_pass_every_launch_shape(ctx, oracle, sphere):
     ctx.surface_upload(*sphere)
     ctx.mesh_upload(xyz)
     try:
-        for shape in range(ctx.NEWTON_SHAPES):
-            ctx.set_newton_shape(shape)
-            out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
-            assert np.array_equal(st.astype(np.int8), wst), shape
-            assert np.array_equal(out, want), shape
+        for fused in (1, 0):
+            ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
+            for shape in range(ctx.NEWTON_SHAPES):
+                ctx.set_newton_shape(shape)
+                out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
+                assert np.array_equal(st.astype(np.int8), wst), (fused, shape)
+                assert np.array_equal(out, want), (fused, shape)
     finally:
         ctx.set_newton_shape(5)
+        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
 
 
 def test_smooth_boundary_stars_use_boundary_surface(ctx, oracle, sphere):
