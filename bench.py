@@ -528,7 +528,6 @@ def run_batching(ctx, V, F, args, dev, ws):
     half on the 100k-tri displaced sphere), tets per star Poisson(24) clamped to [4, 96] (surface
     stars [6, 96]); one Newton step with at most 8 backtracking trials, inversion checks, and
     for surface stars the projection, quality and one-ring face-envelope checks.  The pass is
-    one persistent kernel (k_smooth_fused; the five-kernel staged pass is timed beside it),
     autotuned over the launch shapes, captured in a CUDA graph and replayed; every replay is
     timed with CUDA events on the context stream.  Both precision modes are checked against the
     oracle over the whole batch (status and position bit for bit), and the oracle pass is timed
@@ -594,35 +593,12 @@ def run_batching(ctx, V, F, args, dev, ws):
         ms = [e0.elapsed_time(e1) for e0, e1 in evs]
         g.close()
         cst = ctx.stats()
-        # the same pass as five stage kernels, for comparison (same launch shape)
-        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 0)
-        ctx.capture_begin()
-        ctx.smooth_stars_device(*a)
-        g0 = ctx.capture_end()
-        for _ in range(2):
-            g0.launch()
-        ctx.synchronize()
-        st0 = d_st.cpu().numpy().astype(np.int8)
-        out0 = d_out.cpu().numpy().reshape(-1, 3)
-        staged_same = bool(np.array_equal(st0, wst) and np.array_equal(out0, want))
-        ev0 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(3)]
-        for e0, e1 in ev0:
-            e0.record(stream)
-            g0.launch()
-            e1.record(stream)
-        ctx.synchronize()
-        staged_ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev0]))
-        g0.close()
-        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
         dev_ms = max_over_ranks(sum(ms), ws) / args.steps
         modes[name] = {"stars_per_s": ws * ns / (dev_ms * 1e-3), "ms_per_pass": dev_ms,
                        "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
                        "autotuned_shape": best, "shape_ms": ms_shapes, "mismatches": mism,
                        "env_facet_tests": cst["env_facet_tests"],
-                       "env_recheck_fraction": cst["env_facet_fp64"] / max(1, cst["env_facet_tests"]),
-                       "staged_5_kernels_ms_per_pass": staged_ms,
-                       "staged_matches_oracle": staged_same}
+                       "env_recheck_fraction": cst["env_facet_fp64"] / max(1, cst["env_facet_tests"])}
     ctx.set_precision(tw.TW_PRECISION_FP32_CERTIFIED)
     counts = np.bincount(wst.astype(np.int64), minlength=6)
     return {
@@ -638,9 +614,7 @@ def run_batching(ctx, V, F, args, dev, ws):
         "oracle_status_counts": {"invalid": int(counts[0]), "not_moved": int(counts[1]),
                                  "moved": int(counts[2]), "reject_flip": int(counts[3]),
                                  "reject_quality": int(counts[4]), "reject_envelope": int(counts[5])},
-        "gpu_launches_per_pass": 1,
-        "gpu_launches_note": "k_smooth_fused, one persistent kernel (after a memset of its work "
-                             "counter), replayed from a captured CUDA graph",
+        "gpu_launches_per_pass": 5,
         "cpu_baseline": {"value": ns / cpu_s, "unit": "stars/s", "cores": nthreads, "kind": "port",
                          "sample": f"the whole pass ({ns} stars) through the oracle"},
     }

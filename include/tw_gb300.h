@@ -52,6 +52,7 @@ extern "C" {
 #define TW_ERR_NO_MESH (-5)
 #define TW_ERR_TIMEOUT (-6)
 #define TW_ERR_TOO_LARGE (-7)    /* request exceeds a fixed capacity (tw_amips_soa_noalloc) */
+#define TW_ERR_CANCELLED (-8)    /* serving: the request's job was cancelled before it ran  */
 #define TW_BUSY 2                /* serving: not admitted now (memory budget), retry later  */
 
 /* AMIPS output modes */
@@ -297,10 +298,6 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
  *   (128, 256, 384 default, or 768; 768 resident threads per SM in each): the
  *   warps of a block test neighbouring sorted points together.  Results never
  *   depend on it.
- * TW_TUNE_SMOOTH_FUSED: 1 (default) runs a smoothing pass (tw_smooth_stars*)
- *   as one persistent kernel; 0 as five stage kernels (validity and Newton,
- *   projection, flip / quality / face list, face samples, decisions).
- *   Results never depend on it.
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.
@@ -309,7 +306,6 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 #define TW_TUNE_SORT_POINTS 1
 #define TW_TUNE_TIME_KERNELS 2
 #define TW_TUNE_POINT_BLOCK 3
-#define TW_TUNE_SMOOTH_FUSED 4
 TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
 TW_API int tw_kernel_times(tw_ctx* ctx, float* ms, int max, int* count);
 
@@ -452,6 +448,13 @@ TW_API int tw_server_job_mesh(tw_server* srv, int32_t job, const double* xyz, in
 TW_API int tw_server_job_read_mesh(tw_server* srv, int32_t job, double* xyz, double timeout_s);
 /* Waits (at most timeout_s) for the job's requests, then frees its memory. */
 TW_API int tw_server_job_close(tw_server* srv, int32_t job, double timeout_s);
+/* Cancels a job mid-flight: its requests still waiting for a batch complete
+ * at once with TW_ERR_CANCELLED (tw_server_wait returns it; their outputs are
+ * not written), new submissions for it are refused, the batches already on a
+ * lane finish (waited for at most timeout_s), then its memory is freed as by
+ * tw_server_job_close.  On TW_ERR_TIMEOUT the queued requests are cancelled
+ * and the job stays open; call again to free it.  Other jobs are unaffected. */
+TW_API int tw_server_job_cancel(tw_server* srv, int32_t job, double timeout_s);
 TW_API int tw_server_submit(tw_server* srv, int32_t job, const tw_request* req, uint64_t* ticket);
 /* Waits at most timeout_s for the request; returns its status (TW_ERR_TIMEOUT
  * if not done yet: wait again).  latency_ms: submit to completion.          */

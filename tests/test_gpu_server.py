@@ -215,3 +215,51 @@ def test_smooth_apply_updates_the_resident_mesh(workload):
         want = xyz.copy()
         want[cen[moved]] = out[moved]
         assert np.array_equal(now, want)
+
+
+def test_job_cancel_mid_flight(workload):
+    """tw_server_job_cancel: with one lane and a burst of requests queued for job A, the
+    cancel completes A's waiting requests with TW_ERR_CANCELLED at once, lets the batches
+    already on the lane finish (their results correct), frees A's memory and refuses A
+    afterwards; job B's requests, queued among A's, all run and are correct."""
+    jobs, stars, reqs = workload
+    (Va, Fa, ea), (Vb, Fb, eb) = jobs[2], jobs[0]
+    Pa = syn.envelope_points(Va, Fa, 200_000, ea, seed=71)
+    Pb = syn.envelope_points(Vb, Fb, 50_000, eb, seed=72)
+    with tw.Server(0, 0, lanes=1) as srv, tw.Context(0) as ctx:
+        srv.set_params(tw.TW_PRECISION_FP32_CERTIFIED, 1, 8)
+        a = srv.job_open(Va, Fa, ea * ea, ea / 2)
+        b = srv.job_open(Vb, Fb, eb * eb, eb / 2)
+        before = srv.stats()
+        ta, tb = [], []
+        for k in range(300):
+            ta.append(srv.submit_points(a, Pa))
+            if k % 30 == 0:
+                tb.append(srv.submit_points(b, Pb))
+        srv.job_cancel(a)
+        after = srv.stats()
+        assert after["jobs_open"] == before["jobs_open"] - 1
+        assert after["bytes_used"] < before["bytes_used"]
+        ctx.set_params(ea * ea, ea / 2)
+        ctx.surface_upload(Va, Fa)
+        want_a = ctx.envelope_points(Pa)
+        ctx.set_params(eb * eb, eb / 2)
+        ctx.surface_upload(Vb, Fb)
+        want_b = ctx.envelope_points(Pb)
+        statuses = []
+        for t, out in ta:
+            st, _ = srv.wait_status(t)
+            statuses.append(st)
+            assert st in (tw.TW_OK, tw.TW_ERR_CANCELLED)
+            if st == tw.TW_OK:
+                assert np.array_equal(out, want_a)
+        n_cancelled = statuses.count(tw.TW_ERR_CANCELLED)
+        assert 1 <= n_cancelled < len(ta) or statuses.count(tw.TW_OK) == 0, statuses
+        assert n_cancelled >= 1
+        for t, out in tb:
+            srv.wait(t)
+            assert np.array_equal(out, want_b)
+        with pytest.raises(tw.TetWildGpuError):
+            srv.submit_points(a, Pa)                       # the job is gone
+        srv.job_cancel(b)                                  # nothing queued: frees at once
+        assert srv.stats()["jobs_open"] == before["jobs_open"] - 2

@@ -68,11 +68,8 @@ def _oracle_pass(oracle, sphere, batch, max_step, max_it, boundary=None):
                                nthreads=8)
 
 
-@pytest.mark.parametrize("fused", [1, 0])
 @pytest.mark.parametrize("precision", [tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED])
-def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision, fused):
-    """One pass over 3000 mixed stars, as one persistent kernel (fused=1) and as the
-    five stage kernels (fused=0): every status and position bit for bit."""
+def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision):
     batch = _mixed(sphere, 3000, seed=5)
     xyz, off, tets, ff, cen, kinds = batch
     want, wst = _oracle_pass(oracle, sphere, batch, 1, 8)
@@ -82,20 +79,18 @@ def test_smooth_pass_vs_oracle(ctx, oracle, sphere, precision, fused):
     ctx.surface_upload(*sphere)
     ctx.mesh_upload(xyz)
     ctx.set_precision(precision)
-    ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
     try:
         out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
     finally:
         ctx.set_precision(tw.TW_PRECISION_FP64)
-        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
     assert np.array_equal(st.astype(np.int8), wst)
     assert np.array_equal(out, want)
 
 
 def _large_stars(sphere):
     """Eight surface stars of 400 tets with every face flagged a surface face: 600 faces
-    through each centre, more than one listing window of the fused kernel (288).  Four
-    stars of radius 2e-4 (inside the envelope: two pass every face), four of 4e-3."""
+    through each centre.  Four stars of radius 2e-4 (inside the envelope: two pass every
+    face), four of 4e-3."""
     V, F = sphere
     cp = V[np.random.default_rng(9).choice(len(V), 8, replace=False)]
     parts = [syn.star_batch(4, seed=9 + k, mean_tets=400, lo=400, hi=400, radius=r,
@@ -119,16 +114,13 @@ def test_smooth_pass_large_stars(ctx, oracle, sphere):
     ctx.surface_upload(*sphere)
     ctx.mesh_upload(xyz)
     try:
-        for fused in (1, 0):
-            ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
-            for precision in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
-                ctx.set_precision(precision)
-                out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
-                assert np.array_equal(st.astype(np.int8), wst), (fused, precision)
-                assert np.array_equal(out, want), (fused, precision)
+        for precision in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
+            ctx.set_precision(precision)
+            out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
+            assert np.array_equal(st.astype(np.int8), wst), precision
+            assert np.array_equal(out, want), precision
     finally:
         ctx.set_precision(tw.TW_PRECISION_FP64)
-        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
 
 
 def test_smooth_pass_every_launch_shape(ctx, oracle, sphere):
@@ -139,16 +131,13 @@ def test_smooth_pass_every_launch_shape(ctx, oracle, sphere):
     ctx.surface_upload(*sphere)
     ctx.mesh_upload(xyz)
     try:
-        for fused in (1, 0):
-            ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, fused)
-            for shape in range(ctx.NEWTON_SHAPES):
-                ctx.set_newton_shape(shape)
-                out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
-                assert np.array_equal(st.astype(np.int8), wst), (fused, shape)
-                assert np.array_equal(out, want), (fused, shape)
+        for shape in range(ctx.NEWTON_SHAPES):
+            ctx.set_newton_shape(shape)
+            out, st = ctx.smooth_stars(off, tets, cen, ff, kinds)
+            assert np.array_equal(st.astype(np.int8), wst), shape
+            assert np.array_equal(out, want), shape
     finally:
         ctx.set_newton_shape(5)
-        ctx.set_tuning(ctx.TUNE_SMOOTH_FUSED, 1)
 
 
 def test_smooth_boundary_stars_use_boundary_surface(ctx, oracle, sphere):

@@ -31,6 +31,7 @@ TW_ERR_NO_SURFACE = -4
 TW_ERR_NO_MESH = -5
 TW_ERR_TIMEOUT = -6
 TW_ERR_TOO_LARGE = -7
+TW_ERR_CANCELLED = -8
 TW_ENERGY_RAW = 0
 TW_ENERGY_QUALITY = 1
 TW_SURFACE_INPUT = 0
@@ -165,6 +166,7 @@ _SIGS = {
     "tw_server_job_mesh": [_P, _I32, _P, _I32, _D],
     "tw_server_job_read_mesh": [_P, _I32, _P, _D],
     "tw_server_job_close": [_P, _I32, _D],
+    "tw_server_job_cancel": [_P, _I32, _D],
     "tw_server_submit": [_P, _I32, ctypes.POINTER(TwRequest), ctypes.POINTER(ctypes.c_uint64)],
     "tw_server_wait": [_P, ctypes.c_uint64, _D, ctypes.POINTER(_D)],
     "tw_server_get_stats": [_P, ctypes.POINTER(TwServerStats)],
@@ -388,7 +390,6 @@ class Context:
     TUNE_SORT_POINTS = 1
     TUNE_TIME_KERNELS = 2
     TUNE_POINT_BLOCK = 3
-    TUNE_SMOOTH_FUSED = 4
 
     def set_tuning(self, knob: int, value: float):
         """Work-only knobs (TW_TUNE_*): results are the same for every value."""
@@ -711,6 +712,19 @@ class Server:
 
     def job_close(self, job, timeout_s=60.0):
         self._check(self.lib.tw_server_job_close(self.h, job, timeout_s))
+
+    def job_cancel(self, job, timeout_s=60.0):
+        """Cancels the job: queued requests end with TW_ERR_CANCELLED, batches on a lane
+        finish, then its memory is freed."""
+        self._check(self.lib.tw_server_job_cancel(self.h, job, timeout_s))
+
+    def wait_status(self, ticket, timeout_s=60.0):
+        """(status, latency ms) of a request without raising on its status."""
+        lat = _D()
+        st = self.lib.tw_server_wait(self.h, ticket, timeout_s, ctypes.byref(lat))
+        if st != TW_ERR_TIMEOUT:
+            self._keep.pop(ticket, None)
+        return st, lat.value
 
     def _submit(self, job, req, keep):
         t = ctypes.c_uint64()

@@ -358,11 +358,6 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         c->point_block = (int)value;
         return TW_OK;
     }
-    if (knob == TW_TUNE_SMOOTH_FUSED) {
-        if (!(value == 0.0 || value == 1.0)) return fail(c, TW_ERR_ARG, "smooth_fused: 0 or 1");
-        c->smooth_fused = (int)value;
-        return TW_OK;
-    }
     if (knob == TW_TUNE_TIME_KERNELS) {
         c->time_kernels = value != 0.0;
         c->time_count = 0;
@@ -915,17 +910,6 @@ int smooth_scratch(tw_ctx* c, int32_t nstars, int64_t ntets, SmoothScratch& S) {
 void smooth_launch(tw_ctx* c, const int32_t* off, const int32_t* tets, const uint8_t* ff,
                    const int32_t* cen, const uint8_t* kinds, int32_t nstars, bool any_surface,
                    double* out, uint8_t* status, const SmoothScratch& S) {
-    if (c->smooth_fused) {
-        // one persistent kernel; the face counter word serves as its work counter
-        launch_smooth_fused(c->newton_shape, c->vx, c->vy, c->vz, off, tets,
-                            any_surface ? ff : nullptr, cen, any_surface ? kinds : nullptr,
-                            nstars, c->newton_max_step, c->newton_max_it,
-                            c->surf[TW_SURFACE_INPUT], c->surf[TW_SURFACE_BOUNDARY], c->eps2,
-                            c->sampling_dist, c->precision, out, status,
-                            reinterpret_cast<unsigned int*>(S.face_count), c->counters,
-                            c->stream, c->energy_form);
-        return;
-    }
     launch_smooth_stage1(c->newton_shape, c->vx, c->vy, c->vz, off, tets, cen, kinds, nstars,
                          c->newton_max_step, c->newton_max_it, out, S.pnew, status, c->stream, c->energy_form);
     if (!any_surface) return;

@@ -26,7 +26,6 @@
 
 #include "tw_device.cuh"
 #include "tw_internal.h"
-#include "tw_star.cuh"
 
 namespace tw {
 
@@ -1938,277 +1937,6 @@ __global__ void k_sample_triangle(const double* __restrict__ t, double sd, doubl
 void launch_sample_triangle(const double* tri, double sd, double* out, int64_t cap,
                             int64_t* count, cudaStream_t s) {
     k_sample_triangle<<<1, 32, 0, s>>>(tri, sd, out, cap, count);
-}
-
-// ---------------------------------------------------------------------------
-// The smoothing pass in one persistent kernel (VertexSmoother.cpp:114-210,
-// :244-450).  A warp claims 32/G consecutive stars at a time from a work
-// counter.  Each group of G lanes runs its star's validity check and
-// NewtonsMethod (as k_smooth_stage1: interior stars end there).  Then the
-// whole warp finishes the group's surface stars one after another: the
-// projection onto the nearest facet (lane 0, as k_smooth_project), isFlip and
-// the max-quality comparison at the projected position (32 lanes, as
-// k_smooth_stage2), and the one-ring surface faces: compacted into a per-warp
-// list (at most kFusedFaceCap at a time; a larger star is listed again for
-// each window), headers and the exact degeneracy test computed for
-// kFusedHdr faces at a time by as many lanes, each face's samples tested by
-// the warp until the first face out (the decision is "some face out", so the
-// order of the faces changes only the work).  Same statuses and positions as
-// the staged pass.
-// ---------------------------------------------------------------------------
-constexpr int kFusedBlock = 128;
-constexpr int kFusedWarps = kFusedBlock / 32;
-constexpr int kFusedFaceCap = 288;   // faces through the centre of a star of 96 tets
-constexpr int kFusedHdr = 8;
-
-struct FusedArgs {
-    const double* vx;
-    const double* vy;
-    const double* vz;
-    const int32_t* off;
-    const int4* tets;
-    const uint8_t* ff;
-    const int32_t* cen;
-    const uint8_t* kinds;
-    int32_t nstars;
-    int max_step, max_it, form;
-    double* out;
-    uint8_t* status;
-    EnvTree Tin, Tb;
-    EpsParams E;
-    double sd;
-    unsigned long long* counters;
-    unsigned int* work;   // zeroed before the launch
-};
-
-template <int G, bool FP32>
-__global__ void __launch_bounds__(kFusedBlock) k_smooth_fused(FusedArgs A) {
-    __shared__ int2 flist[kFusedWarps][kFusedFaceCap];
-    __shared__ SampleHeader hdr[kFusedWarps][kFusedHdr];
-    __shared__ int hstate[kFusedWarps][kFusedHdr];
-    constexpr int NG = 32 / G;
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gl = lane & (G - 1);
-    const unsigned gm = group_mask<G>(lane);
-    TravStats tst;
-    uint32_t nq = 0;
-    const FaceCtx F{A.Tin, A.E, A.counters};
-    for (;;) {
-        unsigned base = 0;
-        if (lane == 0) base = atomicAdd(A.work, (unsigned)NG);
-        base = __shfl_sync(full, base, 0);
-        if (base >= (unsigned)A.nstars) break;
-        // 1: validity and NewtonsMethod, one star per group
-        const int64_t sid = (int64_t)base + lane / G;
-        int stt = -1;
-        double pos[3] = {0.0, 0.0, 0.0};
-        if (sid < A.nstars) {
-            const int32_t b = A.off[sid], nt = A.off[sid + 1] - b;
-            StarView S{A.vx, A.vy, A.vz, A.tets + b, nt, A.cen[sid], A.form};
-            const double p0[3] = {A.vx[S.v], A.vy[S.v], A.vz[S.v]};
-            pos[0] = p0[0];
-            pos[1] = p0[1];
-            pos[2] = p0[2];
-            const uint8_t kind = A.kinds ? A.kinds[sid] : (uint8_t)TW_STAR_INTERIOR;
-            const bool surface = (kind == TW_STAR_SURFACE || kind == TW_STAR_BOUNDARY);
-            uint8_t st;
-            if (!star_positive<G>(S, p0, gl, gm)) {
-                st = TW_SMOOTH_INVALID;
-            } else if (!newton_group_star<G>(S, pos, A.max_step, A.max_it, gl, gm)) {
-                st = TW_SMOOTH_NOT_MOVED;
-            } else {
-                st = surface ? kSmoothPendingProject : (uint8_t)TW_SMOOTH_MOVED;
-            }
-            if (gl == 0) {
-                const bool moved = (st == TW_SMOOTH_MOVED);
-                A.out[3 * sid] = moved ? pos[0] : p0[0];
-                A.out[3 * sid + 1] = moved ? pos[1] : p0[1];
-                A.out[3 * sid + 2] = moved ? pos[2] : p0[2];
-                if (st != kSmoothPendingProject) A.status[sid] = st;
-            }
-            stt = st;
-        }
-        __syncwarp(full);
-        // 2: the surface stars of this warp, the whole warp on each
-        for (int g = 0; g < NG; ++g) {
-            const int src = g * G;
-            const int64_t s2 = (int64_t)base + g;
-            const int sst = __shfl_sync(full, stt, src);
-            double p[3] = {__shfl_sync(full, pos[0], src), __shfl_sync(full, pos[1], src),
-                           __shfl_sync(full, pos[2], src)};
-            if (s2 >= A.nstars || sst != (int)kSmoothPendingProject) continue;   // uniform
-            uint8_t result = TW_SMOOTH_MOVED;
-            // projection onto the nearest facet (VertexSmoother.cpp:353-363)
-            {
-                int bad = 0;
-                if (lane == 0) {
-                    const bool bnd = A.kinds[s2] == TW_STAR_BOUNDARY;
-                    const EnvTree& T = bnd ? A.Tb : A.Tin;
-                    if (T.nf <= 0) {
-                        atomicOr(A.counters + kCntError, 4ULL);
-                        bad = 1;
-                    } else {
-                        const V3 pp{p[0], p[1], p[2]};
-                        V3 q;
-                        double d;
-                        int32_t f;
-                        if (!nearest_facet_grid(T, A.E.eps2, pp, q, d, f) &&
-                            nearest_facet(T, pp, q, d) == kTraversalError) {
-                            atomicOr(A.counters + kCntError, 1ULL);
-                            bad = 1;
-                        } else {
-                            p[0] = q.x;
-                            p[1] = q.y;
-                            p[2] = q.z;
-                        }
-                    }
-                }
-                bad = __shfl_sync(full, bad, 0);
-                p[0] = __shfl_sync(full, p[0], 0);
-                p[1] = __shfl_sync(full, p[1], 0);
-                p[2] = __shfl_sync(full, p[2], 0);
-                if (bad) result = TW_SMOOTH_INVALID;
-            }
-            const int32_t b = A.off[s2], nt = A.off[s2 + 1] - b;
-            const StarView S{A.vx, A.vy, A.vz, A.tets + b, nt, A.cen[s2], A.form};
-            const double p0[3] = {A.vx[S.v], A.vy[S.v], A.vz[S.v]};
-            // isFlip at the projected position (:374-378)
-            if (result == TW_SMOOTH_MOVED && !star_positive<32>(S, p, lane, full))
-                result = TW_SMOOTH_REJECT_FLIP;
-            // max calTetQuality before and after (:379-386); max is exact in any order
-            if (result == TW_SMOOTH_MOVED) {
-                double old_max = 0.0, new_max = 0.0;
-                for (int c0 = lane; c0 < nt; c0 += 32) {
-                    double T[12];
-                    const int4 tv = tet_at(S, c0);
-                    gather_tet(S, tv, 0, p0, T);
-                    old_max = fmax(old_max, positive_tet_quality(T, S.form));
-                    gather_tet(S, tv, 0, p, T);
-                    new_max = fmax(new_max, positive_tet_quality(T, S.form));
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    old_max = fmax(old_max, __shfl_xor_sync(full, old_max, o));
-                    new_max = fmax(new_max, __shfl_xor_sync(full, new_max, o));
-                }
-                if (!(new_max < old_max)) result = TW_SMOOTH_REJECT_QUALITY;
-            }
-            // the one-ring surface faces (:314-326, :413-432)
-            if (result == TW_SMOOTH_MOVED) {
-                const uint8_t* ff = A.ff + b;
-                int nmine = 0;
-                for (int c0 = lane; c0 < nt; c0 += 32) {
-                    const int4 tv = tet_at(S, c0);
-                    const uint8_t fl = __ldg(ff + c0);
-                    int32_t key[3];
-                    for (int j = 0; j < 4; ++j) nmine += first_surface_face(S, ff, c0, tv, fl, j, key);
-                }
-                int incl = nmine;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(full, incl, o);
-                    if (lane >= o) incl += t;
-                }
-                const int total = __shfl_sync(full, incl, 31);
-                bool outside = false;
-                for (int w0 = 0; w0 < total && !outside; w0 += kFusedFaceCap) {
-                    // list the faces [w0, w0 + cap) in (tet, face) order
-                    int w = incl - nmine;
-                    for (int c0 = lane; c0 < nt; c0 += 32) {
-                        const int4 tv = tet_at(S, c0);
-                        const uint8_t fl = __ldg(ff + c0);
-                        for (int j = 0; j < 4; ++j) {
-                            int32_t key[3];
-                            if (!first_surface_face(S, ff, c0, tv, fl, j, key)) continue;
-                            if (w >= w0 && w < w0 + kFusedFaceCap) {
-                                // from the centre onward in the cyclic order of the
-                                // sorted triple (:427-432)
-                                const int kv = (key[0] == S.v) ? 0 : (key[1] == S.v) ? 1 : 2;
-                                flist[warp][w - w0] = make_int2(key[(kv + 1) % 3], key[(kv + 2) % 3]);
-                            }
-                            ++w;
-                        }
-                    }
-                    __syncwarp(full);
-                    const int nw = min(kFusedFaceCap, total - w0);
-                    for (int h0 = 0; h0 < nw && !outside; h0 += kFusedHdr) {
-                        const int nh = min(kFusedHdr, nw - h0);
-                        if (lane < nh) {
-                            const int2 vv = flist[warp][h0 + lane];
-                            const double t[9] = {p[0], p[1], p[2],
-                                                 __ldg(A.vx + vv.x), __ldg(A.vy + vv.x), __ldg(A.vz + vv.x),
-                                                 __ldg(A.vx + vv.y), __ldg(A.vy + vv.y), __ldg(A.vz + vv.y)};
-                            int state = 0;
-                            if (!tri_collinear(t)) {
-                                sample_header(t, A.sd, hdr[warp][lane]);
-                                state = 2;
-                                if (header_too_large(hdr[warp][lane])) {
-                                    atomicOr(A.counters + kCntError, 2ULL);
-                                    state = 1;
-                                }
-                            }
-                            hstate[warp][lane] = state;
-                        }
-                        __syncwarp(full);
-                        for (int k = 0; k < nh; ++k) {
-                            const int state = hstate[warp][k];
-                            if (state == 1 ||
-                                (state == 2 &&
-                                 env_face_samples<FP32>(hdr[warp][k], F, A.sd, tst, nq))) {
-                                outside = true;
-                                break;
-                            }
-                        }
-                        __syncwarp(full);
-                    }
-                }
-                if (outside) result = TW_SMOOTH_REJECT_ENVELOPE;
-            }
-            if (lane == 0) {
-                if (result == TW_SMOOTH_MOVED) {
-                    A.out[3 * s2] = p[0];
-                    A.out[3 * s2 + 1] = p[1];
-                    A.out[3 * s2 + 2] = p[2];
-                }
-                A.status[s2] = result;
-            }
-        }
-    }
-    flush_stats(tst, A.counters, nq);
-}
-
-void launch_smooth_fused(int shape, const double* vx, const double* vy, const double* vz,
-                         const int32_t* star_off, const int32_t* tets, const uint8_t* face_flags,
-                         const int32_t* centers, const uint8_t* kinds, int32_t nstars,
-                         int max_step, int max_it, const Surface& Sin, const Surface& Sb,
-                         double eps2, double sd, int precision, double* out, uint8_t* status,
-                         unsigned int* work, unsigned long long* counters, cudaStream_t s,
-                         int form) {
-    if (nstars <= 0) return;
-    FusedArgs A{vx, vy, vz, star_off, reinterpret_cast<const int4*>(tets), face_flags, centers,
-                kinds, nstars, max_step, max_it, form, out, status, env_tree_for(Sin, eps2),
-                env_tree_for(Sb, eps2), eps_params(eps2), sd, counters, work};
-    int group = 8, block = 128;
-    newton_shape_info(shape, &group, &block);
-    if (group == 1) group = 8;
-    cudaMemsetAsync(work, 0, sizeof(unsigned int), s);
-    // persistent: as many blocks as are resident at once (a few per SM), no
-    // more than the stars need
-    const bool fp32 = precision == TW_PRECISION_FP32_CERTIFIED;
-    void (*k)(FusedArgs) =
-        group == 32 ? (fp32 ? k_smooth_fused<32, true> : k_smooth_fused<32, false>)
-        : group == 16 ? (fp32 ? k_smooth_fused<16, true> : k_smooth_fused<16, false>)
-                      : (fp32 ? k_smooth_fused<8, true> : k_smooth_fused<8, false>);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kFusedBlock, 0) != cudaSuccess ||
-        per_sm < 1) {
-        cudaGetLastError();
-        per_sm = 1;
-    }
-    const int64_t need = ((int64_t)nstars * group + kFusedBlock - 1) / kFusedBlock;
-    const int grid = grid_for(std::min<int64_t>(need, INT32_MAX), kFusedBlock, per_sm);
-    k<<<grid, kFusedBlock, 0, s>>>(A);
 }
 
 }  // namespace tw

@@ -142,7 +142,6 @@ struct tw_ctx {
     cudaEvent_t time_ev[2 * kTimeRing] = {};
     int sort_points = 1;     // Morton-order point queries (TW_TUNE_SORT_POINTS)
     int point_block = 384;   // threads per block of the certified grid test (TW_TUNE_POINT_BLOCK)
-    int smooth_fused = 1;    // smoothing pass in one persistent kernel (TW_TUNE_SMOOTH_FUSED)
     tw::Buffer scratch[10];
     // device counters, see the kCnt* indices below
     unsigned long long* counters = nullptr;
@@ -298,15 +297,6 @@ void launch_smooth_stage2(int shape, const double* vx, const double* vy, const d
                           int64_t face_cap, int32_t* face_base, int32_t* face_cnt,
                           unsigned long long* counters, cudaStream_t s,
                           int form = TW_ENERGY_FORM_REFERENCE);
-// The whole pass in one persistent kernel (tw_envelope.cu); work: a device
-// word (zeroed by the launch) for the stars' work counter.
-void launch_smooth_fused(int shape, const double* vx, const double* vy, const double* vz,
-                         const int32_t* star_off, const int32_t* tets, const uint8_t* face_flags,
-                         const int32_t* centers, const uint8_t* kinds, int32_t nstars,
-                         int max_step, int max_it, const Surface& Sin, const Surface& Sb,
-                         double eps2, double sd, int precision, double* out, uint8_t* status,
-                         unsigned int* work, unsigned long long* counters, cudaStream_t s,
-                         int form);
 void launch_smooth_finalize(int32_t nstars, const int32_t* face_base, const int32_t* face_cnt,
                             const uint8_t* face_out, const double* pnew, double* out,
                             uint8_t* status, cudaStream_t s);

@@ -41,6 +41,7 @@ struct Job {
     tw_ctx* c = nullptr;     // owns the job's surfaces, parameters and mesh
     int pending = 0;         // requests submitted and not yet completed
     bool smoothing = false;  // a TW_REQ_SMOOTH of this job is on a lane
+    bool cancelling = false; // tw_server_job_cancel in progress: no new submissions
 };
 
 struct Req {
@@ -669,6 +670,44 @@ int tw_server_job_close(tw_server* s, int32_t job, double timeout_s) {
     return TW_OK;
 }
 
+int tw_server_job_cancel(tw_server* s, int32_t job, double timeout_s) {
+    if (!s) return TW_ERR_ARG;
+    std::lock_guard<std::mutex> ak(s->admin);
+    tw_ctx* c;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        Job* j = job_at(s, job);
+        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
+        j->cancelling = true;
+        // the job's requests still in the queue complete now, cancelled
+        const auto now = Clock::now();
+        for (auto it = s->queue.begin(); it != s->queue.end();) {
+            Req* q = *it;
+            if (q->job != job) {
+                ++it;
+                continue;
+            }
+            q->status = TW_ERR_CANCELLED;
+            q->error = "job cancelled";
+            q->t_done = now;
+            q->done = true;
+            j->pending -= 1;
+            it = s->queue.erase(it);
+        }
+        s->cv.notify_all();
+        // the batches already on a lane finish
+        if (!drain_job(s, lk, j, timeout_s)) {
+            j->cancelling = false;
+            return srv_fail(s, TW_ERR_TIMEOUT, "job has batches in flight");
+        }
+        c = j->c;
+        j->c = nullptr;
+        j->cancelling = false;
+    }
+    tw_ctx_destroy(c);
+    return TW_OK;
+}
+
 int tw_server_submit(tw_server* s, int32_t job, const tw_request* req, uint64_t* ticket) {
     if (!s || !req || !ticket) return TW_ERR_ARG;
     const tw_request& r = *req;
@@ -707,6 +746,10 @@ int tw_server_submit(tw_server* s, int32_t job, const tw_request* req, uint64_t*
     if (!j) {
         s->last_error = "no such job";
         return TW_ERR_ARG;
+    }
+    if (j->cancelling) {
+        s->last_error = "job is being cancelled";
+        return TW_ERR_CANCELLED;
     }
     if (r.kind == TW_REQ_SMOOTH && r.n > 0) {
         if (!j->c->vx) {

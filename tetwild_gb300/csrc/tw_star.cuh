@@ -1,5 +1,5 @@
-// tw_star.cuh -- device routines of one-ring stars shared by the Newton and
-// smoothing kernels (tw_newton.cu) and the fused smoothing pass (tw_envelope.cu):
+// tw_star.cuh -- device routines of one-ring stars used by the Newton,
+// smoothing and collapse kernels (tw_newton.cu):
 // the 3x3 solve, the star view and gathers, NewtonsMethod for G lanes, the
 // inversion and quality checks and the one-ring surface faces.
 #pragma once
