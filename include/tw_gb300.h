@@ -364,6 +364,29 @@ TW_API int tw_collapse_check(tw_ctx* ctx, const int32_t* v12, const uint8_t* fla
                              const int32_t* off, const int32_t* tets, const uint8_t* face_flags,
                              int32_t n, int check_quality, double soft_energy, uint8_t* result);
 
+/* ---- edge-removal (swap) checks ---------------------------------------------------
+ * Replaces: the checks of EdgeRemover::removeAnEdge_32, _44 and _56
+ * (EdgeRemover.cpp:125-177, :277-369, :456-600, decl EdgeRemover.h:59-61)
+ * for a batch of candidate edges v12[i] = (v1, v2) against the resident mesh
+ * (checks only; the caller applies the successful ones).  Shell i = the tets
+ * around the edge, tets[off[i]..off[i+1]) in the caller's order (old_t_ids);
+ * only the variant for a shell of 3, 4 or 5 tets applies.  budget[i] (NULL:
+ * 0) = the remover's equal_buget at the call: while positive, each quality
+ * comparison accepts an equal max energy and spends one unit (spent[i]).
+ * result[i] = TW_SWAP_SUCCESS (config[i] = the configuration taken: 0 for
+ * 3-2, 0-1 for 4-4, 0-4 for 5-6, in the reference's enumeration), _FLIP
+ * (every configuration inverts a tet), _QUALITY (not better), _SIZE (a shell
+ * of another size, or tets not around the edge), _NEEDS_HOST (a vertex is
+ * unrounded: the call returns TW_NEEDS_EXACT_HOST).                        */
+#define TW_SWAP_SUCCESS 0
+#define TW_SWAP_FLIP 1
+#define TW_SWAP_QUALITY 2
+#define TW_SWAP_SIZE 3
+#define TW_SWAP_NEEDS_HOST 4
+TW_API int tw_swap_check(tw_ctx* ctx, const int32_t* v12, const int32_t* off, const int32_t* tets,
+                         const int32_t* budget, int32_t n, uint8_t* result, int8_t* config,
+                         uint8_t* spent);
+
 /* ---- CUDA graphs of the context stream -------------------------------------------
  * Capture the _device calls issued between begin and end into an executable
  * graph and replay it with one launch (the inputs are re-read from the same

@@ -107,6 +107,7 @@ class Oracle:
                                         _P, _I], None),
             "two_collapse_check_batch": ([_P, _P, _P, _P, _P, _P, _I64, _P, _P, _D, _D, _I, _D,
                                           _P, _I], None),
+            "two_swap_check_batch": ([_P, _P, _P, _P, _P, _I64, _P, _P, _P], None),
             "two_energy_stats": ([_P, _P, _I64, _P, _D, _P, _P, _P, _P], None),
             "two_dihedral_minmax": ([_P, _P, _P], None),
             "two_dihedral_stats": ([_P, _P, _I64, _P, _P, _P, _P, _P], None),
@@ -227,6 +228,20 @@ class Oracle:
                                         1 if check_quality else 0, soft_energy, _p(out), nthreads)
         return out
 
+
+    def swap_check(self, xyz, v12, off, tets, budget=None):
+        """Checks of candidate edge removals (two_swap_check): (result, config, spent)."""
+        X = _c(xyz, np.float64).reshape(-1, 3)
+        O = _c(off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        V = _c(v12, np.int32).reshape(-1, 2)
+        B = None if budget is None else _c(budget, np.int32)
+        n = V.shape[0]
+        res = np.empty(n, np.uint8)
+        cfg = np.empty(n, np.int8)
+        sp = np.empty(n, np.uint8)
+        self.L.two_swap_check_batch(_p(X), _p(O), _p(T), _p(V), _p(B), n, _p(res), _p(cfg), _p(sp))
+        return res, cfg, sp
 
     def dihedral_minmax(self, T12):
         """calTetQuality_AD of one tet (12 coordinates): (min, max) dihedral angle."""

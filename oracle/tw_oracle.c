@@ -1993,3 +1993,222 @@ void two_collapse_check_batch(const double* xyz, const int32_t* off, const int32
     j.o0 = result;
     tw_parallel(j, n, nthreads);
 }
+
+/* =========================================================================
+ * The checks of one edge removal (EdgeRemover::removeAnEdge_32 / _44 / _56,
+ * EdgeRemover.cpp:125-177, :277-369, :456-600) for the edge (v1, v2) whose
+ * shell (old_t_ids, in the caller's order) is the k tets shell[4k]; only the
+ * variant for k = 3, 4 or 5 applies (the others return false at once).
+ * Energy AMIPS with use_energy_max (State.h:53): a configuration's quality is
+ * the max of its tets' calTetQuality_AMIPS (getCheckQuality, :575-603), the
+ * old one the max over the shell (the stored qualities, equal to
+ * calTetQuality at the current positions).  budget: equal_buget at the call;
+ * while positive, each comparison accepts an equal max and spends a unit
+ * (:169-176).  The vertices must be rounded (isFlip on posf).  Returns
+ * SWAP_SUCCESS 0 (config: the configuration taken), SWAP_FLIP 1 (every
+ * configuration inverts a tet), SWAP_QUALITY 2 (not better), SWAP_SIZE 3 (a
+ * shell of another size or not around the edge); *spent = budget units spent.
+ * The reference's order of tests is kept, including its early exits: in 4-4
+ * a valid configuration that is not better ends the removal (:356-364), and a
+ * later valid configuration must beat the earlier one.
+ * ========================================================================= */
+static void tw_tet_replace(const int32_t* t, int32_t from, int32_t to, int32_t* o)
+{
+    for (int j = 0; j < 4; ++j) o[j] = t[j];
+    for (int j = 0; j < 4; ++j)
+        if (o[j] == from) { o[j] = to; break; }   /* std::find: the first occurrence */
+}
+static int tw_tet_has(const int32_t* t, int32_t v)
+{
+    return t[0] == v || t[1] == v || t[2] == v || t[3] == v;
+}
+static void tw_tet_coords(const double* xyz, const int32_t* t, double T[12])
+{
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) T[3 * j + k] = xyz[3 * (size_t)t[j] + k];
+}
+static int tw_tets_flip(const double* xyz, const int32_t* ts, int m)
+{
+    for (int i = 0; i < m; ++i) {
+        double T[12];
+        tw_tet_coords(xyz, ts + 4 * i, T);
+        if (two_tet_flip(T)) return 1;
+    }
+    return 0;
+}
+static double tw_tet_q(const double* xyz, const int32_t* t)
+{
+    double T[12];
+    tw_tet_coords(xyz, t, T);
+    return two_tet_quality(T);
+}
+static int tw_swap_better(double nq, double oq, int* budget, int* spent)
+{
+    if (*budget > 0) {
+        --*budget;
+        ++*spent;
+        return nq <= oq;
+    }
+    return nq < oq;
+}
+/* n12_v_ids / n12_t_ids of :278-303 and :457-481: the ring of the shell's
+ * other vertices, walked from tet 0; returns 0 when the shell is not a ring. */
+static int tw_swap_ring(const int32_t* shell, int N, int32_t v1, int32_t v2, int32_t* nv,
+                        int* tid)
+{
+    int32_t e[5][2];
+    for (int i = 0; i < N; ++i) {
+        int c = 0;
+        for (int j = 0; j < 4; ++j) {
+            const int32_t x = shell[4 * i + j];
+            if (x != v1 && x != v2) {
+                if (c == 2) return 0;
+                e[i][c++] = x;
+            }
+        }
+        if (c != 2) return 0;
+    }
+    int visited[5] = {0, 0, 0, 0, 0};
+    int m = 2, mt = 1;
+    nv[0] = e[0][0];
+    nv[1] = e[0][1];
+    tid[0] = 0;
+    visited[0] = 1;
+    for (int it = 0; it < N - 2; ++it) {
+        for (int j = 0; j < N; ++j) {
+            if (visited[j]) continue;
+            if (e[j][0] == nv[m - 1]) {
+                visited[j] = 1;
+                nv[m++] = e[j][1];
+            } else if (e[j][1] == nv[m - 1]) {
+                visited[j] = 1;
+                nv[m++] = e[j][0];
+            }
+            if (visited[j]) {
+                tid[mt++] = j;
+                break;
+            }
+        }
+    }
+    if (m != N) return 0;
+    for (int j = 0; j < N; ++j)
+        if (!visited[j]) { tid[mt++] = j; break; }
+    return mt == N;
+}
+
+int two_swap_check(const double* xyz, const int32_t* shell, int32_t k, int32_t v1, int32_t v2,
+                   int budget, int* config, int* spent)
+{
+    *config = -1;
+    *spent = 0;
+    if (k < 3 || k > 5) return 3;
+    for (int i = 0; i < k; ++i)
+        if (!tw_tet_has(shell + 4 * i, v1) || !tw_tet_has(shell + 4 * i, v2)) return 3;
+    double oq = 0.0;
+    for (int i = 0; i < k; ++i) {
+        const double q = tw_tet_q(xyz, shell + 4 * i);
+        if (q > oq) oq = q;
+    }
+    int32_t nt[8];
+    if (k == 3) {
+        int32_t vv[2];
+        int c = 0;
+        for (int j = 0; j < 4; ++j)
+            if (shell[j] != v1 && shell[j] != v2) vv[c++] = shell[j];
+        const int32_t* a = shell + 4;
+        const int32_t* b = shell + 8;
+        if (!tw_tet_has(a, vv[0])) {
+            a = shell + 8;
+            b = shell + 4;
+        }
+        tw_tet_replace(a, v1, vv[1], nt);
+        tw_tet_replace(b, v2, vv[0], nt + 4);
+        if (tw_tets_flip(xyz, nt, 2)) return 1;
+        const double q0 = tw_tet_q(xyz, nt), q1 = tw_tet_q(xyz, nt + 4);
+        double nq = 0.0;
+        if (q0 > nq) nq = q0;
+        if (q1 > nq) nq = q1;
+        if (!tw_swap_better(nq, oq, &budget, spent)) return 2;
+        *config = 0;
+        return 0;
+    }
+    int32_t nv[5];
+    int tid[5];
+    if (!tw_swap_ring(shell, k, v1, v2, nv, tid)) return 3;
+    if (k == 4) {
+        int valid = 0;
+        for (int i = 0; i < 2; ++i) {
+            int32_t ts[16];
+            const int32_t a = nv[i], b = nv[2 + i];
+            for (int j = 0; j < 4; ++j) {
+                const int32_t* t = shell + 4 * j;
+                if (tw_tet_has(t, a))
+                    tw_tet_replace(t, v2, b, ts + 4 * j);
+                else
+                    tw_tet_replace(t, v1, a, ts + 4 * j);
+            }
+            if (tw_tets_flip(xyz, ts, 4)) continue;
+            double nq = 0.0;
+            for (int j = 0; j < 4; ++j) {
+                const double q = tw_tet_q(xyz, ts + 4 * j);
+                if (q > nq) nq = q;
+            }
+            if (!tw_swap_better(nq, oq, &budget, spent)) return 2;
+            valid = 1;
+            oq = nq;
+            *config = i;
+        }
+        return valid ? 0 : 1;
+    }
+    /* k == 5 */
+    int vvalid[5] = {1, 1, 1, 1, 1};
+    double q1[5][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    for (int i = 0; i < 5; ++i) {
+        if (!vvalid[(i + 1) % 5] && !vvalid[(i + 4) % 5]) continue;
+        const int32_t* t = shell + 4 * tid[i];
+        tw_tet_replace(t, v1, nv[(i + 4) % 5], nt);
+        tw_tet_replace(t, v2, nv[(i + 4) % 5], nt + 4);
+        if (tw_tets_flip(xyz, nt, 2)) {
+            vvalid[(i + 1) % 5] = 0;
+            vvalid[(i + 4) % 5] = 0;
+            continue;
+        }
+        q1[i][0] = tw_tet_q(xyz, nt);
+        q1[i][1] = tw_tet_q(xyz, nt + 4);
+    }
+    if (!(vvalid[0] || vvalid[1] || vvalid[2] || vvalid[3] || vvalid[4])) return 1;
+    int sel = -1, tested = 0;
+    for (int i = 0; i < 5; ++i) {
+        if (!vvalid[i]) continue;
+        const int32_t* t = shell + 4 * tid[(i + 2) % 5];
+        tw_tet_replace(t, v1, nv[i], nt);
+        tw_tet_replace(t, v2, nv[i], nt + 4);
+        if (tw_tets_flip(xyz, nt, 2)) continue;
+        tested = 1;
+        const double qs[6] = {tw_tet_q(xyz, nt), tw_tet_q(xyz, nt + 4), q1[(i + 1) % 5][0],
+                              q1[(i + 4) % 5][0], q1[(i + 1) % 5][1], q1[(i + 4) % 5][1]};
+        double nq = 0.0;
+        for (int j = 0; j < 6; ++j)
+            if (qs[j] > nq) nq = qs[j];
+        if (!tw_swap_better(nq, oq, &budget, spent)) continue;
+        oq = nq;
+        sel = i;
+    }
+    if (sel < 0) return tested ? 2 : 1;
+    *config = sel;
+    return 0;
+}
+
+void two_swap_check_batch(const double* xyz, const int32_t* off, const int32_t* tets,
+                          const int32_t* v12, const int32_t* budget, int64_t n, uint8_t* result,
+                          int8_t* config, uint8_t* spent)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        int cfg = -1, sp = 0;
+        result[i] = (uint8_t)two_swap_check(xyz, tets + 4 * (size_t)off[i], off[i + 1] - off[i],
+                                            v12[2 * i], v12[2 * i + 1], budget ? budget[i] : 0,
+                                            &cfg, &sp);
+        config[i] = (int8_t)cfg;
+        spent[i] = (uint8_t)sp;
+    }
+}

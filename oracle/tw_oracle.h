@@ -162,6 +162,12 @@ void two_smooth_stars_batch(const double* xyz, const int32_t* star_off, const in
                             double* out, int8_t* status, int nthreads);
 void two_nearest_batch(const two_surface* s, const double* P, int64_t n, double* Q, double* D,
                        int32_t* F, int nthreads);
+/* ---- edge removal (EdgeRemover.cpp:125-600) ------------------------------ */
+int two_swap_check(const double* xyz, const int32_t* shell, int32_t k, int32_t v1, int32_t v2,
+                   int budget, int* config, int* spent);
+void two_swap_check_batch(const double* xyz, const int32_t* off, const int32_t* tets,
+                          const int32_t* v12, const int32_t* budget, int64_t n, uint8_t* result,
+                          int8_t* config, uint8_t* spent);
 void two_collapse_check_batch(const double* xyz, const int32_t* off, const int32_t* tets,
                               const uint8_t* fflags, const int32_t* v12, const uint8_t* flags,
                               int64_t n, const two_surface* s_in, const two_surface* s_b,

@@ -167,6 +167,7 @@ _SIGS = {
     "tw_server_job_read_mesh": [_P, _I32, _P, _D],
     "tw_server_job_close": [_P, _I32, _D],
     "tw_server_job_cancel": [_P, _I32, _D],
+    "tw_swap_check": [_P, _P, _P, _P, _P, _I32, _P, _P, _P],
     "tw_server_submit": [_P, _I32, ctypes.POINTER(TwRequest), ctypes.POINTER(ctypes.c_uint64)],
     "tw_server_wait": [_P, ctypes.c_uint64, _D, ctypes.POINTER(_D)],
     "tw_server_get_stats": [_P, ctypes.POINTER(TwServerStats)],
@@ -481,6 +482,22 @@ class Context:
                                                _ptr(FF), n, 1 if check_quality else 0,
                                                soft_energy, _ptr(out)))
         return out
+
+    def swap_check(self, v12, shell_off, tets, budget=None):
+        """Checks of candidate edge removals (EdgeRemover::removeAnEdge_32 / _44 / _56):
+        (result, config, spent) [n]; TW_NEEDS_EXACT_HOST is allowed (result 4 marks them)."""
+        V = _c(v12, np.int32).reshape(-1, 2)
+        O = _c(shell_off, np.int32)
+        T = _c(tets, np.int32).reshape(-1, 4)
+        B = None if budget is None else _c(budget, np.int32)
+        n = V.shape[0]
+        res = np.empty(n, np.uint8)
+        cfg = np.empty(n, np.int8)
+        sp = np.empty(n, np.uint8)
+        self._check(self.lib.tw_swap_check(self.h, _ptr(V), _ptr(O), _ptr(T), _ptr(B), n,
+                                           _ptr(res), _ptr(cfg), _ptr(sp)),
+                    allow=(TW_OK, TW_NEEDS_EXACT_HOST))
+        return res, cfg, sp
 
     # -- nearest facet -----------------------------------------------------------------
     def nearest_points(self, P, which=TW_SURFACE_INPUT):

@@ -27,7 +27,7 @@ NVCC_FLAGS = [
     "--expt-relaxed-constexpr",
 ]
 SOURCES = ["tw_amips.cu", "tw_lbvh.cu", "tw_envelope.cu", "tw_newton.cu", "tw_capi.cu",
-           "tw_noalloc.cu", "tw_server.cu"]
+           "tw_noalloc.cu", "tw_server.cu", "tw_swap.cu"]
 
 
 def nvcc() -> str:

@@ -1221,6 +1221,51 @@ int tw_collapse_check(tw_ctx* c, const int32_t* v12, const uint8_t* flags, const
     return sync_status(c, "tw_collapse_check");
 }
 
+int tw_swap_check(tw_ctx* c, const int32_t* v12, const int32_t* off, const int32_t* tets,
+                  const int32_t* budget, int32_t n, uint8_t* result, int8_t* config,
+                  uint8_t* spent) {
+    if (!c || n < 0 || (n > 0 && (!v12 || !off || !tets || !result || !config || !spent)))
+        return TW_ERR_ARG;
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    if (n == 0) return TW_OK;
+    if (off[0] != 0) return fail(c, TW_ERR_ARG, "shell offsets must start at 0");
+    for (int32_t i = 0; i < n; ++i)
+        if (off[i + 1] < off[i]) return fail(c, TW_ERR_ARG, "shell offsets decrease");
+    const int64_t nt = off[n];
+    Guard g(c->device);
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t ns = (size_t)n;
+    const size_t bytes = align(8 * ns) + align(4 * (ns + 1)) + align(16 * (size_t)nt) +
+                         align(4 * ns) + 3 * align(ns) + 256;
+    void* p;
+    int st = ensure(c, 7, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dv = (int32_t*)q; q += align(8 * ns);
+    int32_t* doff = (int32_t*)q; q += align(4 * (ns + 1));
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)nt);
+    int32_t* db = (int32_t*)q; q += align(4 * ns);
+    uint8_t* dres = (uint8_t*)q; q += align(ns);
+    int8_t* dcfg = (int8_t*)q; q += align(ns);
+    uint8_t* dsp = (uint8_t*)q;
+    cudaMemsetAsync(c->counters + kCntUnrounded, 0, sizeof(unsigned long long), c->stream);
+    cudaMemcpyAsync(dv, v12, 8 * ns, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(doff, off, 4 * (ns + 1), cudaMemcpyHostToDevice, c->stream);
+    if (nt > 0) cudaMemcpyAsync(dt, tets, 16 * (size_t)nt, cudaMemcpyHostToDevice, c->stream);
+    if (budget) cudaMemcpyAsync(db, budget, 4 * ns, cudaMemcpyHostToDevice, c->stream);
+    launch_swap_check(c->vx, c->vy, c->vz, c->rounded, c->nv, dv, doff, dt, budget ? db : nullptr,
+                      n, dres, dcfg, dsp, c->counters, c->stream, c->energy_form);
+    cudaMemcpyAsync(result, dres, ns, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(config, dcfg, ns, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(spent, dsp, ns, cudaMemcpyDeviceToHost, c->stream);
+    unsigned long long unrounded = 0;
+    cudaMemcpyAsync(&unrounded, c->counters + kCntUnrounded, sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_swap_check");
+    if (st != TW_OK) return st;
+    return unrounded ? TW_NEEDS_EXACT_HOST : TW_OK;
+}
+
 // ---- misc ---------------------------------------------------------------------------
 int tw_newton_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
                            const int32_t* centers, int32_t nstars, double* out, uint8_t* moved) {

@@ -336,6 +336,13 @@ void launch_collapse_stage(int shape, const double* vx, const double* vy, const 
 void launch_collapse_finalize(int32_t n, const int32_t* face_base, const int32_t* face_cnt,
                               const uint8_t* face_out, uint8_t* status, cudaStream_t s);
 
+// ---- edge-removal checks (tw_swap.cu) ----
+void launch_swap_check(const double* vx, const double* vy, const double* vz,
+                       const uint8_t* rounded, int32_t nv, const int32_t* v12, const int32_t* off,
+                       const int32_t* tets, const int32_t* budget, int32_t n, uint8_t* result,
+                       int8_t* config, uint8_t* spent, unsigned long long* counters,
+                       cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
+
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);
 void launch_fp32_probe(float* out, int iters, int blocks, cudaStream_t s);
