@@ -230,6 +230,10 @@ def test_job_cancel_mid_flight(workload):
         srv.set_params(tw.TW_PRECISION_FP32_CERTIFIED, 1, 8)
         a = srv.job_open(Va, Fa, ea * ea, ea / 2)
         b = srv.job_open(Vb, Fb, eb * eb, eb / 2)
+        # a burst first, so that the lane's scratch has grown to its largest batch
+        warm = [srv.submit_points(a, Pa) for _ in range(45)]
+        for t, _ in warm:
+            srv.wait(t)
         before = srv.stats()
         ta, tb = [], []
         for k in range(300):
