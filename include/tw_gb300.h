@@ -387,6 +387,27 @@ TW_API int tw_swap_check(tw_ctx* ctx, const int32_t* v12, const int32_t* off, co
                          const int32_t* budget, int32_t n, uint8_t* result, int8_t* config,
                          uint8_t* spent);
 
+/* ---- operator candidates and a conflict-free batch, on the device ------------------
+ * No counterpart in the reference, which applies its operators one at a time
+ * from priority queues; this is a parallel schedule, a separate mode whose
+ * results differ from the reference's sequential passes.  The candidates
+ * mirror the queues' (EdgeSplitter.cpp:37-73, EdgeCollapser.cpp:19-81): for
+ * op = TW_OP_SPLIT every edge of tets[ntets][4] whose squared length exceeds
+ * ideal_weight * s^2, longest first; for TW_OP_COLLAPSE both directions
+ * (v1 -> v2) of every edge shorter than that, shortest first (s = the mean of
+ * the two vertices' scale[], 1 when scale is NULL; equal lengths in edge
+ * order; the caller filters locked or box-bound vertices).  Squared lengths
+ * use the resident positions.  The batch: the greedy choice in that priority
+ * order of candidates whose tets are pairwise disjoint (a split's tets: those
+ * around its edge; a collapse's: those around v1).  out_v12[2 * cap]: the
+ * chosen (v1, v2) in priority order (at most cap written); *n_sched: how
+ * many were chosen; *n_cand: how many candidates there were.             */
+#define TW_OP_SPLIT 0
+#define TW_OP_COLLAPSE 1
+TW_API int tw_schedule_edges(tw_ctx* ctx, const int32_t* tets, int32_t ntets, const double* scale,
+                             double ideal_weight, int op, int32_t* out_v12, int32_t cap,
+                             int32_t* n_sched, int32_t* n_cand);
+
 /* ---- CUDA graphs of the context stream -------------------------------------------
  * Capture the _device calls issued between begin and end into an executable
  * graph and replay it with one launch (the inputs are re-read from the same

@@ -32,6 +32,8 @@ TW_ERR_NO_MESH = -5
 TW_ERR_TIMEOUT = -6
 TW_ERR_TOO_LARGE = -7
 TW_ERR_CANCELLED = -8
+TW_OP_SPLIT = 0
+TW_OP_COLLAPSE = 1
 TW_ENERGY_RAW = 0
 TW_ENERGY_QUALITY = 1
 TW_SURFACE_INPUT = 0
@@ -168,6 +170,7 @@ _SIGS = {
     "tw_server_job_close": [_P, _I32, _D],
     "tw_server_job_cancel": [_P, _I32, _D],
     "tw_swap_check": [_P, _P, _P, _P, _P, _I32, _P, _P, _P],
+    "tw_schedule_edges": [_P, _P, _I32, _P, _D, _I, _P, _I32, _P, _P],
     "tw_server_submit": [_P, _I32, ctypes.POINTER(TwRequest), ctypes.POINTER(ctypes.c_uint64)],
     "tw_server_wait": [_P, ctypes.c_uint64, _D, ctypes.POINTER(_D)],
     "tw_server_get_stats": [_P, ctypes.POINTER(TwServerStats)],
@@ -498,6 +501,20 @@ class Context:
                                            _ptr(res), _ptr(cfg), _ptr(sp)),
                     allow=(TW_OK, TW_NEEDS_EXACT_HOST))
         return res, cfg, sp
+
+    def schedule_edges(self, tets, op, ideal_weight, scale=None):
+        """Operator candidates of the tet list and their conflict-free batch, on the device
+        (tw_schedule_edges): ((v1, v2) chosen [m, 2] in priority order, number of
+        candidates)."""
+        T = _c(tets, np.int32).reshape(-1, 4)
+        S = None if scale is None else _c(scale, np.float64)
+        cap = max(1, T.shape[0])
+        out = np.empty((cap, 2), np.int32)
+        ns, nc = _I32(), _I32()
+        self._check(self.lib.tw_schedule_edges(self.h, _ptr(T), T.shape[0], _ptr(S), ideal_weight,
+                                               op, _ptr(out), cap, ctypes.byref(ns),
+                                               ctypes.byref(nc)))
+        return out[:min(ns.value, cap)].copy(), nc.value
 
     # -- nearest facet -----------------------------------------------------------------
     def nearest_points(self, P, which=TW_SURFACE_INPUT):

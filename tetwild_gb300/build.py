@@ -27,7 +27,8 @@ NVCC_FLAGS = [
     "--expt-relaxed-constexpr",
 ]
 SOURCES = ["tw_amips.cu", "tw_lbvh.cu", "tw_envelope.cu", "tw_newton.cu", "tw_capi.cu",
-           "tw_noalloc.cu", "tw_server.cu", "tw_swap.cu"]
+           "tw_noalloc.cu", "tw_server.cu", "tw_swap.cu",
+           "tw_schedule.cu"]
 
 
 def nvcc() -> str:

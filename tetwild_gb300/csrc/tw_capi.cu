@@ -1266,6 +1266,46 @@ int tw_swap_check(tw_ctx* c, const int32_t* v12, const int32_t* off, const int32
     return unrounded ? TW_NEEDS_EXACT_HOST : TW_OK;
 }
 
+int tw_schedule_edges(tw_ctx* c, const int32_t* tets, int32_t ntets, const double* scale,
+                      double ideal_weight, int op, int32_t* out_v12, int32_t cap, int32_t* n_sched,
+                      int32_t* n_cand) {
+    if (!c || ntets < 0 || cap < 0 || !n_sched || !n_cand || (ntets > 0 && !tets) ||
+        (cap > 0 && !out_v12))
+        return TW_ERR_ARG;
+    if (op != TW_OP_SPLIT && op != TW_OP_COLLAPSE)
+        return fail(c, TW_ERR_ARG, "tw_schedule_edges: unknown operator");
+    if (!(ideal_weight >= 0.0)) return fail(c, TW_ERR_ARG, "tw_schedule_edges: ideal_weight");
+    if (!c->vx) return fail(c, TW_ERR_NO_MESH, "no resident mesh");
+    *n_sched = *n_cand = 0;
+    if (ntets == 0) return TW_OK;
+    if ((int64_t)ntets * 12 > (int64_t)INT32_MAX)
+        return fail(c, TW_ERR_TOO_LARGE, "tw_schedule_edges: too many tets");
+    Guard g(c->device);
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t bytes = align(16 * (size_t)ntets) + align(8 * (size_t)c->nv) +
+                         align(8 * (size_t)std::max(cap, 1)) + 256;
+    void* p;
+    int st = ensure(c, 6, bytes, &p);
+    if (st != TW_OK) return st;
+    char* q = (char*)p;
+    int32_t* dt = (int32_t*)q; q += align(16 * (size_t)ntets);
+    double* ds = (double*)q; q += align(8 * (size_t)c->nv);
+    int32_t* dout = (int32_t*)q;
+    cudaMemcpyAsync(dt, tets, 16 * (size_t)ntets, cudaMemcpyHostToDevice, c->stream);
+    if (scale) cudaMemcpyAsync(ds, scale, 8 * (size_t)c->nv, cudaMemcpyHostToDevice, c->stream);
+    int32_t ns = 0, nc = 0;
+    st = schedule_edges(c, dt, ntets, scale ? ds : nullptr, ideal_weight, op, dout, cap, &ns, &nc,
+                        c->stream);
+    if (st != TW_OK) return st;
+    const int32_t m = std::min(ns, cap);
+    if (m > 0) cudaMemcpyAsync(out_v12, dout, 8 * (size_t)m, cudaMemcpyDeviceToHost, c->stream);
+    st = sync_status(c, "tw_schedule_edges");
+    if (st != TW_OK) return st;
+    *n_sched = ns;
+    *n_cand = nc;
+    return TW_OK;
+}
+
 // ---- misc ---------------------------------------------------------------------------
 int tw_newton_stars_device(tw_ctx* c, const int32_t* star_off, const int32_t* tets,
                            const int32_t* centers, int32_t nstars, double* out, uint8_t* moved) {
@@ -1476,3 +1516,7 @@ int tw_probe_peaks(tw_ctx* c, double* fp64_tflops, double* fp32_tflops) {
 }
 
 }  // extern "C"
+
+namespace tw {
+int stream_status(tw_ctx* c, const char* where) { return sync_status(c, where); }
+}  // namespace tw

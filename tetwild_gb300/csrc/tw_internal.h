@@ -172,6 +172,9 @@ namespace tw {
 
 // Error helpers (implemented in tw_capi.cu).
 int fail(tw_ctx* c, int code, const std::string& msg);
+// Waits for the context's streams and turns a CUDA error or the device error
+// word into a status (and message).
+int stream_status(tw_ctx* c, const char* where);
 int cuda_fail(tw_ctx* c, cudaError_t e, const char* where);
 int ensure(tw_ctx* c, int slot, size_t bytes, void** out);
 int dev_alloc(tw_ctx* c, size_t bytes, void** out);
@@ -342,6 +345,12 @@ void launch_swap_check(const double* vx, const double* vy, const double* vz,
                        const int32_t* tets, const int32_t* budget, int32_t n, uint8_t* result,
                        int8_t* config, uint8_t* spent, unsigned long long* counters,
                        cudaStream_t s, int form = TW_ENERGY_FORM_REFERENCE);
+
+// ---- operator scheduling (tw_schedule.cu): device tets [nt][4] and scale
+// [nv] (may be null); out_v12 device [2 * cap] ----
+int schedule_edges(tw_ctx* c, const int32_t* dtets, int64_t nt, const double* dscale,
+                   double ideal_weight, int op, int32_t* out_v12, int32_t cap, int32_t* n_sched,
+                   int32_t* n_cand, cudaStream_t s);
 
 // ---- peak probes (tw_capi.cu) ----
 void launch_fp64_probe(double* out, int iters, int blocks, cudaStream_t s);
