@@ -2,11 +2,12 @@
 
 TEST INFRASTRUCTURE ONLY.  Two stages:
 
-1. ``slice`` (needs the reference checkout, TW_REFERENCE_ROOT, default
-   /root/reference): copies the exact line ranges listed in SLICES, and the
-   whole files listed in COPIES, into oracle/_ref/src/.  Each slice is checked
-   against the first line it must start with, so a moved line range fails
-   loudly instead of compiling the wrong code.  oracle/_ref/ is git-ignored:
+1. ``slice`` (needs the reference checkout, named by the environment
+   variable TW_REFERENCE_ROOT; nothing is sliced when it is unset): copies
+   the exact line ranges listed in SLICES, and the whole files listed in
+   COPIES, into oracle/_ref/src/.  Each slice is checked against the first
+   line it must start with, so a moved line range fails loudly instead of
+   compiling the wrong code.  oracle/_ref/ is git-ignored:
    nothing from the reference is committed.
 2. ``compile`` (needs only oracle/_ref/src): builds oracle/_ref/libtwref.so
    from those files, the geogram shim (oracle/ref/shim) and the oracle C code,
@@ -46,13 +47,14 @@ COPIES = [
 ]
 
 
-def reference_root() -> Path:
-    return Path(os.environ.get("TW_REFERENCE_ROOT", "/root/reference"))
+def reference_root() -> Path | None:
+    root = os.environ.get("TW_REFERENCE_ROOT")
+    return Path(root) if root else None
 
 
 def do_slice() -> bool:
     root = reference_root()
-    if not (root / "src/tetwild/LocalOperations.cpp").is_file():
+    if root is None or not (root / "src/tetwild/LocalOperations.cpp").is_file():
         return False
     SRC.mkdir(parents=True, exist_ok=True)
     for rel, lo, hi, name, head in SLICES:
@@ -91,7 +93,7 @@ def main(argv: list[str]) -> int:
     what = argv[1] if len(argv) > 1 else "all"
     if what in ("slice", "all"):
         if not do_slice() and what == "slice":
-            print("reference checkout not found; nothing sliced", file=sys.stderr)
+            print("reference checkout not found (TW_REFERENCE_ROOT); nothing sliced", file=sys.stderr)
             return 1
     if what in ("compile", "all"):
         so = do_compile()
