@@ -298,6 +298,12 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
  *   (128, 256, 384 default, or 768; 768 resident threads per SM in each): the
  *   warps of a block test neighbouring sorted points together.  Results never
  *   depend on it.
+ * TW_TUNE_BIN_CELL: bin side of the point test's bin index as a multiple of
+ *   the mean facet extent (default 0.25, at least 1/250 of the surface box's
+ *   largest side; each bin lists its leaves with a mask of the 8x8x8 fine
+ *   cells each reaches; the index is rebuilt); 0 turns the index off (the
+ *   point test then reads the grid's hashed cell lists).  Point queries are
+ *   sorted on the index's bins.  Results never depend on it.
  * TW_TUNE_TIME_KERNELS: 1 records CUDA events around the point-envelope
  *   test kernel of each tw_envelope_points(_device) call (the last 64);
  *   tw_kernel_times returns their durations (ms) and clears the record.
@@ -306,6 +312,7 @@ TW_API int tw_smooth_stars_device(tw_ctx* ctx, const int32_t* star_off, const in
 #define TW_TUNE_SORT_POINTS 1
 #define TW_TUNE_TIME_KERNELS 2
 #define TW_TUNE_POINT_BLOCK 3
+#define TW_TUNE_BIN_CELL 4
 TW_API int tw_set_tuning(tw_ctx* ctx, int knob, double value);
 TW_API int tw_kernel_times(tw_ctx* ctx, float* ms, int max, int* count);
 

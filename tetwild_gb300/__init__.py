@@ -394,6 +394,7 @@ class Context:
     TUNE_SORT_POINTS = 1
     TUNE_TIME_KERNELS = 2
     TUNE_POINT_BLOCK = 3
+    TUNE_BIN_CELL = 4
 
     def set_tuning(self, knob: int, value: float):
         """Work-only knobs (TW_TUNE_*): results are the same for every value."""

@@ -345,6 +345,16 @@ int tw_set_tuning(tw_ctx* c, int knob, double value) {
         }
         return TW_OK;
     }
+    if (knob == TW_TUNE_BIN_CELL) {
+        if (!(value == 0.0 || (value >= 0.05 && value <= 64.0)))
+            return fail(c, TW_ERR_ARG, "bin cell factor: 0 or 0.05..64");
+        c->bin_cell = value;
+        for (auto& S : c->surf) {
+            int st = build_env_grid(c, S, c->eps2, c->grid_cell, c->stream);
+            if (st != TW_OK) return st;
+        }
+        return TW_OK;
+    }
     if (knob == TW_TUNE_SORT_POINTS) {
         if (!(value == 0.0 || value == 1.0 || (value >= 2.0 && value <= 8.0 &&
                                                value == (double)(int)value)))
@@ -441,7 +451,7 @@ int tw_reset_stats(tw_ctx* c) {
     int st = sync_status(c, "tw_reset_stats");
     if (st != TW_OK) return st;
     const int keep[] = {kCntExactOrient, kCntEnvQueries, kCntEnvFacetTests, kCntEnvFp64,
-                        kCntAmipsTets, kCntAmipsFp64};
+                        kCntAmipsTets, kCntAmipsFp64, kCntEnvWarpFallback};
     for (int k : keep) cudaMemset(c->counters + k, 0, sizeof(unsigned long long));
     return sync_status(c, "tw_reset_stats");
 }

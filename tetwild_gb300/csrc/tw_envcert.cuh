@@ -100,15 +100,14 @@ constexpr int kFacetOut = 0;
 constexpr int kFacetIn = 1;
 constexpr int kFacetBand = 2;
 
-__device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull, int32_t f,
-                                              const CertQuery& q) {
-    const float4* w = reinterpret_cast<const float4*>(cull + f);
-    // ah0 ah1 ah2 al0 | al1 al2 n0 n1 | n2 ne00 ne01 ne02 | ne10 ne11 ne12 ne20 |
-    // ne21 ne22 c0 c1 | c2 o0 o1 o2 | len0 len1 len2 ok
-    const float4 w6 = __ldg(w + 6);
+// The facet record as seven float4 (from global or shared memory):
+// ah0 ah1 ah2 al0 | al1 al2 n0 n1 | n2 ne00 ne01 ne02 | ne10 ne11 ne12 ne20 |
+// ne21 ne22 c0 c1 | c2 o0 o1 o2 | len0 len1 len2 ok  (ok == 0: always the band)
+__device__ __forceinline__ int facet_classify_rec(const float4& w0, const float4& w1,
+                                                  const float4& w2, const float4& w3,
+                                                  const float4& w4, const float4& w5,
+                                                  const float4& w6, const CertQuery& q) {
     if (__float_as_uint(w6.w) == 0u) return kFacetBand;
-    const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2), w3 = __ldg(w + 3);
-    const float4 w4 = __ldg(w + 4), w5 = __ldg(w + 5);
     const float rx = (q.ph[0] - w0.x) + (q.pl[0] - w0.w);
     const float ry = (q.ph[1] - w0.y) + (q.pl[1] - w1.x);
     const float rz = (q.ph[2] - w0.z) + (q.pl[2] - w1.y);
@@ -165,6 +164,15 @@ __device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull
     if (L2 > q.e2hi) return kFacetOut;
     if (U2 < q.e2lo) return kFacetIn;
     return kFacetBand;
+}
+
+__device__ __forceinline__ int facet_classify(const FacetCull* __restrict__ cull, int32_t f,
+                                              const CertQuery& q) {
+    const float4* w = reinterpret_cast<const float4*>(cull + f);
+    const float4 w6 = __ldg(w + 6);
+    if (__float_as_uint(w6.w) == 0u) return kFacetBand;
+    return facet_classify_rec(__ldg(w), __ldg(w + 1), __ldg(w + 2), __ldg(w + 3), __ldg(w + 4),
+                              __ldg(w + 5), w6, q);
 }
 
 // The certified test of one leaf: FP32 classification, FP64 in the band.

@@ -30,6 +30,10 @@
 namespace tw {
 
 constexpr int kStack = 64;  // > max depth of a 30-bit LBVH with index tie-break (63)
+// fine cells a side of a bin of the point test's bin index, and the 32-bit
+// words of an entry's fine-cell mask
+constexpr int kFine = 8;
+constexpr int kFineWords = kFine * kFine * kFine / 32;
 
 __device__ __forceinline__ double prune_threshold(const V3& p, double eps2, double scale) {
     double m = scale;
@@ -149,6 +153,14 @@ struct EnvTree {
     const uint4* gslot;   // (cell, first entry, count, -) per hash slot
     uint32_t gshift, gmask;
     const int32_t* glist;
+    // the bin index of the point test (boff == nullptr: none)
+    float blo[3];
+    float binv;
+    int32_t bn[3];
+    const uint32_t* boff;   // first entry per bin (Morton index of its coordinates)
+    const uint32_t* bmask;  // fine-cell mask word w of entry e at bmask[w * bnt + e]
+    const int32_t* bleaf;   // leaf per entry
+    int64_t bnt;            // entries
 };
 
 template <bool FP32>
@@ -182,6 +194,9 @@ static EnvTree env_tree_for(const Surface& S, double eps2) {
     if (S.grid.eps2 != eps2) {
         T.gslot = nullptr;
         T.glist = nullptr;
+        T.boff = nullptr;
+        T.bmask = nullptr;
+        T.bleaf = nullptr;
     }
     return T;
 }
@@ -197,6 +212,15 @@ static EnvTree env_tree(const Surface& S) {
     T.gshift = S.grid.shift;
     T.gmask = S.grid.mask;
     T.glist = S.grid.list;
+    for (int k = 0; k < 3; ++k) {
+        T.blo[k] = S.grid.blo[k];
+        T.bn[k] = S.grid.bn[k];
+    }
+    T.binv = S.grid.binv;
+    T.boff = S.grid.boff;
+    T.bmask = S.grid.bent;
+    T.bleaf = S.grid.bent ? (const int32_t*)(S.grid.bent + kFineWords * S.grid.bnt) : nullptr;
+    T.bnt = S.grid.bnt;
     return T;
 }
 
@@ -455,6 +479,148 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_grid(const double* _
     flush_stats(st, counters, nq);
 }
 
+// ---------------------------------------------------------------------------
+// Test through the bin index: the point's bin and fine cell come from its
+// binary32 coordinates, t = (ph - blo) * binv per axis (round to nearest):
+// bin i = floor(t) and fine cell floor(8 (t - i)) (t - i is exact: t and i
+// are within a factor 2, and x8 is exact), clamped to the grid, so the
+// computed fine index is floor(8 t).  t is within 2^-24 |p| binv (the
+// rounding of p) + 2^-23 |t| (the subtraction and the product) of its exact
+// value (p - blo) binv; inside the grown box |t| / binv is at most its extent
+// (below 2 M + 2 R), so that is a distance of at most 2^-24 |p| + 2^-22 (M +
+// R) <= 2^-21 M per axis, well inside the 2^-17 M of the culling radius R the
+// masks are built for.  A clamped coordinate (outside the grown box) maps to the
+// outer cell, whose cube holds the point's projection onto the box face, no
+// farther from any facet than the point.  So every leaf within the certified
+// culling radius of the point is in its bin's list with its fine-cell bit set,
+// and the point is in iff one of those leaves tests in (in CERT, the
+// certified binary32 bounds with FP64 in the band; else FP64).
+// ---------------------------------------------------------------------------
+// The point's bin (Morton index) and fine cell (fx + 8 fy + 64 fz).
+__device__ __forceinline__ void bin_cell_of(const EnvTree& T, const CertQuery& q, uint32_t& bin,
+                                            int& fine) {
+    uint32_t m = 0;
+    fine = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float t = __fmul_rn(__fsub_rn(q.ph[k], T.blo[k]), T.binv);
+        int i, f;
+        if (!(t > 0.0f)) {   // below the grid, or NaN
+            i = 0;
+            f = 0;
+        } else if (t >= (float)T.bn[k]) {
+            i = T.bn[k] - 1;
+            f = kFine - 1;
+        } else {
+            i = min((int)t, T.bn[k] - 1);
+            f = min((int)(__fsub_rn(t, (float)i) * (float)kFine), kFine - 1);
+        }
+        m |= morton_expand10((uint32_t)i) << (2 - k);
+        fine += f * (k == 0 ? 1 : (k == 1 ? kFine : kFine * kFine));
+    }
+    bin = m;
+}
+
+// The mask words of the bin's entries (the word that holds the point's fine
+// cell) are read first, 32 at a time, as independent loads: the hits form a
+// bit set and only the hit leaves are tested, in entry order.  DEFER (CERT
+// only): a leaf in the certified band is not evaluated here; the point is in
+// when another leaf tests in, and otherwise undecided (2), for the FP64 pass.
+template <bool CERT, bool DEFER = false>
+__device__ __forceinline__ int bins_point_test(const EnvTree& T, const EpsParams& E, const V3& p,
+                                               const CertQuery& q, TravStats& st) {
+    uint32_t bin;
+    int fine;
+    bin_cell_of(T, q, bin, fine);
+    const uint32_t a = __ldg(T.boff + bin), b = __ldg(T.boff + bin + 1);
+    const uint32_t* mw = T.bmask + (int64_t)(fine >> 5) * T.bnt;
+    const uint32_t sh = (uint32_t)fine & 31u;
+    bool band = false;
+    for (uint32_t base = a; base < b; base += 32) {
+        const uint32_t cnt = min(b - base, 32u);
+        uint32_t hits = 0;
+#pragma unroll 8
+        for (uint32_t k = 0; k < cnt; ++k) hits |= ((__ldg(mw + base + k) >> sh) & 1u) << k;
+        while (hits) {
+            const uint32_t k = (uint32_t)(__ffs(hits) - 1);
+            hits &= hits - 1u;
+            const int32_t lf = __ldg(T.bleaf + base + k);
+            if (DEFER) {
+                ++st.facets;
+                const int cls = facet_classify(T.cull, lf, q);
+                if (cls == kFacetIn) return 1;
+                band |= cls == kFacetBand;
+            } else if (CERT ? cert_leaf_within(T.cull, T.tri, lf, p, q, E.eps2, st)
+                            : fp64_leaf_within(T.tri, lf, p, E.eps2, st)) {
+                return 1;
+            }
+        }
+    }
+    return band ? 2 : 0;
+}
+
+template <bool CERT>
+__device__ __forceinline__ bool bins_point_in(const EnvTree& T, const EpsParams& E, const V3& p,
+                                              const CertQuery& q, TravStats& st) {
+    return bins_point_test<CERT>(T, E, p, q, st) == 1;
+}
+
+// recheck: (count, point indices) of the points the certified test left
+// undecided (a leaf in the band and none in), for k_env_points_bins_recheck;
+// nullptr: the band is evaluated in FP64 on the spot.
+template <int BLOCK, int MINB, bool CERT, bool DEFER>
+__global__ void __launch_bounds__(BLOCK, MINB) k_env_points_bins(const double* __restrict__ P,
+                                                           const int32_t* __restrict__ order,
+                                                           int64_t n, EnvTree T, EpsParams E,
+                                                           uint8_t* __restrict__ out,
+                                                           unsigned long long* __restrict__ counters,
+                                                           uint32_t* __restrict__ recheck) {
+    TravStats st;
+    uint32_t nq = 0;
+    const int64_t groups = (n + 31) >> 5;
+    const int64_t warps = (int64_t)gridDim.x * (BLOCK / 32);
+    for (int64_t g = (int64_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5); g < groups;
+         g += warps) {
+        const int64_t i = (g << 5) + (threadIdx.x & 31);
+        if (i < n) {
+            // the points, the order and the answers stream through once
+            // (evict-first), so the bins, entries and facet records stay in L2
+            const int64_t j = order ? (int64_t)__ldcs(order + i) : i;
+            const V3 p{__ldcs(P + 3 * j), __ldcs(P + 3 * j + 1), __ldcs(P + 3 * j + 2)};
+            const CertQuery q = cert_query(p, E, T.scale_hi);
+            const int r = bins_point_test<CERT, DEFER>(T, E, p, q, st);
+            if (DEFER && r == 2) {
+                const uint32_t at = atomicAdd(recheck, 1u);
+                recheck[1 + at] = (uint32_t)j;   // at < n: one entry per point
+            } else {
+                __stcs(out + j, (uint8_t)(r != 1));
+            }
+            ++nq;
+        }
+    }
+    flush_stats(st, counters, nq);
+}
+
+// The undecided points of a deferred certified test, in FP64 (the decision
+// of TW_PRECISION_FP64 for them).
+__global__ void k_env_points_bins_recheck(const double* __restrict__ P,
+                                          const uint32_t* __restrict__ recheck, EnvTree T,
+                                          EpsParams E, uint8_t* __restrict__ out,
+                                          unsigned long long* __restrict__ counters) {
+    TravStats st;
+    const uint32_t cnt = *recheck;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt;
+         k += gridDim.x * blockDim.x) {
+        const int64_t j = recheck[1 + k];
+        const V3 p{P[3 * j], P[3 * j + 1], P[3 * j + 2]};
+        const CertQuery q = cert_query(p, E, T.scale_hi);
+        out[j] = (uint8_t)!bins_point_in<false>(T, E, p, q, st);
+    }
+    // no flush_stats: the counters count each point's certified tests once;
+    // the FP64 evaluations are added per thread
+    if (st.fp64) atomicAdd(counters + kCntEnvFp64, (unsigned long long)st.fp64);
+}
+
 // ---- grid build ----------------------------------------------------------------------
 // Sum over facets of the largest box extent (for the cell size).
 __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
@@ -476,99 +642,64 @@ __global__ void k_grid_mean_extent(const double* __restrict__ tri, int32_t nf,
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
 }
 
-// The cells within reach of every leaf: the cells of its box grown by Rm
-// that a separating-axis test (the three box axes, the triangle's normal and
-// the nine edge x box-axis products) cannot separate from the triangle.  The
-// test uses the cube of half-size cell/2 + Rm + slack around the cell's
-// centre, which holds the ball of radius Rm around every point of the cell
-// (slack = 2^-30 M covers the cell's placement), so a leaf it excludes is
-// farther than Rm from the whole cell.  Counting (fcnt != nullptr): the
-// leaf's count and the total; filling: the (cell << 32 | leaf) pairs from
-// foff[leaf] on.  A leaf whose box spans more than 2^16 cells marks the grid
-// unsuitable (*too_big).  One warp per leaf; the lanes take the box's cells
-// in turn.
-__global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
-                             double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
-                             double Rm, double slack, unsigned long long* __restrict__ total,
-                             uint32_t* __restrict__ fcnt, const uint32_t* __restrict__ foff,
-                             unsigned long long* __restrict__ pairs, int* __restrict__ too_big) {
-    const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (f >= nf) return;   // whole warps
-    double t[9];
+// Binary32 separating-axis test of one leaf against the cells of a regular
+// grid (cell cs from lo, n cells a side): a cell is within reach when no
+// axis (the three box axes, the triangle's normal and the nine edge x
+// box-axis products) separates the triangle from the cube of half-size
+// cs/2 + Rm + slack around the cell's centre, which holds the ball of radius
+// Rm around every point of the cell (slack = 2^-30 M covers the cell's
+// placement), so a leaf it excludes is farther than Rm from the whole cell.
+// Rigorous in binary32: any direction is a valid separating axis, so the
+// binary32 axes themselves are used as exact vectors and only the
+// projections carry rounding.  The vertices relative to t0 (rounded once) and
+// the cell centre relative to t0 (from base = lo - t0 and (x + 1/2) cs) are
+// within 2^-20 L of the exact values (L = 2 (M + the grid's extent) bounds
+// every coordinate and offset), so each projection onto axis a is within
+// |a|_1 2^-19 L; an axis separates only by more than |a|_1 2^-18 L.  Cells no
+// axis separates by that margin are kept (a longer list, never a missing leaf).
+struct SatTri {
+    float basef[3], vf[3][3], ef[3][3], nmf[3];
+    float mL, hf, csf;
+    bool sat_ok;
+
+    __device__ __forceinline__ void init(const double* t, const double* lo, const int32_t* n,
+                                         double cs, double Rm, double slack) {
+        double L = 0.0;
+        for (int k = 0; k < 3; ++k)
+            L = fmax(L, fmax(fabs(lo[k]), fabs(lo[k] + (double)n[k] * cs)) + fabs(t[k]));
+        L = 2.0 * L;
+        mL = (float)ldexp(L, -18) * 1.0001f;
+        hf = (float)(0.5 * cs + Rm + slack) * 1.000001f;
+        csf = (float)cs;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9 * f + k);
-    const double lo[3] = {lo0, lo1, lo2};
-    const int32_t n[3] = {n0, n1, n2};
-    int i0[3], i1[3];
-    for (int k = 0; k < 3; ++k) {
-        const double a = fmin(t[k], fmin(t[3 + k], t[6 + k])) - Rm;
-        const double b = fmax(t[k], fmax(t[3 + k], t[6 + k])) + Rm;
-        double u = floor((a - lo[k]) * inv_c), v = floor((b - lo[k]) * inv_c);
-        u = fmin(fmax(u, 0.0), (double)(n[k] - 1));
-        v = fmin(fmax(v, 0.0), (double)(n[k] - 1));
-        i0[k] = (int)u;
-        i1[k] = (int)v;
-    }
-    const int bx = i1[0] - i0[0] + 1, by = i1[1] - i0[1] + 1;
-    const int64_t box = (int64_t)bx * by * (i1[2] - i0[2] + 1);
-    if (box > 65536) {
-        if (lane == 0) {
-            if (too_big) atomicExch(too_big, 1);
-            if (fcnt) fcnt[f] = 0;
+        for (int k = 0; k < 3; ++k) {
+            basef[k] = (float)(lo[k] - t[k]);
+            vf[0][k] = 0.0f;
+            vf[1][k] = (float)(t[3 + k] - t[k]);
+            vf[2][k] = (float)(t[6 + k] - t[k]);
         }
-        return;
-    }
-    const double cs = 1.0 / inv_c;
-    const double h = 0.5 * cs + Rm + slack;
-    // Binary32 separating-axis test, rigorous: any direction is a valid
-    // separating axis, so the binary32 axes themselves are used as exact
-    // vectors and only the projections carry rounding.  The vertices
-    // relative to t0 (rounded once) and the cell centre relative to t0 (from
-    // base = lo - t0 and (x + 1/2) cs) are within 2^-20 L of the exact values
-    // (L = 2 (M + the grid's extent) bounds every coordinate and offset), so
-    // each projection onto axis a is within |a|_1 2^-19 L; an axis separates
-    // only by more than |a|_1 2^-18 L.  Cells no axis separates by that
-    // margin are kept (a longer list, never a missing leaf).
-    double L = 0.0;
-    for (int k = 0; k < 3; ++k)
-        L = fmax(L, fmax(fabs(lo[k]), fabs(lo[k] + (double)n[k] * cs)) + fabs(t[k]));
-    L = 2.0 * L;
-    const float mL = (float)ldexp(L, -18) * 1.0001f;
-    const float hf = (float)h * 1.000001f;
-    const float csf = (float)cs;
-    const float basef[3] = {(float)(lo0 - t[0]), (float)(lo1 - t[1]), (float)(lo2 - t[2])};
-    float vf[3][3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        vf[0][k] = 0.0f;
-        vf[1][k] = (float)(t[3 + k] - t[k]);
-        vf[2][k] = (float)(t[6 + k] - t[k]);
+        for (int k = 0; k < 3; ++k) {
+            ef[0][k] = vf[1][k] - vf[0][k];
+            ef[1][k] = vf[2][k] - vf[1][k];
+            ef[2][k] = vf[0][k] - vf[2][k];
+        }
+        nmf[0] = ef[0][1] * ef[1][2] - ef[0][2] * ef[1][1];
+        nmf[1] = ef[0][2] * ef[1][0] - ef[0][0] * ef[1][2];
+        nmf[2] = ef[0][0] * ef[1][1] - ef[0][1] * ef[1][0];
+        // 2^-40 <= L < 2^40 and |a|_1 >= 2^-40 keep every product far from
+        // binary32 overflow, and underflow far below the margin (else the
+        // cell is kept)
+        sat_ok = L >= 0x1p-40 && L < 0x1p40;
     }
-    float ef[3][3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        ef[0][k] = vf[1][k] - vf[0][k];
-        ef[1][k] = vf[2][k] - vf[1][k];
-        ef[2][k] = vf[0][k] - vf[2][k];
-    }
-    const float nmf[3] = {ef[0][1] * ef[1][2] - ef[0][2] * ef[1][1],
-                          ef[0][2] * ef[1][0] - ef[0][0] * ef[1][2],
-                          ef[0][0] * ef[1][1] - ef[0][1] * ef[1][0]};
-    // 2^-40 <= L < 2^40 and |a|_1 >= 2^-40 keep every product far from
-    // binary32 overflow, and underflow far below the margin (else the cell
-    // is kept)
-    const bool sat_ok = L >= 0x1p-40 && L < 0x1p40;
-    // true when axis a separates the triangle (projections p) from the cube
-    auto apart = [&](const float* p, float a1) {
+    // true when axis a (|a|_1 = a1) separates the triangle (projections p) from the cube
+    __device__ __forceinline__ bool apart(const float* p, float a1) const {
         if (!(a1 >= 0x1p-40f)) return false;
         const float r = hf * a1 + a1 * mL;
         return fminf(p[0], fminf(p[1], p[2])) > r || fmaxf(p[0], fmaxf(p[1], p[2])) < -r;
-    };
-    // cell q of the box (x fastest): within reach of the leaf?
-    auto within = [&](int q, uint32_t& cell) {
-        const int x = i0[0] + q % bx, y = i0[1] + (q / bx) % by, z = i0[2] + q / (bx * by);
-        cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 + (uint32_t)x;
+    }
+    // cell (x, y, z) within reach of the leaf?
+    __device__ __forceinline__ bool within(int x, int y, int z) const {
         if (!sat_ok) return true;
         const float w[3] = {basef[0] + ((float)x + 0.5f) * csf, basef[1] + ((float)y + 0.5f) * csf,
                             basef[2] + ((float)z + 0.5f) * csf};
@@ -601,6 +732,61 @@ __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double 
             }
         }
         return true;
+    }
+};
+
+// The index range [i0, i1] a side of the cells (cs = 1 / inv_c from lo, n a
+// side) that the leaf's box grown by Rm meets, and their number.
+__device__ __forceinline__ int64_t leaf_cell_box(const double* t, const double* lo,
+                                                 const int32_t* n, double inv_c, double Rm,
+                                                 int* i0, int* i1) {
+    for (int k = 0; k < 3; ++k) {
+        const double a = fmin(t[k], fmin(t[3 + k], t[6 + k])) - Rm;
+        const double b = fmax(t[k], fmax(t[3 + k], t[6 + k])) + Rm;
+        double u = floor((a - lo[k]) * inv_c), v = floor((b - lo[k]) * inv_c);
+        u = fmin(fmax(u, 0.0), (double)(n[k] - 1));
+        v = fmin(fmax(v, 0.0), (double)(n[k] - 1));
+        i0[k] = (int)u;
+        i1[k] = (int)v;
+    }
+    return (int64_t)(i1[0] - i0[0] + 1) * (i1[1] - i0[1] + 1) * (i1[2] - i0[2] + 1);
+}
+
+// The cells within reach of every leaf (SatTri over the cells of its box
+// grown by Rm).  Counting (fcnt != nullptr): the leaf's count and the total;
+// filling: the (cell << 32 | leaf) pairs from foff[leaf] on.  A leaf whose
+// box spans more than 2^16 cells marks the grid unsuitable (*too_big).  One
+// warp per leaf; the lanes take the box's cells in turn.
+__global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
+                             double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
+                             double Rm, double slack, unsigned long long* __restrict__ total,
+                             uint32_t* __restrict__ fcnt, const uint32_t* __restrict__ foff,
+                             unsigned long long* __restrict__ pairs, int* __restrict__ too_big) {
+    const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (f >= nf) return;   // whole warps
+    double t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9 * f + k);
+    const double lo[3] = {lo0, lo1, lo2};
+    const int32_t n[3] = {n0, n1, n2};
+    int i0[3], i1[3];
+    const int64_t box = leaf_cell_box(t, lo, n, inv_c, Rm, i0, i1);
+    if (box > 65536) {
+        if (lane == 0) {
+            if (too_big) atomicExch(too_big, 1);
+            if (fcnt) fcnt[f] = 0;
+        }
+        return;
+    }
+    const int bx = i1[0] - i0[0] + 1, by = i1[1] - i0[1] + 1;
+    SatTri S;
+    S.init(t, lo, n, 1.0 / inv_c, Rm, slack);
+    // cell q of the box (x fastest): within reach of the leaf?
+    auto within = [&](int q, uint32_t& cell) {
+        const int x = i0[0] + q % bx, y = i0[1] + (q / bx) % by, z = i0[2] + q / (bx * by);
+        cell = ((uint32_t)z * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n0 + (uint32_t)x;
+        return S.within(x, y, z);
     };
     const int nbox = (int)box;
     if (fcnt) {
@@ -629,6 +815,96 @@ __global__ void k_grid_cells(const double* __restrict__ tri, int32_t nf, double 
         if (in && at < end) pairs[at] = ((unsigned long long)cell << 32) | (uint32_t)f;
         w += __popc(bal);
     }
+}
+
+// The bins within reach of every leaf, with their fine-cell masks: SatTri
+// over the fine grid (cell cs/8, 8n a side) for the 512 fine cells of each
+// bin of the leaf's grown box (mask word w: fine cells 32 w .. 32 w + 31,
+// lane l taking cell s = 32 w + l = fx + 8 fy + 64 fz); a bin with an empty
+// mask is no entry.  Counting and filling as k_grid_cells; entry at: the key
+// (bin << 32 | leaf; bin: the Morton index of its coordinates), its index in
+// vals and its mask words in masks[w * ntot + at].  A leaf whose box spans
+// more than 4096 bins marks the index unsuitable (*too_big).
+__global__ void k_bin_cells(const double* __restrict__ tri, int32_t nf, double lo0, double lo1,
+                            double lo2, double inv_c, int32_t n0, int32_t n1, int32_t n2,
+                            double Rm, double slack, unsigned long long* __restrict__ total,
+                            uint32_t* __restrict__ fcnt, const uint32_t* __restrict__ foff,
+                            unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals,
+                            uint32_t* __restrict__ masks, int64_t ntot,
+                            int* __restrict__ too_big) {
+    const int64_t f = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (f >= nf) return;   // whole warps
+    double t[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) t[k] = __ldg(tri + 9 * f + k);
+    const double lo[3] = {lo0, lo1, lo2};
+    const int32_t n[3] = {n0, n1, n2};
+    int i0[3], i1[3];
+    const int64_t box = leaf_cell_box(t, lo, n, inv_c, Rm, i0, i1);
+    if (box > 4096) {
+        if (lane == 0) {
+            if (too_big) atomicExch(too_big, 1);
+            if (fcnt) fcnt[f] = 0;
+        }
+        return;
+    }
+    const int bx = i1[0] - i0[0] + 1, by = i1[1] - i0[1] + 1;
+    const int32_t nfine[3] = {kFine * n0, kFine * n1, kFine * n2};
+    SatTri S;
+    S.init(t, lo, nfine, 1.0 / (kFine * inv_c), Rm, slack);
+    uint32_t cnt = 0;
+    uint32_t at = fcnt ? 0u : __ldg(foff + f);
+    const uint32_t end = fcnt ? 0u : __ldg(foff + f + 1);
+    for (int q = 0; q < (int)box; ++q) {
+        const int x = i0[0] + q % bx, y = i0[1] + (q / bx) % by, z = i0[2] + q / (bx * by);
+        uint32_t mine = 0, any = 0;   // lane w keeps word w
+#pragma unroll 1
+        for (int w = 0; w < kFineWords; ++w) {
+            const int c = 32 * w + lane;
+            const unsigned bal = __ballot_sync(
+                0xffffffffu, S.within(kFine * x + c % kFine, kFine * y + (c / kFine) % kFine,
+                                      kFine * z + c / (kFine * kFine)));
+            if (lane == w) mine = bal;
+            any |= bal;
+        }
+        if (any == 0u) continue;
+        if (fcnt) {
+            ++cnt;
+        } else {
+            if (at < end) {
+                if (lane == 0) {
+                    const uint32_t bin = (morton_expand10((uint32_t)x) << 2) |
+                                         (morton_expand10((uint32_t)y) << 1) |
+                                         morton_expand10((uint32_t)z);
+                    keys[at] = ((unsigned long long)bin << 32) | (uint32_t)f;
+                    vals[at] = at;
+                }
+                if (lane < kFineWords) masks[(int64_t)lane * ntot + at] = mine;
+            }
+            ++at;
+        }
+    }
+    if (fcnt && lane == 0) {
+        fcnt[f] = cnt;
+        if (cnt) atomicAdd(total, (unsigned long long)cnt);
+    }
+}
+
+// Sorted (bin << 32 | leaf) keys with the indices of their unsorted entries
+// -> the entries (kFineWords mask-word arrays of n, then the leaves), and the
+// entry count of each bin (zeroed before).
+__global__ void k_bin_split(const unsigned long long* __restrict__ keys,
+                            const uint32_t* __restrict__ src, const uint32_t* __restrict__ masks,
+                            int64_t n, uint32_t* __restrict__ ent, uint32_t* __restrict__ cnt) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = keys[i];
+    const int64_t from = src[i];
+#pragma unroll
+    for (int w = 0; w < kFineWords; ++w) ent[w * n + i] = masks[w * n + from];
+    ent[kFineWords * n + i] = (uint32_t)k;
+    atomicAdd(cnt + (uint32_t)(k >> 32), 1u);
 }
 
 // Sorted pairs -> the cell of each entry and the leaf list.
@@ -687,6 +963,29 @@ __global__ void k_point_bins(const double* __restrict__ P, int64_t n, float lx, 
     bin_rank[i] = make_uint2(bin, atomicAdd(count + bin, 1u));
 }
 
+// The same sort on the bin index's own bins (Morton order of the bin
+// coordinates shifted right by sh): consecutive queries then share a bin and
+// its entries.  The bin coordinates are computed as in bins_point_in.
+__global__ void k_point_bins_idx(const double* __restrict__ P, int64_t n, float lx, float ly,
+                                 float lz, float inv, int32_t n0, int32_t n1, int32_t n2, int sh,
+                                 uint2* __restrict__ bin_rank, uint32_t* __restrict__ count) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float c[3] = {__fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i)), lx), inv),
+                        __fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i + 1)), ly), inv),
+                        __fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i + 2)), lz), inv)};
+    const int32_t nb[3] = {n0, n1, n2};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int v = !(c[k] > 0.0f) ? 0 : (c[k] >= (float)nb[k] ? nb[k] - 1 : min((int)c[k], nb[k] - 1));
+        q[k] = (uint32_t)v >> sh;
+    }
+    const uint32_t bin =
+        (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
+    bin_rank[i] = make_uint2(bin, atomicAdd(count + bin, 1u));
+}
+
 // idx[first of bin + rank] = i, with count holding each bin's first position
 __global__ void k_point_place(const uint2* __restrict__ bin_rank, int64_t n,
                               const uint32_t* __restrict__ first, int32_t* __restrict__ idx) {
@@ -711,6 +1010,7 @@ struct SortLayout {
     int32_t* idx;
     uint32_t* count;
     int64_t nbins;
+    uint32_t* recheck;   // count, then up to n point indices
     void* temp;
     size_t temp_bytes;
 };
@@ -729,6 +1029,7 @@ static SortLayout sort_layout(void* base, int64_t n, int knob) {
     L.bin_rank = (uint2*)q; q += al(8 * (size_t)n);
     L.idx = (int32_t*)q; q += al(4 * (size_t)n);
     L.count = (uint32_t*)q; q += al(4 * (size_t)L.nbins);
+    L.recheck = (uint32_t*)q; q += al(4 * (size_t)n + 4);
     L.temp = q;
     L.temp_bytes = cub_scan_bytes(L.nbins);
     return L;
@@ -738,7 +1039,7 @@ size_t env_sort_scratch_bytes(int64_t n, int knob) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const int64_t nbins = int64_t(1) << (3 * sort_bits(n, knob));
     return al(8 * (size_t)n) + al(4 * (size_t)n) + al(4 * (size_t)nbins) +
-           al(cub_scan_bytes(nbins)) + 256;
+           al(4 * (size_t)n + 4) + al(cub_scan_bytes(nbins)) + 256;
 }
 
 // Batches below this size are traversed in input order (sorting would cost
@@ -752,31 +1053,57 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     if (n <= 0) return;
     const int block = 128;
     const int32_t* order = nullptr;
-    if (sort_scratch && n >= kSortMin && n <= INT32_MAX) {
-        SortLayout L = sort_layout(sort_scratch, n, sort_knob);
-        double sc[3];
-        for (int k = 0; k < 3; ++k) {
-            double ext = S.hi[k] - S.lo[k];
-            sc[k] = ext > 0.0 ? 1.0 / ext : 0.0;
-        }
-        const unsigned nb = (unsigned)((n + 255) / 256);
-        cudaMemsetAsync(L.count, 0, 4 * (size_t)L.nbins, s);
-        k_point_bins<<<nb, 256, 0, s>>>(P, n, (float)S.lo[0], (float)S.lo[1], (float)S.lo[2],
-                                        (float)sc[0], (float)sc[1], (float)sc[2],
-                                        std::ldexp(1.0f, sort_bits(n, sort_knob)),
-                                        L.bin_rank, L.count);
-        size_t tb = L.temp_bytes;
-        cub::DeviceScan::ExclusiveSum(L.temp, tb, L.count, (int)L.nbins, s);
-        k_point_place<<<nb, 256, 0, s>>>(L.bin_rank, n, L.count, L.idx);
-        order = L.idx;
-    }
+    uint32_t* recheck = nullptr;
     const EnvTree T = env_tree_for(S, eps2);
     const EpsParams E = eps_params(eps2);
+    if (sort_scratch && n >= kSortMin && n <= INT32_MAX) {
+        SortLayout L = sort_layout(sort_scratch, n, sort_knob);
+        const unsigned nb = (unsigned)((n + 255) / 256);
+        const int bits = sort_bits(n, sort_knob);
+        if (T.boff) {
+            // on the bin index's own bins (or a coarser Morton prefix of them)
+            const int b = std::min(bits, S.grid.bbits);
+            cudaMemsetAsync(L.count, 0, 4 * ((size_t)1 << (3 * b)), s);
+            k_point_bins_idx<<<nb, 256, 0, s>>>(P, n, T.blo[0], T.blo[1], T.blo[2], T.binv,
+                                                T.bn[0], T.bn[1], T.bn[2], S.grid.bbits - b,
+                                                L.bin_rank, L.count);
+            size_t tb = L.temp_bytes;
+            cub::DeviceScan::ExclusiveSum(L.temp, tb, L.count, 1 << (3 * b), s);
+        } else {
+            double sc[3];
+            for (int k = 0; k < 3; ++k) {
+                double ext = S.hi[k] - S.lo[k];
+                sc[k] = ext > 0.0 ? 1.0 / ext : 0.0;
+            }
+            cudaMemsetAsync(L.count, 0, 4 * (size_t)L.nbins, s);
+            k_point_bins<<<nb, 256, 0, s>>>(P, n, (float)S.lo[0], (float)S.lo[1], (float)S.lo[2],
+                                            (float)sc[0], (float)sc[1], (float)sc[2],
+                                            std::ldexp(1.0f, bits), L.bin_rank, L.count);
+            size_t tb = L.temp_bytes;
+            cub::DeviceScan::ExclusiveSum(L.temp, tb, L.count, (int)L.nbins, s);
+        }
+        k_point_place<<<nb, 256, 0, s>>>(L.bin_rank, n, L.count, L.idx);
+        order = L.idx;
+        recheck = L.recheck;
+    }
     // the tree-walk kernels: at least 6 blocks of 128 threads per SM (85
     // registers), measured best of 1, 6 and 8 on the 10M-point workload (8
     // spills)
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    if (T.gslot && precision == TW_PRECISION_FP32_CERTIFIED) {
+    if (T.boff && precision == TW_PRECISION_FP32_CERTIFIED && recheck) {
+        // no FP64 code in the bulk kernel (64 registers): 8 blocks of 128 per SM
+        cudaMemsetAsync(recheck, 0, 4, s);
+        k_env_points_bins<128, 8, true, true><<<grid_for(n, 128, 32), 128, 0, s>>>(
+            P, order, n, T, E, out, counters, recheck);
+        k_env_points_bins_recheck<<<grid_for(8192, 128, 1), 128, 0, s>>>(P, recheck, T, E, out,
+                                                                         counters);
+    } else if (T.boff && precision == TW_PRECISION_FP32_CERTIFIED) {
+        k_env_points_bins<384, 2, true, false><<<grid_for(n, 384, 6), 384, 0, s>>>(
+            P, order, n, T, E, out, counters, nullptr);
+    } else if (T.boff) {
+        k_env_points_bins<384, 2, false, false><<<grid_for(n, 384, 6), 384, 0, s>>>(
+            P, order, n, T, E, out, counters, nullptr);
+    } else if (T.gslot && precision == TW_PRECISION_FP32_CERTIFIED) {
         // 768 resident threads per SM (85 registers) in every block shape
         switch (point_block) {
         case 256:
@@ -1562,6 +1889,8 @@ __global__ void k_nearest_points(EnvTree T, double eps2, const double* __restric
 void free_env_grid(tw_ctx* c, EnvGrid& G) {
     if (G.slot) dev_free(c, G.slot, G.slot_bytes);
     if (G.list) dev_free(c, G.list, G.list_bytes);
+    if (G.boff) dev_free(c, G.boff, G.boff_bytes);
+    if (G.bent) dev_free(c, G.bent, G.bent_bytes);
     G = EnvGrid{};
 }
 
@@ -1582,9 +1911,136 @@ struct BuildScratch {
 };
 }  // namespace
 
+// The bin index (EnvGrid::boff, bent) of a surface whose grid was just built:
+// bins of side bin_factor x the mean facet extent, but at least 1/250 of the
+// grown box's largest side (at most 256 bins a side).  Leaves it absent when
+// unsuitable (a leaf over more than 4096 bins, more than 2^27 entries).
+static int build_env_bins(tw_ctx* c, Surface& S, const double* blo, const double* bhi,
+                          double mean_ext, double M, double Rm, double bin_factor,
+                          cudaStream_t s) {
+    EnvGrid& g = S.grid;
+    g.bin_factor = bin_factor;   // built for it, or found unsuitable
+    if (!(bin_factor > 0.0)) return TW_OK;
+    const int32_t nf = S.nf;
+    double ext = 0.0;
+    for (int k = 0; k < 3; ++k) ext = std::max(ext, bhi[k] - blo[k] + 2.0 * Rm);
+    double cs = std::max(bin_factor * mean_ext, ext / 250.0);
+    if (!(cs > 0.0) || !std::isfinite(cs)) return TW_OK;
+    int64_t n[3];
+    float lo[3];
+    float inv = 0.0f;
+    for (int iter = 0; iter < 64; ++iter) {
+        inv = (float)(1.0 / cs);
+        int64_t nmax = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double a = blo[k] - Rm;
+            float f = (float)a;
+            if ((double)f > a) f = std::nextafter(f, -INFINITY);
+            lo[k] = f;
+            n[k] = (int64_t)std::floor((bhi[k] + Rm - (double)f) * (double)inv) + 2;
+            nmax = std::max(nmax, n[k]);
+        }
+        if (nmax <= 256) break;
+        cs *= 1.01;
+    }
+    if (std::max(n[0], std::max(n[1], n[2])) > 256) return TW_OK;
+    int bits = 0;
+    while ((int64_t(1) << bits) < std::max(n[0], std::max(n[1], n[2]))) ++bits;
+    const int64_t nmorton = int64_t(1) << (3 * bits);
+    BuildScratch B{c, {}};
+    int st = TW_OK;
+    // acc: [0] entry total, [1] too-big flag
+    unsigned long long* acc = (unsigned long long*)B.get(16, st);
+    if (st != TW_OK) return st;
+    cudaMemsetAsync(acc, 0, 16, s);
+    uint32_t* fcnt = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
+    if (st != TW_OK) return st;
+    uint32_t* foff = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
+    if (st != TW_OK) return st;
+    cudaMemsetAsync(fcnt + nf, 0, 4, s);
+    const int Bk = 256;
+    const int G = (int)(((int64_t)nf * 32 + Bk - 1) / Bk);   // one warp per leaf
+    const double slack = std::ldexp(M, -30);
+    k_bin_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                 (int32_t)n[1], (int32_t)n[2], Rm, slack, acc, fcnt, nullptr,
+                                 nullptr, nullptr, nullptr, 0, (int*)(acc + 1));
+    unsigned long long hacc[2] = {0, 0};
+    cudaMemcpyAsync(hacc, acc, 16, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bin index build");
+    const unsigned long long total = hacc[0];
+    if ((hacc[1] & 0xffffffffULL) != 0 || total == 0 || total > (1ULL << 27)) return TW_OK;
+    const int64_t nt = (int64_t)total;
+    {
+        size_t tbs = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tbs, fcnt, foff, nf + 1, s);
+        void* tmp = B.get(tbs + 16, st);
+        if (st != TW_OK) return st;
+        cub::DeviceScan::ExclusiveSum(tmp, tbs, fcnt, foff, nf + 1, s);
+    }
+    unsigned long long* keys = (unsigned long long*)B.get(8 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    unsigned long long* keys2 = (unsigned long long*)B.get(8 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    uint32_t* vals = (uint32_t*)B.get(4 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    uint32_t* vals2 = (uint32_t*)B.get(4 * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    uint32_t* masks = (uint32_t*)B.get(4 * (size_t)kFineWords * (size_t)nt, st);
+    if (st != TW_OK) return st;
+    k_bin_cells<<<G, Bk, 0, s>>>(S.tri, nf, lo[0], lo[1], lo[2], (double)inv, (int32_t)n[0],
+                                 (int32_t)n[1], (int32_t)n[2], Rm, slack, nullptr, nullptr, foff,
+                                 keys, vals, masks, nt, nullptr);
+    const int key_bits = 32 + 3 * bits;
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, vals2, (int)nt, 0, key_bits,
+                                    s);
+    size_t tb2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb2, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                  (int)(nmorton + 1), s);
+    void* temp = B.get(std::max(tb, tb2) + 16, st);
+    if (st != TW_OK) return st;
+    uint32_t* bcnt = (uint32_t*)B.get(4 * ((size_t)nmorton + 1), st);
+    if (st != TW_OK) return st;
+    cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys2, vals, vals2, (int)nt, 0, key_bits, s);
+    void* offp = nullptr;
+    void* entp = nullptr;
+    const size_t off_bytes = 4 * ((size_t)nmorton + 1),
+                 ent_bytes = 4 * (size_t)(kFineWords + 1) * (size_t)nt;
+    if ((st = dev_alloc(c, off_bytes, &offp)) != TW_OK) return st;
+    if ((st = dev_alloc(c, ent_bytes, &entp)) != TW_OK) {
+        dev_free(c, offp, off_bytes);
+        return st;
+    }
+    cudaMemsetAsync(bcnt, 0, 4 * ((size_t)nmorton + 1), s);
+    k_bin_split<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(keys2, vals2, masks, nt,
+                                                             (uint32_t*)entp, bcnt);
+    cub::DeviceScan::ExclusiveSum(temp, tb2, bcnt, (uint32_t*)offp, (int)(nmorton + 1), s);
+    e = cudaStreamSynchronize(s);   // the scratch is released on return
+    if (e != cudaSuccess) {
+        dev_free(c, offp, off_bytes);
+        dev_free(c, entp, ent_bytes);
+        return cuda_fail(c, e, "bin index build");
+    }
+    for (int k = 0; k < 3; ++k) {
+        g.blo[k] = lo[k];
+        g.bn[k] = (int32_t)n[k];
+    }
+    g.binv = inv;
+    g.bbits = bits;
+    g.boff = (uint32_t*)offp;
+    g.bent = (uint32_t*)entp;
+    g.bnt = nt;
+    g.boff_bytes = off_bytes;
+    g.bent_bytes = ent_bytes;
+    return TW_OK;
+}
+
 int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaStream_t s) {
     if (S.nf <= 0 || !(eps2 >= 0.0)) return TW_OK;
-    if (S.grid.slot && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor) return TW_OK;
+    if (S.grid.slot && S.grid.eps2 == eps2 && S.grid.cell_factor == cell_factor &&
+        S.grid.bin_factor == c->bin_cell)
+        return TW_OK;
     free_env_grid(c, S.grid);
     const int32_t nf = S.nf;
     // bounding box of the facets: the root's two child boxes, or the facet
@@ -1757,7 +2213,7 @@ int build_env_grid(tw_ctx* c, Surface& S, double eps2, double cell_factor, cudaS
     g.cell_factor = cell_factor;
     g.slot_bytes = 16 * H;
     g.list_bytes = 4 * (size_t)nt + 16;
-    return TW_OK;
+    return build_env_bins(c, S, blo, bhi, sum_ext / nf, M, Rm, c->bin_cell, s);
 }
 
 // Point checks of candidate collapses (EdgeCollapser.cpp:286-329): the

@@ -80,6 +80,24 @@ struct EnvGrid {
     double eps2 = -1.0;        // the eps2 it was built for (-1: none)
     double cell_factor = 0.0;  // and the cell-size factor
     size_t slot_bytes = 0, list_bytes = 0;
+    // The bin index of the point test (boff == nullptr: none; the hash grid
+    // serves): cubic bins of side 1/binv from blo, bn per axis (at most 256),
+    // in the Morton order of their coordinates (bits per axis: bbits); the
+    // entries of bin b are boff[b] .. boff[b + 1] - 1 (boff: 2^(3 bbits) + 1
+    // exclusive sums, so the entries of consecutive bins are consecutive),
+    // its leaves in ascending order, each with the 512-bit mask of the bin's
+    // 8x8x8 fine cells whose cube (half-size c/8/2 + R) a separating-axis
+    // test cannot separate from the leaf.  A point tests the leaves whose
+    // mask holds its fine cell: the same leaves a grid of cell c/8 would list.
+    float blo[3] = {0, 0, 0};
+    float binv = 0.0f;
+    int32_t bn[3] = {0, 0, 0};
+    int32_t bbits = 0;
+    uint32_t* boff = nullptr;   // first entry of each bin (Morton index), and the total
+    uint32_t* bent = nullptr;   // mask words 0..15 [16 x nt] (word-major), then the leaves [nt]
+    int64_t bnt = 0;            // entries
+    double bin_factor = 0.0;    // bin side / mean facet extent it was built for
+    size_t boff_bytes = 0, bent_bytes = 0;
 };
 
 struct Surface {
@@ -134,6 +152,7 @@ struct tw_ctx {
     int energy_form = TW_ENERGY_FORM_REFERENCE;   // tw_set_energy_form
     int newton_shape = 5;  // launch shape of the Newton step (tw_newton_autotune)
     double grid_cell = 0.2;   // envelope grid cell size / mean facet extent (TW_TUNE_GRID_CELL)
+    double bin_cell = 0.25;   // point-test bin side / mean facet extent (TW_TUNE_BIN_CELL; 0: none)
     // launch timing of the point-envelope test kernel (TW_TUNE_TIME_KERNELS):
     // a ring of event pairs recorded around each launch
     static constexpr int kTimeRing = 64;
