@@ -217,6 +217,26 @@ def test_smooth_apply_updates_the_resident_mesh(workload):
         assert np.array_equal(now, want)
 
 
+@pytest.mark.timeout(300, method="thread")
+def test_job_errors_on_closed_and_unknown_jobs():
+    """Every job call on a closed or unknown job returns an error (and the server stays
+    usable); none may block.  The thread timeout ends the process if one does."""
+    V, F = syn.icosphere(2)
+    with tw.Server(0, 0, lanes=1) as srv:
+        j = srv.job_open(V, F, 1e-6, 5e-4)
+        srv.job_close(j)
+        for call in (lambda: srv.job_close(j), lambda: srv.job_cancel(j),
+                     lambda: srv.job_close(12345), lambda: srv.job_mesh(j, V),
+                     lambda: srv.job_read_mesh(j, len(V)), lambda: srv.job_boundary(j, V, F)):
+            with pytest.raises(tw.TetWildGpuError) as e:
+                call()
+            assert e.value.code == tw.TW_ERR_ARG
+        k = srv.job_open(V, F, 1e-6, 5e-4)
+        t, out = srv.submit_points(k, syn.envelope_points(V, F, 100, 1e-3, seed=2))
+        srv.wait(t)
+        srv.job_close(k)
+
+
 def test_job_cancel_mid_flight(workload):
     """tw_server_job_cancel: with one lane and a burst of requests queued for job A, the
     cancel completes A's waiting requests with TW_ERR_CANCELLED at once, lets the batches

@@ -196,6 +196,9 @@ static double __longlong_as_double_host(unsigned long long b) {
 namespace {
 
 constexpr int kNumPipe = 3;
+// point chunks of the host-buffer envelope call: the copy of one chunk
+// overlaps the test of the one before, and the last chunk's test is the tail
+constexpr size_t kPointChunkBytes = 96ull << 20;
 
 struct Guard {
     explicit Guard(int dev) { cudaSetDevice(dev); }
@@ -245,9 +248,9 @@ const void* pinned_device_ptr(const void* p) {
     return a.devicePointer;
 }
 
-int64_t chunk_len(int64_t n, size_t bytes_per_item) {
-    // ~96 MB of inputs+outputs per chunk, at least 64k items
-    int64_t c = (int64_t)((96ull << 20) / std::max<size_t>(bytes_per_item, 1));
+int64_t chunk_len(int64_t n, size_t bytes_per_item, size_t chunk_bytes = 96ull << 20) {
+    // ~chunk_bytes of inputs+outputs per chunk, at least 64k items
+    int64_t c = (int64_t)(chunk_bytes / std::max<size_t>(bytes_per_item, 1));
     c = std::max<int64_t>(c, 65536);
     c = (c + 255) & ~int64_t(255);
     return std::min(c, std::max<int64_t>(n, 1));
@@ -730,7 +733,7 @@ int tw_envelope_points(tw_ctx* c, const double* P, int64_t n, int which, uint8_t
     if (c->surf[which].nf == 0) return fail(c, TW_ERR_NO_SURFACE, "no surface uploaded");
     if (n == 0) return TW_OK;
     Guard g(c->device);
-    const int64_t C = chunk_len(n, 25);
+    const int64_t C = chunk_len(n, 25, kPointChunkBytes);
     double* dP[kNumPipe];
     uint8_t* dO[kNumPipe];
     void* dS[kNumPipe];

@@ -144,6 +144,12 @@ int srv_fail(tw_server* s, int code, const std::string& msg) {
     return code;
 }
 
+// the same with s->mu already held by the caller
+int srv_fail_locked(tw_server* s, int code, const std::string& msg) {
+    s->last_error = msg;
+    return code;
+}
+
 size_t lanes_bytes(tw_server* s) {
     size_t b = 0;
     for (auto& L : s->lanes) b += L.bytes;
@@ -567,6 +573,9 @@ int tw_server_job_open(tw_server* s, const double* V, int32_t nv, const int32_t*
     tw_ctx* c = nullptr;
     int st = tw_ctx_create(s->device, 0, &c);
     if (st != TW_OK) return srv_fail(s, st, "tw_ctx_create failed");
+    // no bin index: a job's point queries read the grid's hashed cells, so the
+    // footprint stays within the estimate above
+    c->bin_cell = 0.0;
     st = tw_set_params(c, eps_2, sampling_dist, 15, 20);
     if (st == TW_OK) st = tw_surface_upload(c, V, nv, F, nf, TW_SURFACE_INPUT);
     if (st != TW_OK) {
@@ -578,7 +587,7 @@ int tw_server_job_open(tw_server* s, const double* V, int32_t nv, const int32_t*
     // the estimate admitted it; the bytes the job actually holds decide
     if (s->budget && jobs_bytes(s) + lanes_bytes(s) + c->used > s->budget) {
         tw_ctx_destroy(c);
-        return srv_fail(s, TW_BUSY, "job does not fit in the HBM budget now");
+        return srv_fail_locked(s, TW_BUSY, "job does not fit in the HBM budget now");
     }
     int32_t id = -1;
     for (size_t i = 0; i < s->jobs.size(); ++i)
@@ -606,8 +615,8 @@ int tw_server_job_boundary(tw_server* s, int32_t job, const double* V, int32_t n
     {
         std::unique_lock<std::mutex> lk(s->mu);
         j = job_at(s, job);
-        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
-        if (!drain_job(s, lk, j, 60.0)) return srv_fail(s, TW_ERR_TIMEOUT, "job busy");
+        if (!j) return srv_fail_locked(s, TW_ERR_ARG, "no such job");
+        if (!drain_job(s, lk, j, 60.0)) return srv_fail_locked(s, TW_ERR_TIMEOUT, "job busy");
     }
     int st = tw_surface_upload(j->c, V, nv, F, nf, TW_SURFACE_BOUNDARY);
     return st == TW_OK ? TW_OK : srv_fail(s, st, j->c->last_error);
@@ -621,9 +630,9 @@ int tw_server_job_mesh(tw_server* s, int32_t job, const double* xyz, int32_t nv,
     {
         std::unique_lock<std::mutex> lk(s->mu);
         j = job_at(s, job);
-        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
+        if (!j) return srv_fail_locked(s, TW_ERR_ARG, "no such job");
         if (!drain_job(s, lk, j, timeout_s))
-            return srv_fail(s, TW_ERR_TIMEOUT, "job has requests in flight");
+            return srv_fail_locked(s, TW_ERR_TIMEOUT, "job has requests in flight");
     }
     int st = tw_mesh_upload(j->c, xyz, nv, nullptr);
     return st == TW_OK ? TW_OK : srv_fail(s, st, j->c->last_error);
@@ -636,9 +645,9 @@ int tw_server_job_read_mesh(tw_server* s, int32_t job, double* xyz, double timeo
     {
         std::unique_lock<std::mutex> lk(s->mu);
         j = job_at(s, job);
-        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
+        if (!j) return srv_fail_locked(s, TW_ERR_ARG, "no such job");
         if (!drain_job(s, lk, j, timeout_s))
-            return srv_fail(s, TW_ERR_TIMEOUT, "job has requests in flight");
+            return srv_fail_locked(s, TW_ERR_TIMEOUT, "job has requests in flight");
     }
     tw_ctx* c = j->c;
     if (!c->vx) return srv_fail(s, TW_ERR_NO_MESH, "job has no resident mesh");
@@ -660,9 +669,9 @@ int tw_server_job_close(tw_server* s, int32_t job, double timeout_s) {
     {
         std::unique_lock<std::mutex> lk(s->mu);
         Job* j = job_at(s, job);
-        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
+        if (!j) return srv_fail_locked(s, TW_ERR_ARG, "no such job");
         if (!drain_job(s, lk, j, timeout_s))
-            return srv_fail(s, TW_ERR_TIMEOUT, "job has requests in flight");
+            return srv_fail_locked(s, TW_ERR_TIMEOUT, "job has requests in flight");
         c = j->c;
         j->c = nullptr;
     }
@@ -677,7 +686,7 @@ int tw_server_job_cancel(tw_server* s, int32_t job, double timeout_s) {
     {
         std::unique_lock<std::mutex> lk(s->mu);
         Job* j = job_at(s, job);
-        if (!j) return srv_fail(s, TW_ERR_ARG, "no such job");
+        if (!j) return srv_fail_locked(s, TW_ERR_ARG, "no such job");
         j->cancelling = true;
         // the job's requests still in the queue complete now, cancelled
         const auto now = Clock::now();
@@ -698,7 +707,7 @@ int tw_server_job_cancel(tw_server* s, int32_t job, double timeout_s) {
         // the batches already on a lane finish
         if (!drain_job(s, lk, j, timeout_s)) {
             j->cancelling = false;
-            return srv_fail(s, TW_ERR_TIMEOUT, "job has batches in flight");
+            return srv_fail_locked(s, TW_ERR_TIMEOUT, "job has batches in flight");
         }
         c = j->c;
         j->c = nullptr;
