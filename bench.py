@@ -330,9 +330,13 @@ def run_ours(args):
     T, V, F, P = make_inputs(seed=rank)
     ctx = tw.Context(dev)
     ctx.set_params(EPS * EPS, EPS)
-    # a finer envelope grid than the default 0.2: 4% faster point tests on this
-    # surface for 4x the grid memory (256 MB); results never depend on it
+    # a finer envelope grid than the default 0.2 (4% faster point tests through
+    # the grid's hashed cells, the path of --bin-cell 0, for 4x the grid
+    # memory); the default point test reads the bin index; results never
+    # depend on either
     ctx.set_tuning(tw.Context.TUNE_GRID_CELL, GRID_CELL)
+    if args.bin_cell is not None:
+        ctx.set_tuning(tw.Context.TUNE_BIN_CELL, args.bin_cell)
     ctx.surface_upload(V, F)
     fp64_tflops, fp32_tflops = ctx.probe_peaks()
 
@@ -939,6 +943,9 @@ def main():
                     help="profiling runs may time one mode only (then no benchmark line)")
     ap.add_argument("--tets", type=int, default=N_TETS, help="smaller case for profiling only")
     ap.add_argument("--points", type=int, default=N_POINTS, help="smaller case for profiling only")
+    ap.add_argument("--bin-cell", type=float, default=None,
+                    help="TW_TUNE_BIN_CELL for the step (0: the point test reads the grid's "
+                         "hashed cells instead of the bin index); profiling only")
     args = ap.parse_args()
     set_sizes(args.tets, args.points)
     if args.impl == "reference":
