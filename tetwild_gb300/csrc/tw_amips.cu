@@ -136,14 +136,18 @@ __device__ __forceinline__ void flush_amips_stats(uint32_t ntet, uint32_t nfp64,
 
 // FP64 pass over the tets the binary32 kernels listed (in any order): E (with
 // the calTetQuality_AMIPS sentinel in quality mode), J and H in the context's
-// energy form.  The list length is read on the device.
+// energy form.  The list length is read on the device.  One tet per warp
+// (lane 0): the list is short, and a tet per warp spreads its FP64 work over
+// the SMs' FP64 pipes.
 __global__ void __launch_bounds__(128) k_amips_recheck(
     const double* __restrict__ T, int64_t n, const int32_t* __restrict__ recheck,
     const unsigned long long* __restrict__ nrecheck, double* __restrict__ E,
     double* __restrict__ J, double* __restrict__ H, int qual, int form) {
+    if ((threadIdx.x & 31) != 0) return;
     const int64_t m = (int64_t)*nrecheck;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += stride) {
+    const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < m;
+         k += stride) {
         const int64_t i = recheck[k];
         double t[12], jv[3], hv[9];
 #pragma unroll
@@ -464,8 +468,8 @@ void launch_amips_soa_cert(const double* T, int64_t n, int mode, double* E, doub
                                                    nrecheck);
     }
     if (E || J || H)
-        k_amips_recheck<<<grid_for(n, 128, 1), 128, 0, s>>>(T, n, recheck, nrecheck, E, J, H,
-                                                            qual ? 1 : 0, form);
+        k_amips_recheck<<<grid_for(INT32_MAX, 128, 4), 128, 0, s>>>(T, n, recheck, nrecheck, E,
+                                                                    J, H, qual ? 1 : 0, form);
 }
 
 size_t amips_recheck_scratch_bytes(int64_t n) { return 256 + 4 * (size_t)(n > 0 ? n : 0); }

@@ -161,6 +161,8 @@ struct EnvTree {
     const uint32_t* bmask;  // fine-cell mask word w of entry e at bmask[w * bnt + e]
     const int32_t* bleaf;   // leaf per entry
     int64_t bnt;            // entries
+    const int32_t* bid;     // dense id per bin with entries, -1 for an empty bin
+    int32_t nocc;           // bins with entries
 };
 
 template <bool FP32>
@@ -197,6 +199,8 @@ static EnvTree env_tree_for(const Surface& S, double eps2) {
         T.boff = nullptr;
         T.bmask = nullptr;
         T.bleaf = nullptr;
+        T.bid = nullptr;
+        T.nocc = 0;
     }
     return T;
 }
@@ -221,6 +225,8 @@ static EnvTree env_tree(const Surface& S) {
     T.bmask = S.grid.bent;
     T.bleaf = S.grid.bent ? (const int32_t*)(S.grid.bent + kFineWords * S.grid.bnt) : nullptr;
     T.bnt = S.grid.bnt;
+    T.bid = S.grid.bid;
+    T.nocc = S.grid.nocc;
     return T;
 }
 
@@ -582,15 +588,19 @@ __device__ __forceinline__ bool index_point_in(const EnvTree& T, const EpsParams
     return grid_point_in<CERT>(T, E, valid, p, q, st);
 }
 
+// n_dev (sorted on the dense bin ids): the number of sorted queries, read on
+// the device (the others were decided by the binning pass); else n.
 template <int BLOCK, int MINB, bool CERT, bool DEFER>
 __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_bins(const double* __restrict__ P,
                                                            const int32_t* __restrict__ order,
                                                            int64_t n, EnvTree T, EpsParams E,
                                                            uint8_t* __restrict__ out,
                                                            unsigned long long* __restrict__ counters,
-                                                           uint32_t* __restrict__ recheck) {
+                                                           uint32_t* __restrict__ recheck,
+                                                           const uint32_t* __restrict__ n_dev) {
     TravStats st;
     uint32_t nq = 0;
+    if (n_dev) n = min(n, (int64_t)__ldg(n_dev));
     const int64_t groups = (n + 31) >> 5;
     const int64_t warps = (int64_t)gridDim.x * (BLOCK / 32);
     for (int64_t g = (int64_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5); g < groups;
@@ -616,15 +626,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_bins(const double* _
 }
 
 // The undecided points of a deferred certified test, in FP64 (the decision
-// of TW_PRECISION_FP64 for them).
+// of TW_PRECISION_FP64 for them).  One point per warp (lane 0): the points'
+// leaves take different paths through the FP64 distance, which in one warp
+// would run one after another on the slow FP64 pipe; spread over warps (and
+// SMs) they run side by side.
 __global__ void k_env_points_bins_recheck(const double* __restrict__ P,
                                           const uint32_t* __restrict__ recheck, EnvTree T,
                                           EpsParams E, uint8_t* __restrict__ out,
                                           unsigned long long* __restrict__ counters) {
+    if ((threadIdx.x & 31) != 0) return;
     TravStats st;
     const uint32_t cnt = *recheck;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt;
-         k += gridDim.x * blockDim.x) {
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < cnt; k += warps) {
         const int64_t j = recheck[1 + k];
         const V3 p{P[3 * j], P[3 * j + 1], P[3 * j + 2]};
         const CertQuery q = cert_query(p, E, T.scale_hi);
@@ -921,6 +935,25 @@ __global__ void k_bin_split(const unsigned long long* __restrict__ keys,
     atomicAdd(cnt + (uint32_t)(k >> 32), 1u);
 }
 
+// 1 for a bin with entries, else 0 (boff: nb + 1 exclusive sums).
+__global__ void k_bin_flags(const uint32_t* __restrict__ boff, int64_t nb,
+                            int32_t* __restrict__ flag) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nb) flag[m] = boff[m + 1] > boff[m] ? 1 : 0;
+}
+
+// Exclusive sums of the flags -> the dense id of each bin with entries, -1
+// for the others; *nocc: how many have entries.
+__global__ void k_bin_ids(const uint32_t* __restrict__ boff, int64_t nb, int32_t* __restrict__ bid,
+                          int32_t* __restrict__ nocc) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nb) return;
+    const bool has = boff[m + 1] > boff[m];
+    const int32_t v = bid[m];
+    if (m == nb - 1) *nocc = v + (has ? 1 : 0);
+    bid[m] = has ? v : -1;
+}
+
 // Sorted pairs -> the cell of each entry and the leaf list.
 __global__ void k_grid_split(const unsigned long long* __restrict__ pairs, int64_t n,
                              uint32_t* __restrict__ cells, int32_t* __restrict__ list) {
@@ -1000,12 +1033,49 @@ __global__ void k_point_bins_idx(const double* __restrict__ P, int64_t n, float 
     bin_rank[i] = make_uint2(bin, atomicAdd(count + bin, 1u));
 }
 
+// The same on the dense ids of the bins with entries (bid): a point whose bin
+// has no entry has no leaf within its culling radius, so it is out, decided
+// here (marked 0xffffffff for the placing pass, counted as a query).
+__global__ void k_point_bins_cid(const double* __restrict__ P, int64_t n, float lx, float ly,
+                                 float lz, float inv, int32_t n0, int32_t n1, int32_t n2,
+                                 const int32_t* __restrict__ bid, uint2* __restrict__ bin_rank,
+                                 uint32_t* __restrict__ count, uint8_t* __restrict__ out,
+                                 unsigned long long* __restrict__ counters) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float c[3] = {__fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i)), lx), inv),
+                        __fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i + 1)), ly), inv),
+                        __fmul_rn(__fsub_rn(d2f_rn(__ldcs(P + 3 * i + 2)), lz), inv)};
+    const int32_t nb[3] = {n0, n1, n2};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int v = !(c[k] > 0.0f) ? 0 : (c[k] >= (float)nb[k] ? nb[k] - 1 : min((int)c[k], nb[k] - 1));
+        q[k] = (uint32_t)v;
+    }
+    const uint32_t m =
+        (morton_expand10(q[0]) << 2) | (morton_expand10(q[1]) << 1) | morton_expand10(q[2]);
+    const int32_t id = __ldg(bid + m);
+    const bool empty = id < 0;
+    if (empty) {
+        out[i] = 1;
+        bin_rank[i] = make_uint2(0xffffffffu, 0u);
+    } else {
+        bin_rank[i] = make_uint2((uint32_t)id, atomicAdd(count + id, 1u));
+    }
+    const unsigned act = __activemask();
+    const unsigned dec = __ballot_sync(act, empty);
+    if (dec && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1))
+        atomicAdd(counters + kCntEnvQueries, (unsigned long long)__popc(dec));
+}
+
 // idx[first of bin + rank] = i, with count holding each bin's first position
 __global__ void k_point_place(const uint2* __restrict__ bin_rank, int64_t n,
                               const uint32_t* __restrict__ first, int32_t* __restrict__ idx) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 br = __ldcs(bin_rank + i);
+    if (br.x == 0xffffffffu) return;   // decided by the binning pass
     idx[__ldg(first + br.x) + br.y] = (int32_t)i;
 }
 
@@ -1068,13 +1138,23 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
     const int block = 128;
     const int32_t* order = nullptr;
     uint32_t* recheck = nullptr;
+    const uint32_t* n_dev = nullptr;   // sorted queries, when the binning pass decides some
     const EnvTree T = env_tree_for(S, eps2);
     const EpsParams E = eps_params(eps2);
     if (sort_scratch && n >= kSortMin && n <= INT32_MAX) {
         SortLayout L = sort_layout(sort_scratch, n, sort_knob);
         const unsigned nb = (unsigned)((n + 255) / 256);
         const int bits = sort_bits(n, sort_knob);
-        if (T.boff) {
+        if (T.boff && T.bid && sort_knob == 1 && (int64_t)T.nocc + 1 <= L.nbins) {
+            // on the dense ids of the bins with entries (a 4-byte count each)
+            cudaMemsetAsync(L.count, 0, 4 * ((size_t)T.nocc + 1), s);
+            k_point_bins_cid<<<nb, 256, 0, s>>>(P, n, T.blo[0], T.blo[1], T.blo[2], T.binv,
+                                                T.bn[0], T.bn[1], T.bn[2], T.bid, L.bin_rank,
+                                                L.count, out, counters);
+            size_t tb = L.temp_bytes;
+            cub::DeviceScan::ExclusiveSum(L.temp, tb, L.count, T.nocc + 1, s);
+            n_dev = L.count + T.nocc;
+        } else if (T.boff) {
             // on the bin index's own bins (or a coarser Morton prefix of them)
             const int b = std::min(bits, S.grid.bbits);
             cudaMemsetAsync(L.count, 0, 4 * ((size_t)1 << (3 * b)), s);
@@ -1108,15 +1188,15 @@ void launch_env_points(const Surface& S, const double* P, int64_t n, double eps2
         // no FP64 code in the bulk kernel (64 registers): 8 blocks of 128 per SM
         cudaMemsetAsync(recheck, 0, 4, s);
         k_env_points_bins<128, 8, true, true><<<grid_for(n, 128, 32), 128, 0, s>>>(
-            P, order, n, T, E, out, counters, recheck);
-        k_env_points_bins_recheck<<<grid_for(8192, 128, 1), 128, 0, s>>>(P, recheck, T, E, out,
-                                                                         counters);
+            P, order, n, T, E, out, counters, recheck, n_dev);
+        k_env_points_bins_recheck<<<grid_for(INT32_MAX, 128, 4), 128, 0, s>>>(P, recheck, T, E,
+                                                                             out, counters);
     } else if (T.boff && precision == TW_PRECISION_FP32_CERTIFIED) {
         k_env_points_bins<384, 2, true, false><<<grid_for(n, 384, 6), 384, 0, s>>>(
-            P, order, n, T, E, out, counters, nullptr);
+            P, order, n, T, E, out, counters, nullptr, n_dev);
     } else if (T.boff) {
         k_env_points_bins<384, 2, false, false><<<grid_for(n, 384, 6), 384, 0, s>>>(
-            P, order, n, T, E, out, counters, nullptr);
+            P, order, n, T, E, out, counters, nullptr, n_dev);
     } else if (T.gslot && precision == TW_PRECISION_FP32_CERTIFIED) {
         // 768 resident threads per SM (85 registers) in every block shape
         switch (point_block) {
@@ -1905,6 +1985,7 @@ void free_env_grid(tw_ctx* c, EnvGrid& G) {
     if (G.list) dev_free(c, G.list, G.list_bytes);
     if (G.boff) dev_free(c, G.boff, G.boff_bytes);
     if (G.bent) dev_free(c, G.bent, G.bent_bytes);
+    if (G.bid) dev_free(c, G.bid, G.bid_bytes);
     G = EnvGrid{};
 }
 
@@ -1963,10 +2044,10 @@ static int build_env_bins(tw_ctx* c, Surface& S, const double* blo, const double
     const int64_t nmorton = int64_t(1) << (3 * bits);
     BuildScratch B{c, {}};
     int st = TW_OK;
-    // acc: [0] entry total, [1] too-big flag
-    unsigned long long* acc = (unsigned long long*)B.get(16, st);
+    // acc: [0] entry total, [1] too-big flag, [2] bins with entries
+    unsigned long long* acc = (unsigned long long*)B.get(32, st);
     if (st != TW_OK) return st;
-    cudaMemsetAsync(acc, 0, 16, s);
+    cudaMemsetAsync(acc, 0, 32, s);
     uint32_t* fcnt = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
     if (st != TW_OK) return st;
     uint32_t* foff = (uint32_t*)B.get(4 * ((size_t)nf + 1), st);
@@ -2009,10 +2090,12 @@ static int build_env_bins(tw_ctx* c, Surface& S, const double* blo, const double
     size_t tb = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, vals2, (int)nt, 0, key_bits,
                                     s);
-    size_t tb2 = 0;
+    size_t tb2 = 0, tb3 = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb2, (uint32_t*)nullptr, (uint32_t*)nullptr,
                                   (int)(nmorton + 1), s);
-    void* temp = B.get(std::max(tb, tb2) + 16, st);
+    cub::DeviceScan::ExclusiveSum(nullptr, tb3, (int32_t*)nullptr, (int32_t*)nullptr,
+                                  (int)nmorton, s);
+    void* temp = B.get(std::max(tb, std::max(tb2, tb3)) + 16, st);
     if (st != TW_OK) return st;
     uint32_t* bcnt = (uint32_t*)B.get(4 * ((size_t)nmorton + 1), st);
     if (st != TW_OK) return st;
@@ -2030,12 +2113,31 @@ static int build_env_bins(tw_ctx* c, Surface& S, const double* blo, const double
     k_bin_split<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(keys2, vals2, masks, nt,
                                                              (uint32_t*)entp, bcnt);
     cub::DeviceScan::ExclusiveSum(temp, tb2, bcnt, (uint32_t*)offp, (int)(nmorton + 1), s);
+    // the dense ids of the bins with entries, for the point sort
+    void* bidp = nullptr;
+    const size_t bid_bytes = 4 * (size_t)nmorton;
+    if ((st = dev_alloc(c, bid_bytes, &bidp)) != TW_OK) {
+        dev_free(c, offp, off_bytes);
+        dev_free(c, entp, ent_bytes);
+        return st;
+    }
+    const unsigned gm = (unsigned)((nmorton + 255) / 256);
+    k_bin_flags<<<gm, 256, 0, s>>>((const uint32_t*)offp, nmorton, (int32_t*)bidp);
+    cub::DeviceScan::ExclusiveSum(temp, tb3, (int32_t*)bidp, (int32_t*)bidp, (int)nmorton, s);
+    k_bin_ids<<<gm, 256, 0, s>>>((const uint32_t*)offp, nmorton, (int32_t*)bidp,
+                                 (int32_t*)(acc + 2));
+    int32_t nocc = 0;
+    cudaMemcpyAsync(&nocc, acc + 2, 4, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);   // the scratch is released on return
     if (e != cudaSuccess) {
         dev_free(c, offp, off_bytes);
         dev_free(c, entp, ent_bytes);
+        dev_free(c, bidp, bid_bytes);
         return cuda_fail(c, e, "bin index build");
     }
+    g.bid = (int32_t*)bidp;
+    g.nocc = nocc;
+    g.bid_bytes = bid_bytes;
     for (int k = 0; k < 3; ++k) {
         g.blo[k] = lo[k];
         g.bn[k] = (int32_t)n[k];

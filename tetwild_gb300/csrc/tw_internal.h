@@ -98,6 +98,11 @@ struct EnvGrid {
     int64_t bnt = 0;            // entries
     double bin_factor = 0.0;    // bin side / mean facet extent it was built for
     size_t boff_bytes = 0, bent_bytes = 0;
+    // dense id of each bin with entries (Morton order), -1 for an empty bin:
+    // point queries are sorted on these nocc ids
+    int32_t* bid = nullptr;
+    int32_t nocc = 0;
+    size_t bid_bytes = 0;
 };
 
 struct Surface {
