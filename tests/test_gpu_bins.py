@@ -135,3 +135,33 @@ def test_bin_knob_range(ctx):
         with pytest.raises(tw.TetWildGpuError):
             ctx.set_tuning(tw.Context.TUNE_BIN_CELL, bad)
     ctx.set_tuning(tw.Context.TUNE_BIN_CELL, 0.25)
+
+
+def test_points_in_bins_without_entries(ctx, oracle):
+    """Points inside the sphere and around it, in bins that list no leaf: the binning pass
+    decides them (out) and counts them as queries; the others take the sorted test."""
+    V, F = syn.icosphere(4)
+    eps = 2e-3
+    rng = np.random.default_rng(50)
+
+    def shell(n, r0, r1):
+        d = rng.normal(size=(n, 3))
+        return d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(r0, r1, (n, 1))
+
+    P = np.vstack([syn.envelope_points(V, F, 100_000, eps, seed=51), shell(100_000, 0.0, 0.6),
+                   shell(100_000, 1.3, 3.0)])
+    P = P[rng.permutation(len(P))]
+    want = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
+    ctx.set_params(eps * eps, eps)
+    ctx.surface_upload(V, F)
+    for prec in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
+        ctx.set_precision(prec)
+        ctx.reset_stats()
+        try:
+            got = ctx.envelope_points(P)
+            st = ctx.stats()
+        finally:
+            ctx.set_precision(tw.TW_PRECISION_FP64)
+        assert np.array_equal(got, want), prec
+        assert st["env_queries"] == len(P)
+    assert want.sum() >= 200_000          # every shell point, and part of the near ones
