@@ -136,9 +136,11 @@ __device__ __forceinline__ void flush_amips_stats(uint32_t ntet, uint32_t nfp64,
 
 // FP64 pass over the tets the binary32 kernels listed (in any order): E (with
 // the calTetQuality_AMIPS sentinel in quality mode), J and H in the context's
-// energy form.  The list length is read on the device.  One tet per warp
-// (lane 0): the list is short, and a tet per warp spreads its FP64 work over
-// the SMs' FP64 pipes.
+// energy form.  The list length is read on the device.  The list is short and
+// each evaluation a long chain of binary64 operations on a slow pipe, so the
+// work is spread for latency: in the reference form the energy, the gradient
+// and the Hessian of a tet are three independent evaluations, each taken by
+// its own warp (lane 0); the closed form evaluates all three in one warp.
 __global__ void __launch_bounds__(128) k_amips_recheck(
     const double* __restrict__ T, int64_t n, const int32_t* __restrict__ recheck,
     const unsigned long long* __restrict__ nrecheck, double* __restrict__ E,
@@ -146,18 +148,39 @@ __global__ void __launch_bounds__(128) k_amips_recheck(
     if ((threadIdx.x & 31) != 0) return;
     const int64_t m = (int64_t)*nrecheck;
     const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < m;
-         k += stride) {
+    for (int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < 3 * m;
+         u += stride) {
+        const int64_t k = u / 3;
+        const int part = (int)(u - 3 * k);   // 0: E, 1: J, 2: H
         const int64_t i = recheck[k];
-        double t[12], jv[3], hv[9];
+        double t[12];
 #pragma unroll
         for (int c = 0; c < 12; ++c) t[c] = T[(int64_t)c * n + i];
-        const double e = amips_egh_f(t, J ? jv : nullptr, H ? hv : nullptr, form);
-        if (E) E[i] = qual ? quality_from(orient3d(t, t + 3, t + 6, t + 9), e) : e;
-        if (J)
-            for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
-        if (H)
+        if (form == TW_ENERGY_FORM_CLOSED) {
+            if (part != 0) continue;
+            double jv[3], hv[9];
+            const double e = amips_egh(t, J ? jv : nullptr, H ? hv : nullptr);
+            if (E) E[i] = qual ? quality_from(orient3d(t, t + 3, t + 6, t + 9), e) : e;
+            if (J)
+                for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+            if (H)
+                for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+        } else if (part == 0) {
+            if (E) {
+                const double e = amips_rf_energy(t);
+                E[i] = qual ? quality_from(orient3d(t, t + 3, t + 6, t + 9), e) : e;
+            }
+        } else if (part == 1) {
+            if (J) {
+                double jv[3];
+                amips_rf_jacobian(t, jv);
+                for (int c = 0; c < 3; ++c) J[(int64_t)c * n + i] = jv[c];
+            }
+        } else if (H) {
+            double hv[9];
+            amips_rf_hessian(t, hv);
             for (int c = 0; c < 9; ++c) H[(int64_t)c * n + i] = hv[c];
+        }
     }
 }
 
