@@ -100,7 +100,7 @@ constexpr int kFacetOut = 0;
 constexpr int kFacetIn = 1;
 constexpr int kFacetBand = 2;
 
-// The facet record as seven float4 (from global or shared memory):
+// The facet record as seven float4:
 // ah0 ah1 ah2 al0 | al1 al2 n0 n1 | n2 ne00 ne01 ne02 | ne10 ne11 ne12 ne20 |
 // ne21 ne22 c0 c1 | c2 o0 o1 o2 | len0 len1 len2 ok  (ok == 0: always the band)
 __device__ __forceinline__ int facet_classify_rec(const float4& w0, const float4& w1,
