@@ -492,7 +492,7 @@ def run_ours(args):
                               "(half the FMA flop rate): no FP contraction, one op each"},
         "e2e": e2e,
         "gpu_launches": 6 * args.steps,
-        "gpu_launches_note": "per step: k_amips_soa_cert_bulk, k_amips_recheck, k_point_bins_idx, "
+        "gpu_launches_note": "per step: k_amips_soa_cert_bulk, k_amips_recheck, k_point_bins_cid, "
                              "k_point_place, k_env_points_bins, k_env_points_bins_recheck (+ three "
                              "memsets and a CUB scan of the bin counts)",
         "clocks": cert["clocks"],
