@@ -165,3 +165,29 @@ def test_points_in_bins_without_entries(ctx, oracle):
         assert np.array_equal(got, want), prec
         assert st["env_queries"] == len(P)
     assert want.sum() >= 200_000          # every shell point, and part of the near ones
+
+
+def test_bins_on_both_surfaces_and_eps_change(ctx, oracle):
+    """The input and the boundary surface each get their own index; a new eps2 rebuilds
+    both (an index built for another eps2 is never read)."""
+    V, F = syn.icosphere(4)
+    Vb, Fb = syn.torus(1.0, 0.3, 60, 20)
+    P = np.vstack([syn.envelope_points(V, F, 60_000, 3e-3, seed=52),
+                   syn.envelope_points(Vb, Fb, 60_000, 3e-3, seed=53)])
+    ctx.set_params(1e-6, 1e-3)
+    ctx.surface_upload(V, F, tw.TW_SURFACE_INPUT)
+    ctx.surface_upload(Vb, Fb, tw.TW_SURFACE_BOUNDARY)
+    for eps in (1e-3, 2.5e-3):
+        ctx.set_params(eps * eps, eps)
+        wi = oracle.surface(V, F).points_out(P, eps * eps, nthreads=8)
+        wb = oracle.surface(Vb, Fb).points_out(P, eps * eps, nthreads=8)
+        for prec in (tw.TW_PRECISION_FP64, tw.TW_PRECISION_FP32_CERTIFIED):
+            ctx.set_precision(prec)
+            try:
+                gi = ctx.envelope_points(P, tw.TW_SURFACE_INPUT)
+                gb = ctx.envelope_points(P, tw.TW_SURFACE_BOUNDARY)
+            finally:
+                ctx.set_precision(tw.TW_PRECISION_FP64)
+            assert np.array_equal(gi, wi), (eps, prec)
+            assert np.array_equal(gb, wb), (eps, prec)
+        assert 0 < wi.sum() < len(P) and 0 < wb.sum() < len(P)
