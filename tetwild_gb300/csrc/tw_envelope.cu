@@ -625,8 +625,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_env_points_bins(const double* _
     flush_stats(st, counters, nq);
 }
 
-// The undecided points of a deferred certified test, in FP64 (the decision
-// of TW_PRECISION_FP64 for them).  One point per warp (lane 0): the points'
+// The undecided points of a deferred certified test (the decision of
+// TW_PRECISION_FP64 for them).  One point per warp (lane 0): the points'
 // leaves take different paths through the FP64 distance, which in one warp
 // would run one after another on the slow FP64 pipe; spread over warps (and
 // SMs) they run side by side.
@@ -642,7 +642,9 @@ __global__ void k_env_points_bins_recheck(const double* __restrict__ P,
         const int64_t j = recheck[1 + k];
         const V3 p{P[3 * j], P[3 * j + 1], P[3 * j + 2]};
         const CertQuery q = cert_query(p, E, T.scale_hi);
-        out[j] = (uint8_t)!bins_point_in<false>(T, E, p, q, st);
+        // the certified test again, now evaluating the band in FP64 on the
+        // spot: only the leaves in the band cost a binary64 distance
+        out[j] = (uint8_t)!bins_point_in<true>(T, E, p, q, st);
     }
     // no flush_stats: the counters count each point's certified tests once;
     // the FP64 evaluations are added per thread
