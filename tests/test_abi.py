@@ -180,3 +180,23 @@ def test_header_compiles_for_c_and_cpp_hosts(tmp_path, compiler, std, ext):
     out = subprocess.run(["nm", "-u", str(tmp_path / "u.o")], capture_output=True, text=True,
                          check=True).stdout
     assert sorted(l.split()[-1] for l in out.splitlines() if "tw_" in l) == syms
+
+
+def test_python_constants_match_the_header():
+    """Every integer #define of the header that the binding mirrors (TW_* module
+    constants, Context.TUNE_* knobs) has the header's value."""
+    import tetwild_gb300 as tw
+
+    defines = {m.group(1): int(m.group(2)) for m in
+               re.finditer(r"^#define\s+(TW_\w+)\s+\(?(-?\d+)\)?\s*(?:/\*.*)?$", HEADER.read_text(), re.M)}
+    assert defines, "no integer defines parsed"
+    checked = 0
+    for name, value in defines.items():
+        if name.startswith("TW_TUNE_"):
+            attr = name[len("TW_"):]
+            assert getattr(tw.Context, attr) == value, name
+            checked += 1
+        elif hasattr(tw, name):
+            assert getattr(tw, name) == value, name
+            checked += 1
+    assert checked >= 30, checked
