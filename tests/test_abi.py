@@ -199,4 +199,4 @@ def test_python_constants_match_the_header():
         elif hasattr(tw, name):
             assert getattr(tw, name) == value, name
             checked += 1
-    assert checked >= 30, checked
+    assert checked >= 45, checked

@@ -85,6 +85,17 @@ TW_PRECISION_FP64 = 0
 TW_PRECISION_FP32_CERTIFIED = 1
 TW_ENERGY_FORM_REFERENCE = 0
 TW_ENERGY_FORM_CLOSED = 1
+TW_COLLAPSE_SUCCESS = 0
+TW_COLLAPSE_FLIP = 1
+TW_COLLAPSE_QUALITY = 2
+TW_COLLAPSE_ENVELOP = 3
+TW_SWAP_SUCCESS = 0
+TW_SWAP_FLIP = 1
+TW_SWAP_QUALITY = 2
+TW_SWAP_SIZE = 3
+TW_SWAP_NEEDS_HOST = 4
+TW_NEWTON_SHAPES = 10
+TW_NOALLOC_MAX_TETS = 65536
 
 _STAT_FIELDS = ("exact_orientations", "env_queries", "env_facet_tests", "env_facet_fp64",
                 "amips_tets", "amips_fp64", "env_warp_fallbacks")
